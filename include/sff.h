@@ -1,0 +1,132 @@
+/*
+ * sff.h -- the C ABI of the generalized-Born energy/gradient path, as a
+ * drop-in replacement for the SFF library of dacase/nabc.
+ *
+ * Every declaration here mirrors one in the reference's src/sff/sff.h; the
+ * comment on each gives the reference line it replaces.  The topology struct
+ * keeps the reference's exact field order and types (src/sff/sff.h:40-62) so
+ * that a driver compiled against the reference header (for example
+ * test/tmd.c) links against libsffg.so unchanged.
+ *
+ * Semantics that callers rely on (src/sff/eff.c:2432-2439, sff.c:858-1846):
+ *  - coordinates x and gradients f are double[3*Natom], xyz interleaved;
+ *    f is the gradient dE/dx (md() integrates -f);
+ *  - units are kcal/mol, Angstrom, charges pre-multiplied by 18.2223;
+ *  - mme_init_sff borrows prm, frozen and constrained for the life of the
+ *    session and modifies prm in place (charges scaled by 1/sqrt(dielc),
+ *    screening factors overwritten for gb=7/8);
+ *  - the iter argument of mme: >=0 normal call (pair list rebuilt on the
+ *    first call and whenever iter%nsnb==0, "ff:" line every ntpr),
+ *    -1 verbose energy breakdown, -3 release per-session state,
+ *    -4 force a pair-list rebuild, other negatives quiet with no rebuild;
+ *  - errors in these legacy entry points are fail-stop (message, exit(1)),
+ *    as in the reference; the batched API in sffg.h returns status codes.
+ *
+ * The library is one GPU-resident session: these entry points are not
+ * re-entrant, like the reference's process-global state.
+ */
+#ifndef SFFG_SFF_H
+#define SFFG_SFF_H
+
+#include <stdio.h>
+#include <stddef.h>
+
+#ifndef FALSE
+#define FALSE 0
+#endif
+#ifndef TRUE
+#define TRUE 1
+#endif
+
+typedef int INT_T;
+typedef size_t SIZE_T;
+#define REAL_T double
+typedef char STRING_T;
+typedef FILE FILE_T;
+
+#define NAMESIZE 6
+typedef char NAME_T[NAMESIZE];
+
+/* Topology read from a parm7 file (src/sff/sff.h:40-62, same layout). */
+typedef struct parm {
+  char ititl[81];
+  INT_T IfBox, Nmxrs, IfCap,
+      Natom, Ntypes, Nbonh, Mbona, Ntheth, Mtheta,
+      Nphih, Mphia, Nhparm, Nparm, Nnb, Nres,
+      Nbona, Ntheta, Nphia, Numbnd, Numang, Nptra,
+      Natyp, Nphb, Nat3, Ntype2d, Nttyp, Nspm, Iptres, Nspsol,
+      Ipatm, Natcap, Numextra;
+  NAME_T *AtomNames, *ResNames, *AtomType, *AtomTree;
+  REAL_T *Charges, *Masses, *Rk, *Req, *Tk, *Teq, *Pk, *Pn, *Phase,
+      *Solty, *Cn1, *Cn2, *HB12, *HB10, *Rborn, *Fs;
+  REAL_T Box[4], Cutcap, Xcap, Ycap, Zcap, Fsmax;
+  INT_T *Iac, *Iblo, *Cno, *Ipres, *ExclAt, *TreeJoin,
+      *AtomRes, *BondHAt1, *BondHAt2, *BondHNum, *BondAt1, *BondAt2,
+      *BondNum, *AngleHAt1, *AngleHAt2, *AngleHAt3, *AngleHNum,
+      *AngleAt1, *AngleAt2, *AngleAt3, *AngleNum, *DihHAt1,
+      *DihHAt2, *DihHAt3, *DihHAt4, *DihHNum, *DihAt1, *DihAt2,
+      *DihAt3, *DihAt4, *DihNum, *Boundary, *AtomicNum;
+  INT_T *N14pairs, *N14pairlist;
+  REAL_T *Gvdw, *Scee, *Scnb, *N14sceelist, *N14scnblist;
+  INT_T Nstrand, Ncomplex;
+  INT_T *Ipstrand, *Ipcomplex;
+} PARMSTRUCT_T;
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* Output stream for every printed line; defined by the caller, as in the
+ * reference (src/sff/sff.h:116, test/tmd.c:18). */
+extern FILE *nabout;
+
+/* Option string "key=value, ..." with the reference's grammar
+ * (src/sff/sff.h:139, src/sff/mm_options.l:18-97). Keys prefixed "sffg_"
+ * are this library's own additions. */
+INT_T mm_options(STRING_T *opts);
+
+/* Start a session on prm (src/sff/sff.h:148, src/sff/sff.c:858). */
+INT_T mme_init_sff(PARMSTRUCT_T *prm, INT_T *frozen, INT_T *constrained,
+                   REAL_T *x0, STRING_T *ncname);
+
+/* Energy and gradient; returns the total energy (src/sff/sff.h:141,
+ * src/sff/sff.c:1854 -> eff.c:2442). */
+REAL_T mme(REAL_T *x, REAL_T *f, INT_T *iter);
+
+/* Velocity-Verlet Langevin/Berendsen dynamics driven by func
+ * (src/sff/sff.h:136, src/sff/sff.c:2071). */
+INT_T md(INT_T n, INT_T maxstep, REAL_T *x, REAL_T *f, REAL_T *v,
+         REAL_T (*func)(REAL_T *, REAL_T *, INT_T *));
+
+/* Conjugate-gradient minimisation driven by func (src/sff/sff.h:124,
+ * src/sff/conjgrad.c:34). */
+INT_T conjgrad(REAL_T *x, INT_T *n, REAL_T *f,
+               REAL_T (*func)(REAL_T *, REAL_T *, INT_T *),
+               REAL_T *rmsgrad, REAL_T *dfpred, INT_T *maxiter);
+
+/* Print the timing summary (src/sff/sff.h:149, src/sff/timer.c:71). */
+INT_T mme_timer(void);
+
+/* parm7 reader, writer and release (src/sff/sff.h:178-180, prm.c:584,
+ * prm.c:1997, prm.c:2810). */
+PARMSTRUCT_T *rdparm(STRING_T *name);
+INT_T wrparm(PARMSTRUCT_T *prm, STRING_T *name);
+INT_T free_prm(PARMSTRUCT_T *prm);
+
+/* Amber ASCII restart read/write (src/sff/sff.h:128,163; sff.c:651,733). */
+INT_T getxv(STRING_T *fname, INT_T natom, REAL_T start_time, REAL_T *x,
+            REAL_T *v);
+INT_T putxv(STRING_T *fname, STRING_T *title, INT_T natom, REAL_T start_time,
+            REAL_T *x, REAL_T *v);
+
+/* The serial uniform/Gaussian stream md() draws its Langevin noise from
+ * (src/sff/sff.h:162,165; rand2.c:119-140; gauss2 is rand2.c:125). */
+REAL_T rand2(void);
+REAL_T gauss2(REAL_T *mean, REAL_T *sd);
+INT_T setseed(INT_T *seed);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* SFFG_SFF_H */

@@ -1,0 +1,103 @@
+/*
+ * sffg.h -- the batched and serving API of libsffg (no counterpart in the
+ * reference, which evaluates one process-global system at a time).
+ *
+ * A batch holds many independent systems (conformers or molecules of any
+ * size) resident on one GPU.  One evaluation computes every system's
+ * generalized-Born energy and gradient in a single flattened work queue.
+ * The model options (gb, cut, rgbmax, kappa, epsext, dielc, nsnb) use the
+ * mm_options() grammar and are shared by all systems of a batch.
+ *
+ * Every call returns SFFG_OK (0) or a negative status and never exits the
+ * process; sffg_last_error() describes the most recent failure on the
+ * calling thread.  Streams are passed as void* (a cudaStream_t; NULL is the
+ * legacy default stream).  A handle must not be used from two threads at
+ * once.
+ */
+#ifndef SFFG_SFFG_H
+#define SFFG_SFFG_H
+
+#include <stddef.h>
+
+#include "sff.h"
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define SFFG_OK 0
+#define SFFG_EINVAL (-1)    /* bad argument or option */
+#define SFFG_ENOMEM (-2)    /* device or host allocation failed, or budget exceeded */
+#define SFFG_ECUDA (-3)     /* a CUDA call failed */
+#define SFFG_ESTATE (-4)    /* call not valid in the handle's current state */
+#define SFFG_ENONFINITE (-5) /* non-finite coordinates or energy in a system */
+#define SFFG_ENODEV (-6)    /* no usable CUDA device */
+
+/* Energy components of one system, in the reference's ene[] layout
+ * (src/sff/eff.c:2864-2874): 0 total, 1 vdW, 2 elec, 3 bond, 4 angle,
+ * 5 dihedral, 7 1-4 vdW, 8 1-4 elec, 10 generalized Born. */
+#define SFFG_NENE 13
+
+const char *sffg_last_error(void);
+
+/* ---- synthetic molecules (benchmarks and tests) ------------------------ */
+
+/* A compact self-avoiding chain molecule of natom atoms generated from seed
+ * (see the README of the package for the recipe).  Writes 3*natom
+ * coordinates into x and the realised confining radius into *radius.
+ * Release the topology with free_prm(). */
+PARMSTRUCT_T *sffg_synth_molecule(int natom, unsigned long long seed, double *x,
+                                  double *radius);
+
+/* ---- batches ------------------------------------------------------------ */
+
+typedef struct sffg_batch sffg_batch;
+
+int sffg_batch_create(const char *opts, sffg_batch **out);
+/* Adds a system (topology borrowed only during the call; coordinates x,
+ * 3*Natom doubles; frozen may be NULL).  Returns the system index. */
+int sffg_batch_add_system(sffg_batch *b, PARMSTRUCT_T *prm, const int *frozen, const double *x,
+                          int *sys_index);
+/* Uploads topologies and allocates device state; no systems may be added
+ * afterwards. */
+int sffg_batch_finalize(sffg_batch *b);
+int sffg_batch_num_systems(const sffg_batch *b);
+int sffg_batch_num_atoms(const sffg_batch *b, int sys);
+
+/* Copies coordinates of one system host->device (stream-ordered). */
+int sffg_batch_set_coords(sffg_batch *b, int sys, const double *x, void *stream);
+int sffg_batch_get_coords(sffg_batch *b, int sys, double *x, void *stream);
+/* Energy and gradient of every system.  The pair lists are rebuilt when
+ * rebuild != 0 and on the first evaluation. */
+int sffg_batch_eval(sffg_batch *b, int rebuild, void *stream);
+int sffg_batch_get_energy(sffg_batch *b, int sys, double *ene, void *stream);
+int sffg_batch_get_grad(sffg_batch *b, int sys, double *g, void *stream);
+/* Effective Born radii of the last evaluation, in atom order. */
+int sffg_batch_get_reff(sffg_batch *b, int sys, double *reff, void *stream);
+/* Number of unordered pairs on the current pair lists of one system. */
+long long sffg_batch_num_pairs(sffg_batch *b, int sys);
+
+/* Langevin md() on every system with device Philox noise (the reference's
+ * integrator, src/sff/sff.c:2223-2354, options dt/temp0/gamma_ln/...).
+ * Velocities start at zero unless set with sffg_batch_set_velocities. */
+int sffg_batch_md(sffg_batch *b, int nsteps, void *stream);
+int sffg_batch_set_velocities(sffg_batch *b, int sys, const double *v, void *stream);
+int sffg_batch_get_velocities(sffg_batch *b, int sys, double *v, void *stream);
+
+/* Batched conjgrad() (src/sff/conjgrad.c:34): each system runs its own
+ * copy of the reference's state machine; at most maxiter evaluations.
+ * status[sys] receives the reference's return code (>0 converged after that
+ * many evaluations, -1..-4 as the reference) and energy[sys] the final
+ * energy; either may be NULL. */
+int sffg_batch_cg(sffg_batch *b, int maxiter, double rmsgrad, double dfpred, int *status,
+                  double *energy, void *stream);
+
+/* Device memory the batch holds, in bytes. */
+size_t sffg_batch_device_bytes(const sffg_batch *b);
+int sffg_batch_destroy(sffg_batch *b);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* SFFG_SFFG_H */

@@ -1,0 +1,113 @@
+// Internal declarations shared by the host (C++) and device (CUDA) parts of
+// libsffg.  Nothing here is part of the public ABI (include/sff.h,
+// include/sffg.h).
+#pragma once
+
+#include <cstdint>
+#include <cstdio>
+#include <string>
+#include <vector>
+
+#include "../../include/sff.h"
+#include "../../include/sffg.h"
+
+namespace sffg {
+
+// ---------------------------------------------------------------- options
+// Every key of the reference's option grammar (src/sff/mm_options.l:28-97)
+// with the reference's defaults (src/sff/sff.c:68-199), plus this library's
+// own "sffg_" keys.
+struct Options {
+  double cut = 20.0, cutnp = 10.0, scnb = 2.0, scee = 1.2, rgbmax = 15.0;
+  double hcp_h1 = 15.0, hcp_h2 = 50.0, hcp_h3 = 150.0, dhcp = 0.25;
+  int ntpr = 10, nscm = 0, nsnb = 10, nsnp = 10, ntwx = 0, nchk = 10000, nchk2 = 10000;
+  double dt = 0.001, t = 0.0, tautp = 999999.0, temp0 = 300.0, tempi = 0.0;
+  double vlimit = 10.0, gamma_ln = 0.0, genmass = 10.0, wcons = 0.0, k4d = 0.0;
+  int ntpr_md = 10, zerov = 0, ips = 0, gb = 0, gb_debug = 0, nr_debug = 0, gb2_debug = 0;
+  int gbsa_debug = 0, e_debug = 0, hcp = 0;
+  double epsext = 78.5, kappa = 0.0, surften = 0.005, dradius = 0.5, deltar = 0.5;
+  double rwater = 1.4, alphanp = 0.75, kappanp = 2.227, min_volume = 0.01;
+  int max_set_size = 20, mpi_min_tasks = 8, cull_np_lists = 1, use_lower_tri = 0;
+  int dynamic_loops = 1, blocksize = 8, gbsa = 0, dim = 3, dield = 1, irattle = 0;
+  double dielc = 1.0;
+  // Library keys: noise source for md() ("reference" replays the reference's
+  // serial gauss2 stream on the host; "philox" draws on the device), tile
+  // kernel tuning and CUDA-graph use.
+  int sffg_noise = 0;           // 0 = reference stream, 1 = device Philox
+  unsigned long long sffg_seed = 0x5eedULL;
+  int sffg_graph = 1;           // capture the md/cg step in a CUDA graph
+  int sffg_warps = 8;           // warps per CTA for the pair kernels (0 = tuned)
+  int sffg_verbose = 0;
+};
+
+Options &options();
+FILE *legacy_out();  // the caller's nabout, or stdout
+// Parses an option string into o (echoing accepted items when echo is set).
+// With fail_stop the process exits on a bad item, as the reference does;
+// otherwise -1 is returned and the item copied to *bad.
+int parse_options(const char *opts, Options &o, bool echo, bool fail_stop, std::string *bad);
+
+// ---------------------------------------------------------------- model
+enum GbModel { GB_NONE = 0, GB_HCT = 1, GB_OBC1 = 2, GB_OBC2 = 5, GB_NECK = 7, GB_NECK2 = 8 };
+
+struct ModelParams {
+  int gb = 0;
+  double gboffset = 0.09, gbneckscale = 0.0;
+  double rgbmax = 15.0, cut = 20.0, kappa = 0.0, epsext = 78.5;
+};
+
+// One dihedral term (multi-term dihedrals are expanded into several).
+struct DihTerm {
+  int a, b, c, d;      // atom indices
+  double pk, pn, phase;
+  int chain_next;      // unused after expansion
+};
+
+// Host-side description of one system, derived from a PARMSTRUCT_T and the
+// options exactly as the reference's mme_init_sff (src/sff/sff.c:858-1846).
+struct HostSystem {
+  int natom = 0;
+  double fsmax = 0.0;
+  std::vector<double> q, rborn, fs, alpha, beta, gamma, mass;
+  std::vector<int> neck, type, frozen;
+  int ntypes = 0;
+  std::vector<float> lj_a, lj_b;          // ntypes^2, zero where no 6-12 term
+  std::vector<std::pair<int, int>> excl;  // excluded pairs i<j (Coulomb/LJ only)
+  struct Bond { int a, b; double rk, req; };
+  struct Angle { int a, b, c; double tk, teq; };
+  struct Pair14 { int a, b; double scee, scnb, c12, c6; int pow10; };
+  std::vector<Bond> bonds;
+  std::vector<Angle> angles;
+  std::vector<DihTerm> dihedrals;
+  std::vector<Pair14> pairs14;
+};
+
+ModelParams model_from_options(const Options &o);
+// Builds a HostSystem; prm is read (and, like the reference, modified: the
+// charges are scaled by 1/sqrt(dielc) and Fs overwritten for gb=7/8) only
+// when mutate_prm is true.
+void build_host_system(PARMSTRUCT_T *prm, const int *frozen, const Options &o, bool mutate_prm,
+                       HostSystem &out, ModelParams &mp);
+
+void prm_allocate_arrays(PARMSTRUCT_T *prm);
+void prm_finish_derived(PARMSTRUCT_T *prm, bool newparm);
+
+// ---------------------------------------------------------------- fixed point
+// Scales of the 64-bit fixed-point accumulators.
+constexpr double kForceScale = 4294967296.0;      // 2^32 per kcal/mol/A
+constexpr double kEnergyScale = 4294967296.0;     // 2^32 per kcal/mol
+constexpr double kBornScale = 1099511627776.0;    // 2^40 per 1/A
+constexpr double kSumdScale = 4294967296.0;       // 2^32
+
+// Per-system energy slots kept in fixed point on the device.
+enum EnergySlot { E_EGB = 0, E_EEL, E_EVDW, E_BOND, E_ANGLE, E_DIHED, E_EEL14, E_ENB14, E_NSLOTS };
+
+// ---------------------------------------------------------------- timing
+struct Timers {
+  double init = 0, md = 0, cg = 0, mme = 0, pair = 0, born = 0, bonded = 0, other = 0;
+  long nevals = 0;
+};
+Timers &timers();
+double wall_seconds();
+
+}  // namespace sffg

@@ -1,0 +1,133 @@
+/*
+ * Test infrastructure only: a command-line driver for the reference SFF
+ * library (dacase/nabc src/sff) compiled by oracle/Makefile into oracle/_ref.
+ * It follows the reference's own C drivers (test/tmd.c:20-80) and the NAB
+ * test programs (test/nab/gb5trx.nab:1-16): rdparm, mm_options,
+ * mme_init_sff with nothing frozen or constrained, then one of
+ *
+ *   sp  <out.bin>                     one mme() at iter=-1 (verbose breakdown)
+ *   cg  <maxiter> <dfpred> <rmsgrad> [out.bin]   conjgrad() driven by mme
+ *   md  <nsteps> [out.bin]            md() driven by mme
+ *   time <nevals>                     repeated quiet mme() evaluations
+ *
+ * Coordinates come from a PDB (columns 31-54 of ATOM/HETATM records, the
+ * order the prmtop uses) or an Amber ASCII restart read with getxv().
+ * out.bin holds natom (int32) then E (f64) then x[3N] and g[3N] (f64).
+ */
+#include <stdio.h>
+#include <stdlib.h>
+#include <string.h>
+#include <sys/time.h>
+#include "sff.h"
+
+FILE *nabout;
+int mytaskid = 0;
+int numtasks = 1;
+
+static double now_s(void)
+{
+  struct timeval tv;
+  gettimeofday(&tv, NULL);
+  return (double)tv.tv_sec + 1e-6 * (double)tv.tv_usec;
+}
+
+static int read_pdb(const char *name, int natom, double *x)
+{
+  FILE *fp = fopen(name, "r");
+  char line[256], field[9];
+  int n = 0, k;
+  if (!fp) return -1;
+  while (fgets(line, sizeof(line), fp) && n < natom) {
+    if (strncmp(line, "ATOM", 4) && strncmp(line, "HETATM", 6)) continue;
+    for (k = 0; k < 3; k++) {
+      memcpy(field, line + 30 + 8 * k, 8);
+      field[8] = '\0';
+      x[3 * n + k] = atof(field);
+    }
+    n++;
+  }
+  fclose(fp);
+  return n == natom ? 0 : -1;
+}
+
+static void dump(const char *name, int natom, double e, const double *x, const double *g)
+{
+  FILE *fp;
+  if (!name) return;
+  fp = fopen(name, "wb");
+  if (!fp) { perror(name); exit(2); }
+  fwrite(&natom, sizeof(int), 1, fp);
+  fwrite(&e, sizeof(double), 1, fp);
+  fwrite(x, sizeof(double), 3 * (size_t)natom, fp);
+  fwrite(g, sizeof(double), 3 * (size_t)natom, fp);
+  fclose(fp);
+}
+
+int main(int argc, char **argv)
+{
+  PARMSTRUCT_T *prm;
+  int natom, n3, *frozen, *constrained, iter;
+  double *x, *g, *v, e = 0.0;
+  const char *mode;
+  size_t len;
+
+  nabout = stdout;
+  if (argc < 5) {
+    fprintf(stderr, "usage: %s prmtop coords sp|cg|md|time opts [args]\n", argv[0]);
+    return 2;
+  }
+  prm = rdparm(argv[1]);
+  natom = prm->Natom;
+  n3 = 3 * natom;
+  x = calloc((size_t)n3, sizeof(double));
+  g = calloc((size_t)n3, sizeof(double));
+  v = calloc((size_t)n3, sizeof(double));
+  len = strlen(argv[2]);
+  if (len > 4 && strcmp(argv[2] + len - 4, ".pdb") == 0) {
+    if (read_pdb(argv[2], natom, x)) {
+      fprintf(stderr, "cannot read %d atoms from %s\n", natom, argv[2]);
+      return 2;
+    }
+  } else {
+    getxv(argv[2], natom, 0.0, x, v);
+  }
+  mm_options(argv[4]);
+  frozen = calloc((size_t)natom, sizeof(int));
+  constrained = calloc((size_t)natom, sizeof(int));
+  mme_init_sff(prm, frozen, constrained, NULL, NULL);
+
+  mode = argv[3];
+  if (strcmp(mode, "sp") == 0) {
+    iter = -1;
+    e = mme(x, g, &iter);
+    printf("oracle_total: %.17g\n", e);
+    dump(argc > 5 ? argv[5] : NULL, natom, e, x, g);
+  } else if (strcmp(mode, "cg") == 0) {
+    int maxiter = atoi(argv[5]), ier;
+    double dfpred = atof(argv[6]), rmsgrad = atof(argv[7]);
+    ier = conjgrad(x, &n3, &e, mme, &rmsgrad, &dfpred, &maxiter);
+    printf("conjgrad returns %d\n", ier);
+    printf("oracle_total: %.17g\n", e);
+    dump(argc > 8 ? argv[8] : NULL, natom, e, x, g);
+  } else if (strcmp(mode, "md") == 0) {
+    int nsteps = atoi(argv[5]);
+    md(n3, nsteps, x, g, v, mme);
+    dump(argc > 6 ? argv[6] : NULL, natom, 0.0, x, v);
+  } else if (strcmp(mode, "time") == 0) {
+    int nevals = atoi(argv[5]), k;
+    double t0, t1;
+    iter = -2;
+    e = mme(x, g, &iter); /* first call builds the pair list */
+    t0 = now_s();
+    for (k = 0; k < nevals; k++) {
+      iter = -2;
+      e = mme(x, g, &iter);
+    }
+    t1 = now_s();
+    printf("oracle_time: %d evals %.6f s total %.17g\n", nevals, t1 - t0, e);
+  } else {
+    fprintf(stderr, "unknown mode %s\n", mode);
+    return 2;
+  }
+  return 0;
+}
