@@ -1,0 +1,1248 @@
+// Batch engine: device memory, uploads, list builds, the evaluation
+// pipeline, device-resident md() and conjgrad().
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <cmath>
+#include <cstring>
+#include <map>
+#include <numeric>
+
+#include "engine.h"
+#include "gbneck_tables.h"
+#include "kernels_aux.cuh"
+#include "passes.h"
+
+namespace sffg {
+
+namespace {
+
+template <class T>
+struct DBuf {
+  T *p = nullptr;
+  size_t n = 0;
+  cudaError_t alloc(size_t count) {
+    release();
+    n = count;
+    if (count == 0) return cudaSuccess;
+    return cudaMalloc(&p, count * sizeof(T));
+  }
+  void release() {
+    if (p) cudaFree(p);
+    p = nullptr;
+    n = 0;
+  }
+  size_t bytes() const { return n * sizeof(T); }
+};
+
+// State of one system's conjugate-gradient run (the locals of the
+// reference's conjgrad(), src/sff/conjgrad.c:40-55).
+struct CgState {
+  int done, ret, niter, nfbeg, iterc, nfopt, iterfm, iterrs, iretry, ier, maxiter;
+  double f, fmin, gmin, dfpr, gnew, step, finit, ginit, gsqrd, stmin, gamden, ddspln, stepch, sbound,
+      fch, sum, beta, gama, dgrad, dfpred;
+};
+
+}  // namespace
+
+struct DeviceState {
+  cudaStream_t stream = nullptr;
+  int nsm = 0, grid_pair = 0;
+  // per slot
+  DBuf<float4> pos_hi, pos_lo, gbpar;
+  DBuf<int> param, slot_atom;
+  DBuf<float> q32, reff32, rinv2, sumda32;
+  DBuf<double> rborn64, q64, alpha, beta, gamma, reff64, psi64, chainfac;
+  DBuf<long long> acc_sumi, acc_sd, acc_fx, acc_fy, acc_fz;
+  // per tile
+  DBuf<unsigned> tile_valid;
+  DBuf<int> tile_sys;
+  DBuf<float4> box_lo, box_hi;
+  DBuf<int> excl_tile_start, excl_tile_j, excl_tile_idx;
+  DBuf<unsigned> excl_masks;
+  // per system
+  DBuf<int> sys_active, sys_lj_off, sys_ntypes, sys_tile_end, sys_has_frozen, nonfinite;
+  DBuf<int> sys_natom, sys_atom_off;
+  DBuf<float2> lj;
+  DBuf<long long> energy;
+  DBuf<double> etot;
+  // per atom
+  DBuf<double> x, grad, v, accel, minv, sqrmass;
+  DBuf<int> atom_slot, atom_sys, atom_frozen;
+  // bonded
+  DBuf<int2> bond_atoms;
+  DBuf<double2> bond_par, angle_par;
+  DBuf<int4> angle_atoms, dih_atoms, p14_atoms;
+  DBuf<double4_32a> dih_par, p14_par;
+  // lists and work counters: 0 nitems, 1 nmasks, 2 overflow, 3..5 pass queues
+  DBuf<Item> items;
+  DBuf<unsigned> masks;
+  DBuf<int> counters;
+  // model tables
+  DBuf<float> neck_pos, neck_val;
+  // dynamics
+  DBuf<double> tscal, noise;
+  DBuf<long long> ekin;
+  // minimisation
+  DBuf<double> cg_w;
+  DBuf<CgState> cg_state;
+
+  ~DeviceState() {
+    if (stream) cudaStreamDestroy(stream);
+    // DBuf members release in their own destructors? they are PODs: free here
+    auto rel = [](auto &b) { b.release(); };
+    rel(pos_hi); rel(pos_lo); rel(gbpar); rel(param); rel(slot_atom); rel(q32); rel(reff32);
+    rel(rinv2); rel(sumda32); rel(rborn64); rel(q64); rel(alpha); rel(beta); rel(gamma);
+    rel(reff64); rel(psi64); rel(chainfac); rel(acc_sumi); rel(acc_sd); rel(acc_fx); rel(acc_fy);
+    rel(acc_fz); rel(tile_valid); rel(tile_sys); rel(box_lo); rel(box_hi); rel(excl_tile_start);
+    rel(excl_tile_j); rel(excl_tile_idx); rel(excl_masks); rel(sys_active); rel(sys_lj_off);
+    rel(sys_ntypes); rel(sys_tile_end); rel(sys_has_frozen); rel(nonfinite); rel(sys_natom);
+    rel(sys_atom_off); rel(lj); rel(energy); rel(etot); rel(x); rel(grad); rel(v); rel(accel);
+    rel(minv); rel(sqrmass); rel(atom_slot); rel(atom_sys); rel(atom_frozen); rel(bond_atoms);
+    rel(bond_par); rel(angle_par); rel(angle_atoms); rel(dih_atoms); rel(p14_atoms); rel(dih_par);
+    rel(p14_par); rel(items); rel(masks); rel(counters); rel(neck_pos); rel(neck_val); rel(tscal);
+    rel(noise); rel(ekin); rel(cg_w); rel(cg_state);
+  }
+};
+
+#define SFFG_CK(call)                                                               \
+  do {                                                                              \
+    cudaError_t e_ = (call);                                                        \
+    if (e_ != cudaSuccess) {                                                        \
+      last_error = std::string(#call) + ": " + cudaGetErrorString(e_);              \
+      return SFFG_ECUDA;                                                            \
+    }                                                                               \
+  } while (0)
+
+Batch::Batch(const Options &opts) : opts_(opts), mp_(model_from_options(opts)) {}
+
+Batch::~Batch() = default;
+
+int Batch::add_system(PARMSTRUCT_T *prm, const int *frozen, const double *x, bool mutate_prm) {
+  if (finalized_) {
+    last_error = "add_system after finalize";
+    return SFFG_ESTATE;
+  }
+  if (!prm || !x || prm->Natom <= 0) {
+    last_error = "add_system: null topology or coordinates";
+    return SFFG_EINVAL;
+  }
+  HostSystem hs;
+  ModelParams mp;
+  build_host_system(prm, frozen, opts_, mutate_prm, hs, mp);
+  SystemInfo si;
+  si.natom = hs.natom;
+  si.atom_off = natom_total_;
+  si.fsmax = hs.fsmax;
+  si.frozen = hs.frozen;
+  si.mass = hs.mass;
+  si.ntypes = hs.ntypes;
+  for (int f : hs.frozen) si.has_frozen |= f != 0;
+  for (auto &d : hs.dihedrals) {
+    const bool usual = !(std::fabs(d.phase - 3.142) > 0.01 && std::fabs(d.phase) > 0.01);
+    const int m = static_cast<int>(std::fabs(d.pn));
+    if (usual && (m < 1 || m > 6)) {
+      last_error = "bad value for Pn in a dihedral";
+      return SFFG_EINVAL;
+    }
+  }
+  natom_total_ += hs.natom;
+  x0_.emplace_back(x, x + 3 * hs.natom);
+  host_.push_back(std::move(hs));
+  sys_.push_back(std::move(si));
+  return static_cast<int>(sys_.size()) - 1;
+}
+
+namespace {
+
+// Morton (Z-order) code of a point quantised to 10 bits per axis.
+uint32_t spread10(uint32_t v) {
+  v &= 0x3ff;
+  v = (v | (v << 16)) & 0x030000FF;
+  v = (v | (v << 8)) & 0x0300F00F;
+  v = (v | (v << 4)) & 0x030C30C3;
+  v = (v | (v << 2)) & 0x09249249;
+  return v;
+}
+
+}  // namespace
+
+int Batch::finalize() {
+  if (finalized_) return SFFG_OK;
+  if (sys_.empty()) {
+    last_error = "finalize: no systems";
+    return SFFG_EINVAL;
+  }
+  int dev = 0;
+  if (cudaGetDevice(&dev) != cudaSuccess) {
+    last_error = "no CUDA device";
+    return SFFG_ENODEV;
+  }
+  d_.reset(new DeviceState());
+  SFFG_CK(cudaStreamCreateWithFlags(&d_->stream, cudaStreamNonBlocking));
+  SFFG_CK(cudaDeviceGetAttribute(&d_->nsm, cudaDevAttrMultiProcessorCount, dev));
+  // slot and tile layout
+  int slot = 0, tile = 0;
+  for (auto &s : sys_) {
+    s.slot_off = slot;
+    s.tile_off = tile;
+    s.ntile = (s.natom + 31) / 32;
+    slot += s.ntile * 32;
+    tile += s.ntile;
+  }
+  nslot_ = slot;
+  ntile_ = tile;
+  const int rc = upload();
+  if (rc) return rc;
+  finalized_ = true;
+  return SFFG_OK;
+}
+
+int Batch::upload() {
+  DeviceState &d = *d_;
+  const int nsys = num_systems();
+  std::vector<int> slot_atom(nslot_, -1), param(nslot_, 0), tile_sys(ntile_, 0);
+  std::vector<unsigned> tile_valid(ntile_, 0u);
+  std::vector<float> q32(nslot_, 0.f);
+  std::vector<float4> gbpar(nslot_, make_float4(1.f, 0.f, 1.f, 1.f));
+  std::vector<double> rb64(nslot_, 1.0), q64(nslot_, 0.0), al(nslot_, 0.0), be(nslot_, 0.0), ga(nslot_, 0.0);
+  std::vector<int> atom_slot(natom_total_), atom_sys(natom_total_), atom_frozen(natom_total_);
+  std::vector<double> x(3 * static_cast<size_t>(natom_total_)), minv(3 * static_cast<size_t>(natom_total_)),
+      sqrmass(3 * static_cast<size_t>(natom_total_));
+  std::vector<int> sys_tile_end(nsys), sys_has_frozen(nsys), sys_ntypes(nsys), sys_lj_off(nsys),
+      sys_natom(nsys), sys_atom_off(nsys);
+  std::vector<float2> lj;
+  std::map<std::vector<float>, int> lj_dedupe;
+  std::vector<int> excl_tile_start(ntile_ + 1, 0);
+  std::vector<std::vector<std::pair<int, int>>> excl_by_tile(ntile_);
+  std::vector<unsigned> excl_masks;
+  std::vector<int2> bond_atoms;
+  std::vector<double2> bond_par, angle_par;
+  std::vector<int4> angle_atoms, dih_atoms, p14_atoms;
+  std::vector<double4_32a> dih_par, p14_par;
+  const double off = mp_.gboffset;
+  for (int s = 0; s < nsys; s++) {
+    const SystemInfo &si = sys_[s];
+    const HostSystem &hs = host_[s];
+    const std::vector<double> &xs = x0_[s];
+    const int n = si.natom;
+    // spatial order: Morton code of the initial coordinates
+    double lo[3] = {1e300, 1e300, 1e300}, hi[3] = {-1e300, -1e300, -1e300};
+    for (int i = 0; i < n; i++)
+      for (int k = 0; k < 3; k++) {
+        lo[k] = std::min(lo[k], xs[3 * i + k]);
+        hi[k] = std::max(hi[k], xs[3 * i + k]);
+      }
+    double ext = std::max({hi[0] - lo[0], hi[1] - lo[1], hi[2] - lo[2], 1e-6});
+    std::vector<std::pair<uint32_t, int>> key(n);
+    for (int i = 0; i < n; i++) {
+      uint32_t c[3];
+      for (int k = 0; k < 3; k++) {
+        double u = (xs[3 * i + k] - lo[k]) / ext;
+        if (!(u >= 0.0)) u = 0.0;
+        c[k] = static_cast<uint32_t>(std::min(1023.0, u * 1023.0));
+      }
+      key[i] = {spread10(c[0]) | (spread10(c[1]) << 1) | (spread10(c[2]) << 2), i};
+    }
+    std::sort(key.begin(), key.end());
+    std::vector<int> local_slot(n);
+    for (int k = 0; k < n; k++) local_slot[key[k].second] = k;
+    for (int i = 0; i < n; i++) {
+      const int sl = si.slot_off + local_slot[i];
+      const int a = si.atom_off + i;
+      slot_atom[sl] = a;
+      atom_slot[a] = sl;
+      atom_sys[a] = s;
+      atom_frozen[a] = hs.frozen[i];
+      const double rho = hs.rborn[i] - off;
+      gbpar[sl] = make_float4(static_cast<float>(rho), static_cast<float>(hs.fs[i] * rho),
+                              static_cast<float>(hs.rborn[i]), static_cast<float>(1.0 / rho));
+      param[sl] = (hs.type[i] & 0xffff) | (hs.neck[i] << 16) | (hs.frozen[i] ? (1 << 24) : 0);
+      q32[sl] = static_cast<float>(hs.q[i]);
+      q64[sl] = hs.q[i];
+      rb64[sl] = hs.rborn[i];
+      al[sl] = hs.alpha[i];
+      be[sl] = hs.beta[i];
+      ga[sl] = hs.gamma[i];
+      for (int k = 0; k < 3; k++) {
+        x[3 * static_cast<size_t>(a) + k] = xs[3 * i + k];
+        minv[3 * static_cast<size_t>(a) + k] = 1.0 / hs.mass[i];
+        sqrmass[3 * static_cast<size_t>(a) + k] = 1.0 / std::sqrt(1.0 / hs.mass[i]);
+      }
+    }
+    for (int t = 0; t < si.ntile; t++) {
+      const int T = si.tile_off + t;
+      tile_sys[T] = s;
+      const int cnt = std::min(32, n - 32 * t);
+      tile_valid[T] = cnt >= 32 ? 0xffffffffu : ((1u << cnt) - 1u);
+    }
+    sys_tile_end[s] = si.tile_off + si.ntile;
+    sys_has_frozen[s] = si.has_frozen;
+    sys_ntypes[s] = hs.ntypes;
+    sys_natom[s] = n;
+    sys_atom_off[s] = si.atom_off;
+    {
+      std::vector<float> keyv(hs.lj_a);
+      keyv.insert(keyv.end(), hs.lj_b.begin(), hs.lj_b.end());
+      keyv.push_back(static_cast<float>(hs.ntypes));
+      auto it = lj_dedupe.find(keyv);
+      if (it == lj_dedupe.end()) {
+        const int o = static_cast<int>(lj.size());
+        for (size_t k = 0; k < hs.lj_a.size(); k++) lj.push_back(make_float2(hs.lj_a[k], hs.lj_b[k]));
+        it = lj_dedupe.emplace(keyv, o).first;
+      }
+      sys_lj_off[s] = it->second;
+    }
+    // exclusion masks by tile pair: row = lane of the lower tile's atom
+    std::map<std::pair<int, int>, int> pair_idx;
+    for (auto &e : hs.excl) {
+      int si1 = si.slot_off + local_slot[e.first], si2 = si.slot_off + local_slot[e.second];
+      int t1 = si1 >> 5, t2 = si2 >> 5, l1 = si1 & 31, l2 = si2 & 31;
+      if (t1 > t2 || (t1 == t2 && l1 > l2)) {
+        std::swap(t1, t2);
+        std::swap(l1, l2);
+      }
+      auto key2 = std::make_pair(t1, t2);
+      auto it = pair_idx.find(key2);
+      if (it == pair_idx.end()) {
+        const int idx = static_cast<int>(excl_masks.size() / 32);
+        excl_masks.resize(excl_masks.size() + 32, 0u);
+        it = pair_idx.emplace(key2, idx).first;
+        excl_by_tile[t1].push_back({t2, idx});
+      }
+      excl_masks[static_cast<size_t>(it->second) * 32 + l1] |= 1u << l2;
+    }
+    const int ao = si.atom_off;
+    for (auto &b : hs.bonds) {
+      bond_atoms.push_back(make_int2(ao + b.a, ao + b.b));
+      bond_par.push_back(make_double2(b.rk, b.req));
+    }
+    for (auto &a : hs.angles) {
+      angle_atoms.push_back(make_int4(ao + a.a, ao + a.b, ao + a.c, 0));
+      angle_par.push_back(make_double2(a.tk, a.teq));
+    }
+    for (auto &t : hs.dihedrals) {
+      dih_atoms.push_back(make_int4(ao + t.a, ao + t.b, ao + t.c, ao + t.d));
+      dih_par.push_back(make_double4_32a(t.pk, t.pn, t.phase, 0.0));
+    }
+    for (auto &p : hs.pairs14) {
+      p14_atoms.push_back(make_int4(ao + p.a, ao + p.b, p.pow10, 0));
+      // q_i * (q_j * scee), the reference's cgi * cgj (eff.c:1123-1125)
+      p14_par.push_back(make_double4_32a(hs.q[p.a] * (hs.q[p.b] * p.scee), p.c12, p.c6, p.scnb));
+    }
+  }
+  std::vector<int> excl_tile_j, excl_tile_idx;
+  for (int T = 0; T < ntile_; T++) {
+    excl_tile_start[T] = static_cast<int>(excl_tile_j.size());
+    for (auto &e : excl_by_tile[T]) {
+      excl_tile_j.push_back(e.first);
+      excl_tile_idx.push_back(e.second);
+    }
+  }
+  excl_tile_start[ntile_] = static_cast<int>(excl_tile_j.size());
+  // list capacities: every tile pair of a system could be listed
+  long long cap = 0;
+  for (auto &s : sys_) cap += static_cast<long long>(s.ntile) * (s.ntile + 1) / 2;
+  if (cap > (1LL << 31) - 64) {
+    last_error = "batch too large for one pair list";
+    return SFFG_ENOMEM;
+  }
+  // masks are needed only for tile pairs straddling the cutoff
+  long long mcap = 0;
+  for (int s = 0; s < nsys; s++) {
+    const std::vector<double> &xs = x0_[s];
+    double lo[3] = {1e300, 1e300, 1e300}, hi[3] = {-1e300, -1e300, -1e300};
+    for (int i = 0; i < sys_[s].natom; i++)
+      for (int k = 0; k < 3; k++) {
+        lo[k] = std::min(lo[k], xs[3 * i + k]);
+        hi[k] = std::max(hi[k], xs[3 * i + k]);
+      }
+    const double diag = std::sqrt((hi[0] - lo[0]) * (hi[0] - lo[0]) + (hi[1] - lo[1]) * (hi[1] - lo[1]) +
+                                  (hi[2] - lo[2]) * (hi[2] - lo[2]));
+    if (sys_[s].has_frozen || diag + 20.0 > mp_.cut)
+      mcap += static_cast<long long>(sys_[s].ntile) * (sys_[s].ntile + 1) / 2;
+  }
+  auto up = [&](auto &buf, const auto &vec) -> cudaError_t {
+    cudaError_t e = buf.alloc(vec.size());
+    if (e != cudaSuccess || vec.empty()) return e;
+    return cudaMemcpy(buf.p, vec.data(), vec.size() * sizeof(vec[0]), cudaMemcpyHostToDevice);
+  };
+  SFFG_CK(up(d.slot_atom, slot_atom));
+  SFFG_CK(up(d.param, param));
+  SFFG_CK(up(d.q32, q32));
+  SFFG_CK(up(d.gbpar, gbpar));
+  SFFG_CK(up(d.rborn64, rb64));
+  SFFG_CK(up(d.q64, q64));
+  SFFG_CK(up(d.alpha, al));
+  SFFG_CK(up(d.beta, be));
+  SFFG_CK(up(d.gamma, ga));
+  SFFG_CK(up(d.tile_sys, tile_sys));
+  SFFG_CK(up(d.tile_valid, tile_valid));
+  SFFG_CK(up(d.sys_tile_end, sys_tile_end));
+  SFFG_CK(up(d.sys_has_frozen, sys_has_frozen));
+  SFFG_CK(up(d.sys_ntypes, sys_ntypes));
+  SFFG_CK(up(d.sys_lj_off, sys_lj_off));
+  SFFG_CK(up(d.sys_natom, sys_natom));
+  SFFG_CK(up(d.sys_atom_off, sys_atom_off));
+  SFFG_CK(up(d.lj, lj));
+  SFFG_CK(up(d.excl_tile_start, excl_tile_start));
+  SFFG_CK(up(d.excl_tile_j, excl_tile_j));
+  SFFG_CK(up(d.excl_tile_idx, excl_tile_idx));
+  SFFG_CK(up(d.excl_masks, excl_masks));
+  SFFG_CK(up(d.atom_slot, atom_slot));
+  SFFG_CK(up(d.atom_sys, atom_sys));
+  SFFG_CK(up(d.atom_frozen, atom_frozen));
+  SFFG_CK(up(d.x, x));
+  SFFG_CK(up(d.minv, minv));
+  SFFG_CK(up(d.sqrmass, sqrmass));
+  SFFG_CK(up(d.bond_atoms, bond_atoms));
+  SFFG_CK(up(d.bond_par, bond_par));
+  SFFG_CK(up(d.angle_atoms, angle_atoms));
+  SFFG_CK(up(d.angle_par, angle_par));
+  SFFG_CK(up(d.dih_atoms, dih_atoms));
+  SFFG_CK(up(d.dih_par, dih_par));
+  SFFG_CK(up(d.p14_atoms, p14_atoms));
+  SFFG_CK(up(d.p14_par, p14_par));
+  std::vector<float> npos(441), nval(441);
+  for (int i = 0; i < 441; i++) {
+    npos[i] = static_cast<float>(sffg_neck_max_pos[i]);
+    nval[i] = static_cast<float>(sffg_neck_max_val[i]);
+  }
+  SFFG_CK(up(d.neck_pos, npos));
+  SFFG_CK(up(d.neck_val, nval));
+  std::vector<int> ones(nsys, 1);
+  SFFG_CK(up(d.sys_active, ones));
+  SFFG_CK(d.nonfinite.alloc(nsys));
+  SFFG_CK(d.pos_hi.alloc(nslot_));
+  SFFG_CK(d.pos_lo.alloc(nslot_));
+  SFFG_CK(d.reff32.alloc(nslot_));
+  SFFG_CK(d.rinv2.alloc(nslot_));
+  SFFG_CK(d.sumda32.alloc(nslot_));
+  SFFG_CK(d.reff64.alloc(nslot_));
+  SFFG_CK(d.psi64.alloc(nslot_));
+  SFFG_CK(d.chainfac.alloc(nslot_));
+  SFFG_CK(d.acc_sumi.alloc(nslot_));
+  SFFG_CK(d.acc_sd.alloc(nslot_));
+  SFFG_CK(d.acc_fx.alloc(nslot_));
+  SFFG_CK(d.acc_fy.alloc(nslot_));
+  SFFG_CK(d.acc_fz.alloc(nslot_));
+  SFFG_CK(d.box_lo.alloc(ntile_));
+  SFFG_CK(d.box_hi.alloc(ntile_));
+  SFFG_CK(d.energy.alloc(static_cast<size_t>(nsys) * 8));
+  SFFG_CK(d.etot.alloc(nsys));
+  SFFG_CK(d.grad.alloc(3 * static_cast<size_t>(natom_total_)));
+  SFFG_CK(d.v.alloc(3 * static_cast<size_t>(natom_total_)));
+  SFFG_CK(d.accel.alloc(3 * static_cast<size_t>(natom_total_)));
+  SFFG_CK(cudaMemset(d.v.p, 0, d.v.bytes()));
+  SFFG_CK(cudaMemset(d.accel.p, 0, d.accel.bytes()));
+  SFFG_CK(cudaMemset(d.nonfinite.p, 0, d.nonfinite.bytes()));
+  SFFG_CK(d.items.alloc(static_cast<size_t>(cap)));
+  SFFG_CK(d.masks.alloc(static_cast<size_t>(std::max<long long>(mcap, 1)) * 32));
+  SFFG_CK(d.counters.alloc(8));
+  SFFG_CK(cudaMemset(d.counters.p, 0, d.counters.bytes()));
+  SFFG_CK(d.tscal.alloc(nsys));
+  SFFG_CK(d.ekin.alloc(nsys));
+  std::vector<double> onesd(nsys, 1.0);
+  SFFG_CK(cudaMemcpy(d.tscal.p, onesd.data(), nsys * sizeof(double), cudaMemcpyHostToDevice));
+  d.grid_pair = d.nsm * pair_blocks_per_sm();
+  return SFFG_OK;
+}
+
+size_t Batch::device_bytes() const {
+  if (!d_) return 0;
+  const DeviceState &d = *d_;
+  size_t b = 0;
+  b += d.pos_hi.bytes() + d.pos_lo.bytes() + d.gbpar.bytes() + d.param.bytes() + d.slot_atom.bytes();
+  b += d.q32.bytes() + d.reff32.bytes() + d.rinv2.bytes() + d.sumda32.bytes() + d.rborn64.bytes();
+  b += d.q64.bytes() + d.alpha.bytes() + d.beta.bytes() + d.gamma.bytes() + d.reff64.bytes();
+  b += d.psi64.bytes() + d.chainfac.bytes() + d.acc_sumi.bytes() + d.acc_sd.bytes() + d.acc_fx.bytes();
+  b += d.acc_fy.bytes() + d.acc_fz.bytes() + d.items.bytes() + d.masks.bytes() + d.x.bytes();
+  b += d.grad.bytes() + d.v.bytes() + d.accel.bytes() + d.minv.bytes() + d.sqrmass.bytes();
+  b += d.excl_masks.bytes() + d.cg_w.bytes() + d.noise.bytes();
+  b += d.bond_par.bytes() + d.angle_par.bytes() + d.dih_par.bytes() + d.p14_par.bytes();
+  return b;
+}
+
+double *Batch::d_coords() { return d_ ? d_->x.p : nullptr; }
+double *Batch::d_grad() { return d_ ? d_->grad.p : nullptr; }
+void *Batch::default_stream() { return d_ ? d_->stream : nullptr; }
+
+static cudaStream_t pick(DeviceState &d, void *stream) {
+  return stream ? static_cast<cudaStream_t>(stream) : d.stream;
+}
+
+int Batch::set_coords(int s, const double *x, void *stream) {
+  if (!finalized_ || s < 0 || s >= num_systems()) return SFFG_EINVAL;
+  const SystemInfo &si = sys_[s];
+  SFFG_CK(cudaMemcpyAsync(d_->x.p + 3 * static_cast<size_t>(si.atom_off), x, 3 * sizeof(double) * si.natom,
+                          cudaMemcpyHostToDevice, pick(*d_, stream)));
+  return SFFG_OK;
+}
+
+static int copy_out(Batch &b, DeviceState &d, double *dev, int s, double *host, int per_atom,
+                    void *stream, std::string &err) {
+  const SystemInfo &si = b.system(s);
+  cudaStream_t st = pick(d, stream);
+  cudaError_t e = cudaMemcpyAsync(host, dev + static_cast<size_t>(per_atom) * si.atom_off,
+                                  per_atom * sizeof(double) * si.natom, cudaMemcpyDeviceToHost, st);
+  if (e == cudaSuccess) e = cudaStreamSynchronize(st);
+  if (e != cudaSuccess) {
+    err = cudaGetErrorString(e);
+    return SFFG_ECUDA;
+  }
+  return SFFG_OK;
+}
+
+int Batch::get_coords(int s, double *x, void *stream) {
+  if (!finalized_ || s < 0 || s >= num_systems()) return SFFG_EINVAL;
+  return copy_out(*this, *d_, d_->x.p, s, x, 3, stream, last_error);
+}
+
+int Batch::get_grad(int s, double *g, void *stream) {
+  if (!finalized_ || s < 0 || s >= num_systems()) return SFFG_EINVAL;
+  return copy_out(*this, *d_, d_->grad.p, s, g, 3, stream, last_error);
+}
+
+int Batch::set_velocities(int s, const double *v, void *stream) {
+  if (!finalized_ || s < 0 || s >= num_systems()) return SFFG_EINVAL;
+  const SystemInfo &si = sys_[s];
+  SFFG_CK(cudaMemcpyAsync(d_->v.p + 3 * static_cast<size_t>(si.atom_off), v, 3 * sizeof(double) * si.natom,
+                          cudaMemcpyHostToDevice, pick(*d_, stream)));
+  return SFFG_OK;
+}
+
+int Batch::get_velocities(int s, double *v, void *stream) {
+  if (!finalized_ || s < 0 || s >= num_systems()) return SFFG_EINVAL;
+  return copy_out(*this, *d_, d_->v.p, s, v, 3, stream, last_error);
+}
+
+int Batch::get_reff(int s, double *reff, void *stream) {
+  if (!finalized_ || s < 0 || s >= num_systems()) return SFFG_EINVAL;
+  const SystemInfo &si = sys_[s];
+  std::vector<double> r(static_cast<size_t>(si.ntile) * 32);
+  cudaStream_t st = pick(*d_, stream);
+  SFFG_CK(cudaMemcpyAsync(r.data(), d_->reff64.p + si.slot_off, r.size() * sizeof(double), cudaMemcpyDeviceToHost, st));
+  std::vector<int> sa(r.size());
+  SFFG_CK(cudaMemcpyAsync(sa.data(), d_->slot_atom.p + si.slot_off, sa.size() * sizeof(int), cudaMemcpyDeviceToHost, st));
+  SFFG_CK(cudaStreamSynchronize(st));
+  for (size_t k = 0; k < r.size(); k++)
+    if (sa[k] >= 0) reff[sa[k] - si.atom_off] = r[k];
+  return SFFG_OK;
+}
+
+static void ene_from_fixed(const long long *e, double *ene) {
+  const double k = 1.0 / kEnergyScale;
+  for (int i = 0; i < 13; i++) ene[i] = 0.0;
+  ene[1] = e[E_EVDW] * k;
+  ene[2] = e[E_EEL] * k;
+  ene[3] = e[E_BOND] * k;
+  ene[4] = e[E_ANGLE] * k;
+  ene[5] = e[E_DIHED] * k;
+  ene[7] = e[E_ENB14] * k;
+  ene[8] = e[E_EEL14] * k;
+  ene[10] = e[E_EGB] * k;
+  for (int i = 1; i <= 12; i++) ene[0] += ene[i];
+}
+
+int Batch::get_energy(int s, double *ene, void *stream) {
+  if (!finalized_ || s < 0 || s >= num_systems()) return SFFG_EINVAL;
+  long long e[8];
+  cudaStream_t st = pick(*d_, stream);
+  SFFG_CK(cudaMemcpyAsync(e, d_->energy.p + 8 * s, sizeof(e), cudaMemcpyDeviceToHost, st));
+  SFFG_CK(cudaStreamSynchronize(st));
+  ene_from_fixed(e, ene);
+  return SFFG_OK;
+}
+
+int Batch::get_all_energies(std::vector<double> &out, void *stream) {
+  if (!finalized_) return SFFG_ESTATE;
+  const int nsys = num_systems();
+  std::vector<long long> e(8 * static_cast<size_t>(nsys));
+  cudaStream_t st = pick(*d_, stream);
+  SFFG_CK(cudaMemcpyAsync(e.data(), d_->energy.p, e.size() * sizeof(long long), cudaMemcpyDeviceToHost, st));
+  SFFG_CK(cudaStreamSynchronize(st));
+  out.resize(13 * static_cast<size_t>(nsys));
+  for (int s = 0; s < nsys; s++) ene_from_fixed(&e[8 * s], &out[13 * s]);
+  return SFFG_OK;
+}
+
+DevTables make_tables(DeviceState &d, const ModelParams &mp, double fsmax, int queue) {
+  DevTables t;
+  t.pos_hi = d.pos_hi.p;
+  t.pos_lo = d.pos_lo.p;
+  t.gbpar = d.gbpar.p;
+  t.param = d.param.p;
+  t.reff32 = d.reff32.p;
+  t.rinv2 = d.rinv2.p;
+  t.sumda32 = d.sumda32.p;
+  t.tile_valid = d.tile_valid.p;
+  t.tile_sys = d.tile_sys.p;
+  t.box_lo = d.box_lo.p;
+  t.box_hi = d.box_hi.p;
+  t.sys_active = d.sys_active.p;
+  t.sys_lj_off = d.sys_lj_off.p;
+  t.sys_ntypes = d.sys_ntypes.p;
+  t.lj = d.lj.p;
+  t.items = d.items.p;
+  t.nitems = d.counters.p + 0;
+  t.masks = d.masks.p;
+  t.excl_masks = d.excl_masks.p;
+  t.counter = d.counters.p + queue;
+  t.acc_sumi = d.acc_sumi.p;
+  t.acc_sd = d.acc_sd.p;
+  t.acc_fx = d.acc_fx.p;
+  t.acc_fy = d.acc_fy.p;
+  t.acc_fz = d.acc_fz.p;
+  t.energy = d.energy.p;
+  t.born.rgbmax = static_cast<float>(mp.rgbmax);
+  t.born.rgbmax1i = static_cast<float>(1.0 / mp.rgbmax);
+  t.born.rgbmax2i = static_cast<float>(1.0 / (mp.rgbmax * mp.rgbmax));
+  t.born.cutoff2 = static_cast<float>((mp.rgbmax + fsmax) * (mp.rgbmax + fsmax));
+  t.pair.kappa_s = static_cast<float>(mp.kappa * kKscale);
+  t.pair.inv_epsext = static_cast<float>(1.0 / mp.epsext);
+  t.pair.dielfac0 = static_cast<float>(1.0 - 1.0 / mp.epsext);
+  t.neck_scale = static_cast<float>(mp.gbneckscale);
+  t.neck_pos = d.neck_pos.p;
+  t.neck_val = d.neck_val.p;
+  return t;
+}
+
+int Batch::build_lists(void *stream) {
+  DeviceState &d = *d_;
+  cudaStream_t st = pick(d, stream);
+  for (int attempt = 0; attempt < 4; attempt++) {
+    SFFG_CK(cudaMemsetAsync(d.counters.p, 0, 3 * sizeof(int), st));
+    ListArgs a;
+    a.pos_hi = d.pos_hi.p;
+    a.pos_lo = d.pos_lo.p;
+    a.box_lo = d.box_lo.p;
+    a.box_hi = d.box_hi.p;
+    a.x = d.x.p;
+    a.slot_atom = d.slot_atom.p;
+    a.param = d.param.p;
+    a.tile_valid = d.tile_valid.p;
+    a.tile_sys = d.tile_sys.p;
+    a.sys_tile_end = d.sys_tile_end.p;
+    a.sys_has_frozen = d.sys_has_frozen.p;
+    a.sys_active = d.sys_active.p;
+    a.excl_tile_start = d.excl_tile_start.p;
+    a.excl_tile_j = d.excl_tile_j.p;
+    a.excl_tile_idx = d.excl_tile_idx.p;
+    a.ntile = ntile_;
+    a.cut2f = static_cast<float>(mp_.cut * mp_.cut);
+    a.cut2 = mp_.cut * mp_.cut;
+    a.items = d.items.p;
+    a.nitems = d.counters.p + 0;
+    a.capacity = static_cast<int>(d.items.n);
+    a.masks = d.masks.p;
+    a.nmasks = d.counters.p + 1;
+    a.mask_capacity = static_cast<int>(d.masks.n / 32);
+    a.overflow = d.counters.p + 2;
+    const int threads = 128;
+    const long long warps = ntile_;
+    const int blocks = static_cast<int>((warps * 32 + threads - 1) / threads);
+    k_build_list<<<blocks, threads, 0, st>>>(a);
+    SFFG_CK(cudaGetLastError());
+    int c[3];
+    SFFG_CK(cudaMemcpyAsync(c, d.counters.p, sizeof(c), cudaMemcpyDeviceToHost, st));
+    SFFG_CK(cudaStreamSynchronize(st));
+    if (!c[2]) {
+      have_list_ = true;
+      return SFFG_OK;
+    }
+    // overflow: grow the mask store (items are sized for the worst case)
+    size_t want = std::max<size_t>(static_cast<size_t>(c[1]) + 1024, d.masks.n / 32 * 2);
+    want = std::min<size_t>(want, d.items.n);
+    SFFG_CK(d.masks.alloc(want * 32));
+  }
+  last_error = "pair list build did not fit";
+  return SFFG_ENOMEM;
+}
+
+int Batch::eval(bool rebuild, void *stream) {
+  if (!finalized_) {
+    last_error = "eval before finalize";
+    return SFFG_ESTATE;
+  }
+  return run_eval(rebuild || !have_list_, stream);
+}
+
+int Batch::run_eval(bool rebuild, void *stream) {
+  DeviceState &d = *d_;
+  cudaStream_t st = pick(d, stream);
+  const int nsys = num_systems();
+  SFFG_CK(cudaMemsetAsync(d.counters.p + 3, 0, 3 * sizeof(int), st));
+  SFFG_CK(cudaMemsetAsync(d.energy.p, 0, d.energy.bytes(), st));
+  k_pack<<<(nslot_ + 255) / 256, 256, 0, st>>>(d.x.p, d.slot_atom.p, d.q32.p, d.tile_valid.p, nslot_, d.pos_hi.p,
+                                               d.pos_lo.p, d.box_lo.p, d.box_hi.p, d.acc_sumi.p, d.acc_fx.p,
+                                               d.acc_fy.p, d.acc_fz.p, d.nonfinite.p, d.tile_sys.p);
+  SFFG_CK(cudaGetLastError());
+  if (rebuild) {
+    const int rc = build_lists(st);
+    if (rc) return rc;
+  }
+  double fsmax = 0.0;
+  for (auto &s : sys_) fsmax = std::max(fsmax, s.fsmax);
+  // bonded and 1-4 terms (FP64)
+  BondedArgs ba;
+  ba.x = d.x.p;
+  ba.atom_slot = d.atom_slot.p;
+  ba.atom_sys = d.atom_sys.p;
+  ba.acc_fx = d.acc_fx.p;
+  ba.acc_fy = d.acc_fy.p;
+  ba.acc_fz = d.acc_fz.p;
+  ba.energy = d.energy.p;
+  ba.sys_active = d.sys_active.p;
+  auto blocks = [](size_t n) { return static_cast<int>((n + 127) / 128); };
+  if (d.bond_atoms.n) k_bonds<<<blocks(d.bond_atoms.n), 128, 0, st>>>(ba, d.bond_atoms.p, d.bond_par.p, static_cast<int>(d.bond_atoms.n));
+  if (d.angle_atoms.n) k_angles<<<blocks(d.angle_atoms.n), 128, 0, st>>>(ba, d.angle_atoms.p, d.angle_par.p, static_cast<int>(d.angle_atoms.n));
+  if (d.dih_atoms.n) k_dihedrals<<<blocks(d.dih_atoms.n), 128, 0, st>>>(ba, d.dih_atoms.p, d.dih_par.p, static_cast<int>(d.dih_atoms.n));
+  if (d.p14_atoms.n) k_pairs14<<<blocks(d.p14_atoms.n), 128, 0, st>>>(ba, d.p14_atoms.p, d.p14_par.p, static_cast<int>(d.p14_atoms.n));
+  SFFG_CK(cudaGetLastError());
+  // pass 1
+  const bool neck = mp_.gb == 7 || mp_.gb == 8;
+  {
+    DevTables t = make_tables(d, mp_, fsmax, 3);
+    launch_born(neck, d.grid_pair, st, t);
+    SFFG_CK(cudaGetLastError());
+  }
+  // Born radii, diagonal terms
+  {
+    FinishArgs f;
+    f.acc_sumi = d.acc_sumi.p;
+    f.acc_sd = d.acc_sd.p;
+    f.energy = d.energy.p;
+    f.slot_atom = d.slot_atom.p;
+    f.tile_sys = d.tile_sys.p;
+    f.sys_active = d.sys_active.p;
+    f.param = d.param.p;
+    f.rborn64 = d.rborn64.p;
+    f.q64 = d.q64.p;
+    f.alpha = d.alpha.p;
+    f.beta = d.beta.p;
+    f.gamma = d.gamma.p;
+    f.reff64 = d.reff64.p;
+    f.psi64 = d.psi64.p;
+    f.chainfac = d.chainfac.p;
+    f.reff32 = d.reff32.p;
+    f.rinv2 = d.rinv2.p;
+    f.nslot = nslot_;
+    f.gb = mp_.gb;
+    f.gboffset = mp_.gboffset;
+    f.kappa = mp_.kappa;
+    f.epsext = mp_.epsext;
+    k_born_finish<<<(nslot_ + 255) / 256, 256, 0, st>>>(f);
+    SFFG_CK(cudaGetLastError());
+  }
+  // pass 2
+  {
+    DevTables t = make_tables(d, mp_, fsmax, 4);
+    launch_gbpair(mp_.kappa != 0.0, d.grid_pair, st, t);
+    SFFG_CK(cudaGetLastError());
+  }
+  k_chain_prep<<<(nslot_ + 255) / 256, 256, 0, st>>>(d.acc_sd.p, d.chainfac.p, d.param.p, d.slot_atom.p,
+                                                     d.sumda32.p, nslot_);
+  // pass 3
+  {
+    DevTables t = make_tables(d, mp_, fsmax, 5);
+    launch_chain(neck, d.grid_pair, st, t);
+    SFFG_CK(cudaGetLastError());
+  }
+  k_gather_grad<<<(natom_total_ + 255) / 256, 256, 0, st>>>(d.acc_fx.p, d.acc_fy.p, d.acc_fz.p, d.atom_slot.p,
+                                                            d.atom_frozen.p, d.atom_sys.p, d.sys_active.p,
+                                                            d.grad.p, natom_total_);
+  k_energy_total<<<(nsys + 127) / 128, 128, 0, st>>>(d.energy.p, d.etot.p, nsys);
+  SFFG_CK(cudaGetLastError());
+  timers().nevals++;
+  return SFFG_OK;
+}
+
+long long Batch::num_pairs(int s) {
+  // Count listed pairs of system s from the device list (diagnostic path).
+  if (!finalized_ || !have_list_) return -1;
+  DeviceState &d = *d_;
+  int c[2];
+  if (cudaMemcpy(c, d.counters.p, sizeof(c), cudaMemcpyDeviceToHost) != cudaSuccess) return -1;
+  std::vector<Item> items(c[0]);
+  std::vector<unsigned> masks(static_cast<size_t>(c[1]) * 32);
+  std::vector<unsigned> valid(ntile_);
+  std::vector<int> tsys(ntile_);
+  cudaMemcpy(items.data(), d.items.p, items.size() * sizeof(Item), cudaMemcpyDeviceToHost);
+  if (!masks.empty()) cudaMemcpy(masks.data(), d.masks.p, masks.size() * sizeof(unsigned), cudaMemcpyDeviceToHost);
+  cudaMemcpy(valid.data(), d.tile_valid.p, valid.size() * sizeof(unsigned), cudaMemcpyDeviceToHost);
+  cudaMemcpy(tsys.data(), d.tile_sys.p, tsys.size() * sizeof(int), cudaMemcpyDeviceToHost);
+  long long n = 0;
+  for (auto &it : items) {
+    if (tsys[it.x] != s) continue;
+    for (int l = 0; l < 32; l++) {
+      unsigned row = it.z < 0 ? valid[it.y] : masks[static_cast<size_t>(it.z) * 32 + l];
+      if (!((valid[it.x] >> l) & 1u)) row = 0;
+      if (it.x == it.y) row &= l < 31 ? (0xffffffffu << (l + 1)) : 0u;
+      n += __builtin_popcount(row);
+    }
+  }
+  return n;
+}
+
+// ------------------------------------------------------------------ md
+
+__global__ void k_md_tscal(const long long *ekin, double *tscal, double *ekin_out, int nsys, double ekin0_per_dof,
+                           const double *rndf, double dttp, double c_ave_factor, int apply) {
+  const int s = blockIdx.x * blockDim.x + threadIdx.x;
+  if (s >= nsys) return;
+  double ek = 0.5 * static_cast<double>(ekin[s]) * (1.0 / 4294967296.0) * c_ave_factor;
+  if (ekin_out) ekin_out[s] = ek;
+  if (apply) {
+    const double ekin0 = ekin0_per_dof * rndf[s];
+    tscal[s] = ek > 0.01 ? sqrt(1. + dttp * (ekin0 / ek - 1.)) : 1.0;
+  }
+}
+
+static void md_args(Batch &b, DeviceState &d, const Options &o, int natom_total, MdArgs &a, double &c_ave) {
+  const double boltz2 = 9.93595e-4;
+  const double dtx = o.dt * 20.455, dt5 = 0.5 * dtx, gammai = o.gamma_ln / 20.455;
+  a.x = d.x.p;
+  a.v = d.v.p;
+  a.accel = d.accel.p;
+  a.grad = d.grad.p;
+  a.minv = d.minv.p;
+  a.sqrmass = d.sqrmass.p;
+  a.atom_frozen = d.atom_frozen.p;
+  a.atom_sys = d.atom_sys.p;
+  a.sys_active = d.sys_active.p;
+  a.noise = nullptr;
+  a.tscal = d.tscal.p;
+  a.ekin = d.ekin.p;
+  a.n3 = 3 * natom_total;
+  a.dtx = dtx;
+  a.dt5 = dt5;
+  a.c_explic = 1.0 - gammai * dt5;
+  a.c_implic = 1.0 / (1.0 + gammai * dt5);
+  a.sdfac = std::sqrt(4.0 * gammai * boltz2 * o.temp0 / dtx);
+  a.vlimit = o.vlimit;
+  a.gammai = gammai;
+  a.seed = o.sffg_seed;
+  a.step = 0;
+  c_ave = gammai > 0.0 ? 1.0 + gammai * dt5 : 1.0;
+  (void)b;
+}
+
+// Uploads one step's worth of reference-stream draws (coordinate order,
+// frozen atoms skipped) for every system.
+static int upload_noise(Batch &b, DeviceState &d, Batch::NoiseFn noise, void *ctx, cudaStream_t st,
+                        std::vector<double> &h) {
+  const int nsys = b.num_systems();
+  const size_t n3 = 3 * static_cast<size_t>(b.total_atoms());
+  if (d.noise.n != n3 && d.noise.alloc(n3) != cudaSuccess) return SFFG_ENOMEM;
+  h.assign(n3, 0.0);
+  std::vector<double> draws;
+  for (int s = 0; s < nsys; s++) {
+    const SystemInfo &si = b.system(s);
+    int cnt = 0;
+    for (int i = 0; i < 3 * si.natom; i++) cnt += si.frozen[i / 3] ? 0 : 1;
+    draws.resize(cnt);
+    noise(ctx, s, cnt, draws.data());
+    int k = 0;
+    for (int i = 0; i < 3 * si.natom; i++)
+      if (!si.frozen[i / 3]) h[3 * static_cast<size_t>(si.atom_off) + i] = draws[k++];
+  }
+  cudaError_t e = cudaMemcpyAsync(d.noise.p, h.data(), n3 * sizeof(double), cudaMemcpyHostToDevice, st);
+  if (e == cudaSuccess) e = cudaStreamSynchronize(st);  // h is reused by the next step
+  return e == cudaSuccess ? SFFG_OK : SFFG_ECUDA;
+}
+
+int Batch::md_begin(bool rebuild, NoiseFn noise, void *noise_ctx, void *stream) {
+  if (!finalized_) return SFFG_ESTATE;
+  DeviceState &d = *d_;
+  cudaStream_t st = pick(d, stream);
+  MdArgs a;
+  double c_ave;
+  md_args(*this, d, opts_, natom_total_, a, c_ave);
+  int rc = run_eval(rebuild || !have_list_, st);
+  if (rc) return rc;
+  std::vector<double> h;
+  if (noise && a.gammai != 0.0) {
+    if ((rc = upload_noise(*this, d, noise, noise_ctx, st, h))) return rc;
+    a.noise = d.noise.p;
+  }
+  SFFG_CK(cudaMemsetAsync(d.ekin.p, 0, d.ekin.bytes(), st));
+  const int nb = (a.n3 + 255) / 256;
+  k_md_kick<<<nb, 256, 0, st>>>(a, 1);
+  SFFG_CK(cudaGetLastError());
+  return SFFG_OK;
+}
+
+int Batch::md_steps(int step0, int k, NoiseFn noise, void *noise_ctx, void *stream) {
+  if (!finalized_) return SFFG_ESTATE;
+  DeviceState &d = *d_;
+  cudaStream_t st = pick(d, stream);
+  const int nsys = num_systems();
+  MdArgs a;
+  double c_ave;
+  md_args(*this, d, opts_, natom_total_, a, c_ave);
+  const double boltz2 = 9.93595e-4;
+  std::vector<double> rndf(nsys), h;
+  for (int s = 0; s < nsys; s++) {
+    int nf = 0;
+    for (int f : sys_[s].frozen) nf += f != 0;
+    rndf[s] = 3.0 * sys_[s].natom - 3.0 * nf;
+  }
+  DBuf<double> d_rndf;
+  SFFG_CK(d_rndf.alloc(nsys));
+  SFFG_CK(cudaMemcpyAsync(d_rndf.p, rndf.data(), nsys * sizeof(double), cudaMemcpyHostToDevice, st));
+  if (d.etot.n && d.noise.n == 0 && noise) SFFG_CK(d.noise.alloc(a.n3));
+  const int nb = (a.n3 + 255) / 256;
+  int rc = SFFG_OK;
+  for (int i = 1; i <= k; i++) {
+    const int nstep = step0 + i;
+    k_md_drift<<<nb, 256, 0, st>>>(a);
+    const bool rebuild = opts_.nsnb > 0 && nstep % opts_.nsnb == 0;
+    if ((rc = run_eval(rebuild, st))) break;
+    if (noise && a.gammai != 0.0) {
+      if ((rc = upload_noise(*this, d, noise, noise_ctx, st, h))) break;
+      a.noise = d.noise.p;
+    }
+    a.step = static_cast<unsigned>(nstep);
+    SFFG_CK(cudaMemsetAsync(d.ekin.p, 0, d.ekin.bytes(), st));
+    k_md_kick<<<nb, 256, 0, st>>>(a, 0);
+    k_md_tscal<<<(nsys + 127) / 128, 128, 0, st>>>(d.ekin.p, d.tscal.p, nullptr, nsys,
+                                                   boltz2 * opts_.temp0, d_rndf.p, opts_.dt / opts_.tautp, c_ave,
+                                                   a.gammai == 0.0);
+    SFFG_CK(cudaGetLastError());
+  }
+  SFFG_CK(cudaStreamSynchronize(st));
+  d_rndf.release();
+  return rc;
+}
+
+int Batch::md_kinetic(std::vector<double> &ekin, void *stream) {
+  if (!finalized_) return SFFG_ESTATE;
+  DeviceState &d = *d_;
+  cudaStream_t st = pick(d, stream);
+  const int nsys = num_systems();
+  std::vector<long long> e(nsys);
+  SFFG_CK(cudaMemcpyAsync(e.data(), d.ekin.p, nsys * sizeof(long long), cudaMemcpyDeviceToHost, st));
+  SFFG_CK(cudaStreamSynchronize(st));
+  const double dt5 = 0.5 * opts_.dt * 20.455, gammai = opts_.gamma_ln / 20.455;
+  const double c_ave = gammai > 0.0 ? 1.0 + gammai * dt5 : 1.0;
+  ekin.resize(nsys);
+  for (int s = 0; s < nsys; s++) ekin[s] = 0.5 * static_cast<double>(e[s]) * (1.0 / 4294967296.0) * c_ave;
+  return SFFG_OK;
+}
+
+int Batch::md_set_tscal(const std::vector<double> &tscal, void *stream) {
+  if (!finalized_ || static_cast<int>(tscal.size()) != num_systems()) return SFFG_EINVAL;
+  SFFG_CK(cudaMemcpyAsync(d_->tscal.p, tscal.data(), tscal.size() * sizeof(double), cudaMemcpyHostToDevice,
+                          pick(*d_, stream)));
+  return SFFG_OK;
+}
+
+// ------------------------------------------------------------------ conjgrad
+
+namespace {
+
+constexpr int kCgThreads = 256;
+
+// Sum of a value over the block; every thread receives the total.
+__device__ double block_sum(double v, double *red) {
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(kFull, v, o);
+  const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+  __syncthreads();
+  if (lane == 0) red[w] = v;
+  __syncthreads();
+  double t = 0.0;
+  for (int k = 0; k < kCgThreads / 32; k++) t += red[k];
+  return t;
+}
+
+__device__ double block_max(double v, double *red) {
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) v = fmax(v, __shfl_xor_sync(kFull, v, o));
+  const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+  __syncthreads();
+  if (lane == 0) red[w] = v;
+  __syncthreads();
+  double t = red[0];
+  for (int k = 1; k < kCgThreads / 32; k++) t = fmax(t, red[k]);
+  return t;
+}
+
+struct CgArgs {
+  CgState *state;
+  double *x, *g, *w;
+  const double *etot;
+  const int *sys_natom, *sys_atom_off;
+  int *sys_active;
+  int *nactive;
+};
+
+// Runs one system's copy of the reference's conjgrad() (conjgrad.c:75-263)
+// from just after an evaluation up to the next evaluation request (label
+// L10) or to its end (L100).  Every thread follows the same scalar control
+// flow; vector loops and dot products are spread over the block.
+__global__ void __launch_bounds__(kCgThreads) k_cg_post(CgArgs a) {
+  const int s = blockIdx.x;
+  if (!a.sys_active[s]) return;
+  __shared__ double red[kCgThreads / 32];
+  CgState st = a.state[s];
+  const int n = 3 * a.sys_natom[s];
+  const size_t off = 3 * static_cast<size_t>(a.sys_atom_off[s]);
+  double *x = a.x + off, *g = a.g + off, *w = a.w + 6 * off;
+  double *wd = w, *rsdx = w + n, *rsdg = w + 2 * n, *wginit = w + 3 * n, *xopt = w + 4 * n, *gopt = w + 5 * n;
+  const int maxlin = 10, mxfcon = 4;
+  double f = a.etot[s];
+  st.f = f;
+  int label = st.niter >= 2 ? 30 : 20;
+  for (int guard = 0; guard < 1000; guard++) {
+    switch (label) {
+      case 20:
+        for (int i = threadIdx.x; i < n; i += kCgThreads) wd[i] = -g[i];
+        st.iterrs = 0;
+        if (st.iterc > 0) { label = 40; break; }
+        // fall through
+      case 30: {
+        double pg = 0.0, ps = 0.0;
+        for (int i = threadIdx.x; i < n; i += kCgThreads) {
+          pg += wd[i] * g[i];
+          ps += g[i] * g[i];
+        }
+        st.gnew = block_sum(pg, red);
+        st.sum = block_sum(ps, red);
+        bool take = false;
+        if (st.niter == 1) {
+          st.fmin = f;
+          take = true;
+        } else {
+          st.fch = f - st.fmin;
+          if (st.fch < 0.0 || (st.fch == 0.0 && st.gnew / st.gmin >= -1.0)) {
+            st.fmin = f;
+            take = true;
+          }
+        }
+        if (take) {
+          st.gsqrd = st.sum;
+          st.nfopt = st.niter;
+          for (int i = threadIdx.x; i < n; i += kCgThreads) {
+            xopt[i] = x[i];
+            gopt[i] = g[i];
+          }
+          if (st.sum <= st.dgrad) { label = 100; break; }
+        }
+        if (st.niter == st.maxiter + 1) { st.ier = -3; label = 100; break; }
+        if (st.niter > 1) { label = 60; break; }
+        st.dfpr = st.dfpred;
+        st.stmin = st.dfpred / st.gsqrd;
+      }
+        // fall through
+      case 40: {
+        ++st.iterc;
+        st.finit = f;
+        double pg = 0.0;
+        for (int i = threadIdx.x; i < n; i += kCgThreads) {
+          wginit[i] = g[i];
+          pg += wd[i] * g[i];
+        }
+        st.ginit = block_sum(pg, red);
+        if (st.ginit >= 0.0) { st.ier = -2; label = 90; break; }
+        st.gmin = st.ginit;
+        st.sbound = -1.0;
+        st.nfbeg = st.niter;
+        st.iretry = -1;
+        {
+          const double q = fabs(st.dfpr / st.ginit);
+          st.stepch = st.stmin <= q ? st.stmin : q;
+        }
+        st.stmin = 0.0;
+      }
+        // fall through
+      case 50: {
+        st.step = st.stmin + st.stepch;
+        double pw = 0.0;
+        for (int i = threadIdx.x; i < n; i += kCgThreads) {
+          x[i] = xopt[i] + st.stepch * wd[i];
+          pw = fmax(pw, fabs(x[i] - xopt[i]));
+        }
+        const double work = block_max(pw, red);
+        if (work > 0.0) { label = 10; break; }
+        if (st.niter > st.nfbeg + 1) st.ier = -1;
+        if (fabs(st.gmin / st.ginit) > 0.2) st.ier = -1;
+        label = 90;
+        break;
+      }
+      case 60: {
+        const double work = (st.fch + st.fch) / st.stepch - st.gnew - st.gmin;
+        st.ddspln = (st.gnew - st.gmin) / st.stepch;
+        if (st.niter > st.nfopt) st.sbound = st.step;
+        if (st.niter <= st.nfopt) {
+          if (st.gmin * st.gnew <= 0.0) st.sbound = st.stmin;
+          st.stmin = st.step;
+          st.gmin = st.gnew;
+          st.stepch = -st.stepch;
+        }
+        if (st.fch != 0.0) st.ddspln += (work + work) / st.stepch;
+        if (st.gmin == 0.0) { label = 90; break; }
+        if (st.niter > st.nfbeg + 1) {
+          if (fabs(st.gmin / st.ginit) <= 0.2) { label = 90; break; }
+          if (st.niter >= st.nfopt + maxlin) { st.ier = -1; label = 90; break; }
+        }
+      }
+        // fall through
+      case 70: {
+        st.stepch = (st.sbound - st.stmin) * 0.5;
+        if (st.sbound < -0.5) st.stepch = st.stmin * 9.0;
+        const double gspln = st.gmin + st.stepch * st.ddspln;
+        if (st.gmin * gspln < 0.0) st.stepch = st.stepch * st.gmin / (st.gmin - gspln);
+        label = 50;
+        break;
+      }
+      case 80: {
+        double pg = 0.0;
+        for (int i = threadIdx.x; i < n; i += kCgThreads) pg += g[i] * wginit[i];
+        st.sum = block_sum(pg, red);
+        st.beta = (st.gsqrd - st.sum) / (st.gmin - st.ginit);
+        if (fabs(st.beta * st.gmin) > st.gsqrd * 0.2) {
+          ++st.iretry;
+          if (st.iretry <= 0) {
+            if (st.niter >= st.nfopt + maxlin) { st.ier = -1; label = 90; break; }
+            label = 70;
+            break;
+          }
+        }
+        if (f < st.finit) st.iterfm = st.iterc;
+        if (st.iterc >= st.iterfm + mxfcon) { st.ier = -4; label = 100; break; }
+        st.dfpr = st.stmin * st.ginit;
+        if (st.iretry > 0) { label = 20; break; }
+        if (st.iterrs != 0 && st.iterc - st.iterrs < n && fabs(st.sum) < st.gsqrd * 0.2) {
+          double pga = 0.0, pgs = 0.0;
+          for (int i = threadIdx.x; i < n; i += kCgThreads) {
+            pga += g[i] * rsdg[i];
+            pgs += g[i] * rsdx[i];
+          }
+          st.gama = block_sum(pga, red) / st.gamden;
+          const double gs = block_sum(pgs, red);
+          if (fabs(st.beta * st.gmin + st.gama * gs) < st.gsqrd * 0.2) {
+            __syncthreads();
+            for (int i = threadIdx.x; i < n; i += kCgThreads) wd[i] = -g[i] + st.beta * wd[i] + st.gama * rsdx[i];
+            __syncthreads();
+            label = 40;
+            break;
+          }
+        }
+        st.gamden = st.gmin - st.ginit;
+        for (int i = threadIdx.x; i < n; i += kCgThreads) {
+          rsdx[i] = wd[i];
+          rsdg[i] = g[i] - wginit[i];
+          wd[i] = -g[i] + st.beta * wd[i];
+        }
+        __syncthreads();
+        st.iterrs = st.iterc;
+        label = 40;
+        break;
+      }
+      case 90:
+        if (st.niter != st.nfopt) {
+          f = st.fmin;
+          for (int i = threadIdx.x; i < n; i += kCgThreads) {
+            x[i] = xopt[i];
+            g[i] = gopt[i];
+          }
+          __syncthreads();
+        }
+        if (st.ier == 0) { label = 80; break; }
+        label = 100;
+        break;
+      case 10:
+        // request the next evaluation (the reference's L10)
+        ++st.niter;
+        guard = 1 << 30;
+        break;
+      case 100:
+        st.done = 1;
+        st.ret = st.ier == 0 ? st.niter : st.ier;
+        guard = 1 << 30;
+        break;
+      default:
+        st.done = 1;
+        st.ret = -99;
+        guard = 1 << 30;
+        break;
+    }
+  }
+  st.f = f;
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    a.state[s] = st;
+    if (st.done) {
+      a.sys_active[s] = 0;
+      atomicSub(a.nactive, 1);
+    }
+  }
+}
+
+}  // namespace
+
+int Batch::cg(int maxiter, double rmsgrad, double dfpred, bool first_rebuild, std::vector<int> &status,
+              std::vector<double> &energy, void *stream, const std::function<int(int)> &after_eval) {
+  if (!finalized_) return SFFG_ESTATE;
+  DeviceState &d = *d_;
+  cudaStream_t st = pick(d, stream);
+  const int nsys = num_systems();
+  SFFG_CK(d.cg_w.alloc(6 * 3 * static_cast<size_t>(natom_total_)));
+  SFFG_CK(d.cg_state.alloc(nsys));
+  std::vector<CgState> init(nsys);
+  for (int s = 0; s < nsys; s++) {
+    CgState c;
+    std::memset(&c, 0, sizeof(c));
+    c.niter = 1;  // the reference's first ++niter at L10
+    c.maxiter = maxiter;
+    c.dgrad = rmsgrad * rmsgrad * 3.0 * sys_[s].natom;
+    c.dfpred = dfpred;
+    init[s] = c;
+  }
+  SFFG_CK(cudaMemcpyAsync(d.cg_state.p, init.data(), nsys * sizeof(CgState), cudaMemcpyHostToDevice, st));
+  std::vector<int> ones(nsys, 1);
+  SFFG_CK(cudaMemcpyAsync(d.sys_active.p, ones.data(), nsys * sizeof(int), cudaMemcpyHostToDevice, st));
+  DBuf<int> nactive;
+  SFFG_CK(nactive.alloc(1));
+  SFFG_CK(cudaMemcpyAsync(nactive.p, &nsys, sizeof(int), cudaMemcpyHostToDevice, st));
+  CgArgs a;
+  a.state = d.cg_state.p;
+  a.x = d.x.p;
+  a.g = d.grad.p;
+  a.w = d.cg_w.p;
+  a.etot = d.etot.p;
+  a.sys_natom = d.sys_natom.p;
+  a.sys_atom_off = d.sys_atom_off.p;
+  a.sys_active = d.sys_active.p;
+  a.nactive = nactive.p;
+  int rc = SFFG_OK;
+  for (int turn = 0; turn <= maxiter; turn++) {
+    // every active system is at evaluation turn+1, so iter = turn for all
+    const bool rebuild = (turn == 0 && first_rebuild) || (turn > 0 && opts_.nsnb > 0 && turn % opts_.nsnb == 0);
+    if ((rc = run_eval(rebuild || !have_list_, st))) break;
+    if (after_eval && (rc = after_eval(turn))) break;
+    k_cg_post<<<nsys, kCgThreads, 0, st>>>(a);
+    SFFG_CK(cudaGetLastError());
+    if ((turn & 7) == 7 || turn == maxiter) {
+      int na = 0;
+      SFFG_CK(cudaMemcpyAsync(&na, nactive.p, sizeof(int), cudaMemcpyDeviceToHost, st));
+      SFFG_CK(cudaStreamSynchronize(st));
+      if (na <= 0) break;
+    }
+  }
+  std::vector<CgState> fin(nsys);
+  SFFG_CK(cudaMemcpyAsync(fin.data(), d.cg_state.p, nsys * sizeof(CgState), cudaMemcpyDeviceToHost, st));
+  SFFG_CK(cudaMemcpyAsync(d.sys_active.p, ones.data(), nsys * sizeof(int), cudaMemcpyHostToDevice, st));
+  SFFG_CK(cudaStreamSynchronize(st));
+  nactive.release();
+  status.resize(nsys);
+  energy.resize(nsys);
+  for (int s = 0; s < nsys; s++) {
+    status[s] = fin[s].done ? fin[s].ret : -3;
+    energy[s] = fin[s].f;
+  }
+  return rc;
+}
+
+}  // namespace sffg

@@ -1,0 +1,116 @@
+// The device engine: a batch of independent systems resident on one GPU.
+//
+// Layout in device memory (all systems flattened, never mixed in a tile):
+//   slot  = position in the spatially sorted atom order; 32 consecutive
+//           slots form a tile, tiles never straddle two systems, padding
+//           slots are marked invalid in the tile's lane mask;
+//   atom  = index in the caller's atom order (systems concatenated).
+// Per-slot FP32 arrays feed the pair kernels; FP64 arrays hold coordinates,
+// velocities, gradients and the per-atom Born-radius finish; forces, Born
+// sums, sumdeijda and energies accumulate in 64-bit fixed point, so results
+// do not depend on the order in which tile pairs are processed.
+#pragma once
+
+#include <functional>
+#include <memory>
+#include <string>
+#include <vector>
+
+#include "sffg_internal.h"
+
+namespace sffg {
+
+struct DeviceState;  // defined in engine.cu
+
+struct SystemInfo {
+  int natom = 0, atom_off = 0, slot_off = 0, tile_off = 0, ntile = 0;
+  double fsmax = 0.0;
+  bool has_frozen = false;
+  std::vector<int> frozen;
+  std::vector<double> mass;
+  int ntypes = 0;
+  int lj_off = 0;
+};
+
+class Batch {
+ public:
+  explicit Batch(const Options &opts);
+  ~Batch();
+  Batch(const Batch &) = delete;
+  Batch &operator=(const Batch &) = delete;
+
+  // Returns the system index, or a negative status.
+  int add_system(PARMSTRUCT_T *prm, const int *frozen, const double *x, bool mutate_prm);
+  int finalize();
+  bool finalized() const { return finalized_; }
+  int num_systems() const { return static_cast<int>(sys_.size()); }
+  const SystemInfo &system(int s) const { return sys_[s]; }
+  const ModelParams &model() const { return mp_; }
+  const Options &opts() const { return opts_; }
+  int total_atoms() const { return natom_total_; }
+
+  // Host <-> device transfers of one system (stream-ordered, async unless
+  // stated).
+  int set_coords(int sys, const double *x, void *stream);
+  int get_coords(int sys, double *x, void *stream);      // synchronous
+  int get_grad(int sys, double *g, void *stream);        // synchronous
+  int get_reff(int sys, double *reff, void *stream);     // synchronous
+  int set_velocities(int sys, const double *v, void *stream);
+  int get_velocities(int sys, double *v, void *stream);  // synchronous
+  // Energy components of the last evaluation in the reference's ene[]
+  // layout (13 entries); synchronous.
+  int get_energy(int sys, double *ene, void *stream);
+  int get_all_energies(std::vector<double> &ene13, void *stream);
+
+  // One energy+gradient evaluation of every active system.  rebuild
+  // requests a pair-list rebuild first (always done on the first call).
+  int eval(bool rebuild, void *stream);
+  long long num_pairs(int sys);
+
+  // Device-resident Langevin/Berendsen md (the reference's integrator,
+  // src/sff/sff.c:2191-2354) over all systems.  md_begin evaluates the first
+  // force and sets the initial accelerations; md_steps then advances k
+  // steps numbered step0+1 .. step0+k.  noise: nullptr -> device Philox;
+  // otherwise a host callback that fills the unit Gaussian draws of every
+  // non-frozen coordinate in the reference's order.
+  using NoiseFn = void (*)(void *ctx, int sys, int n, double *out);
+  int md_begin(bool rebuild, NoiseFn noise, void *noise_ctx, void *stream);
+  int md_steps(int step0, int k, NoiseFn noise, void *noise_ctx, void *stream);
+  // Kinetic energy after the last md step (reference convention,
+  // sff.c:2294-2306) and Berendsen factor for the next step.
+  int md_kinetic(std::vector<double> &ekin, void *stream);
+  int md_set_tscal(const std::vector<double> &tscal, void *stream);
+
+  // Batched conjgrad: every system runs the reference's state machine
+  // (src/sff/conjgrad.c:34-263).  first_rebuild forces a pair-list build
+  // before the first evaluation; after_eval (optional) runs on the host
+  // after every evaluation with the evaluation index (the reference's
+  // iteration count).
+  int cg(int maxiter, double rmsgrad, double dfpred, bool first_rebuild, std::vector<int> &status,
+         std::vector<double> &energy, void *stream, const std::function<int(int)> &after_eval);
+  // True once a pair list has been built.
+  bool have_list() const { return have_list_; }
+
+  size_t device_bytes() const;
+  std::string last_error;
+
+  // Raw device views used by the legacy session.
+  double *d_coords();
+  double *d_grad();
+  void *default_stream();
+
+ private:
+  int upload();
+  int build_lists(void *stream);
+  int run_eval(bool rebuild, void *stream);
+  Options opts_;
+  ModelParams mp_;
+  std::vector<SystemInfo> sys_;
+  std::vector<HostSystem> host_;
+  std::vector<std::vector<double>> x0_;
+  int natom_total_ = 0, nslot_ = 0, ntile_ = 0;
+  bool finalized_ = false, have_list_ = false;
+  std::unique_ptr<DeviceState> d_;
+};
+
+}  // namespace sffg

@@ -1,0 +1,590 @@
+// Per-atom, per-tile, list-building, bonded and integrator kernels.
+#pragma once
+
+#include <cstdint>
+
+#include "kernels.cuh"
+
+namespace sffg {
+
+constexpr double kLog2eQuarterSqrt = 0.60056120439322491;  // sqrt(log2(e) / 4)
+constexpr double kKscale = 0.73;                           // src/sff/eff.c:1368
+
+// ------------------------------------------------------------ packing
+// Splits the FP64 coordinates of every slot into FP32 high/low parts,
+// computes each tile's bounding box, and clears the per-slot accumulators.
+// One warp per tile.  Padding slots sit far away with zero charge.
+__global__ void k_pack(const double *__restrict__ x, const int *__restrict__ slot_atom,
+                       const float *__restrict__ q32, const unsigned *__restrict__ tile_valid,
+                       int nslot, float4 *pos_hi, float4 *pos_lo, float4 *box_lo, float4 *box_hi,
+                       long long *acc_sumi, long long *acc_fx, long long *acc_fy, long long *acc_fz,
+                       int *nonfinite_sys, const int *tile_sys) {
+  const int slot = blockIdx.x * blockDim.x + threadIdx.x;
+  const int lane = threadIdx.x & 31;
+  if (slot - lane >= nslot) return;  // whole warp beyond the last tile
+  const int tile = slot >> 5;
+  const int a = slot < nslot ? slot_atom[slot] : -1;
+  float4 hi, lo;
+  float bx0 = 3e38f, by0 = 3e38f, bz0 = 3e38f, bx1 = -3e38f, by1 = -3e38f, bz1 = -3e38f;
+  bool bad = false;
+  if (a >= 0) {
+    const double X = x[3 * a], Y = x[3 * a + 1], Z = x[3 * a + 2];
+    bad = !(isfinite(X) && isfinite(Y) && isfinite(Z));
+    const float hx = static_cast<float>(X), hy = static_cast<float>(Y), hz = static_cast<float>(Z);
+    hi = make_float4(hx, hy, hz, q32[slot]);
+    lo = make_float4(static_cast<float>(X - hx), static_cast<float>(Y - hy), static_cast<float>(Z - hz), 0.f);
+    if (!bad) {
+      bx0 = bx1 = hx;
+      by0 = by1 = hy;
+      bz0 = bz1 = hz;
+    }
+  } else {
+    hi = make_float4(1.0e6f + 16.0f * lane, 1.0e6f, 1.0e6f, 0.f);
+    lo = make_float4(0.f, 0.f, 0.f, 0.f);
+  }
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) {
+    bx0 = fminf(bx0, __shfl_xor_sync(kFull, bx0, o));
+    by0 = fminf(by0, __shfl_xor_sync(kFull, by0, o));
+    bz0 = fminf(bz0, __shfl_xor_sync(kFull, bz0, o));
+    bx1 = fmaxf(bx1, __shfl_xor_sync(kFull, bx1, o));
+    by1 = fmaxf(by1, __shfl_xor_sync(kFull, by1, o));
+    bz1 = fmaxf(bz1, __shfl_xor_sync(kFull, bz1, o));
+  }
+  const unsigned anybad = __ballot_sync(kFull, bad);
+  if (slot >= nslot) return;
+  pos_hi[slot] = hi;
+  pos_lo[slot] = lo;
+  acc_sumi[slot] = 0;
+  acc_fx[slot] = 0;
+  acc_fy[slot] = 0;
+  acc_fz[slot] = 0;
+  if (lane == 0) {
+    box_lo[tile] = make_float4(bx0, by0, bz0, 0.f);
+    box_hi[tile] = make_float4(bx1, by1, bz1, 0.f);
+    if (anybad) nonfinite_sys[tile_sys[tile]] = 1;
+  }
+  (void)tile_valid;
+}
+
+// ------------------------------------------------------------ pair lists
+struct ListArgs {
+  const float4 *pos_hi, *pos_lo, *box_lo, *box_hi;
+  const double *x;
+  const int *slot_atom, *param;
+  const unsigned *tile_valid;
+  const int *tile_sys, *sys_tile_end, *sys_has_frozen, *sys_active;
+  const int *excl_tile_start;  // per tile: range into excl_tile_j / excl_tile_idx
+  const int *excl_tile_j, *excl_tile_idx;
+  int ntile;
+  float cut2f;
+  double cut2;
+  Item *items;
+  int *nitems;
+  int capacity;
+  unsigned *masks;
+  int *nmasks;
+  int mask_capacity;
+  int *overflow;
+};
+
+__device__ __forceinline__ bool box_candidate(const ListArgs &a, float4 il, float4 ih, int J) {
+  const float4 bl = a.box_lo[J], bh = a.box_hi[J];
+  float dx = fmaxf(0.0f, fmaxf(il.x - bh.x, bl.x - ih.x));
+  float dy = fmaxf(0.0f, fmaxf(il.y - bh.y, bl.y - ih.y));
+  float dz = fmaxf(0.0f, fmaxf(il.z - bh.z, bl.z - ih.z));
+  return dx * dx + dy * dy + dz * dz < a.cut2f * 1.0001f + 1e-3f;
+}
+
+// One warp per i-tile: writes every (I, J >= I) tile pair that can hold a
+// listed pair -- r^2 < cut^2 at build time, two frozen atoms never
+// (src/sff/nblist.c:726-746) -- with a per-row bit mask unless the whole
+// tile pair is certainly inside the cutoff.
+__global__ void k_build_list(const ListArgs a) {
+  const int lane = threadIdx.x & 31;
+  const int I = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+  if (I >= a.ntile) return;
+  const int sys = a.tile_sys[I];
+  if (!a.sys_active[sys]) return;
+  const int jend = a.sys_tile_end[sys];
+  const float4 il = a.box_lo[I], ih = a.box_hi[I];
+  int cnt = 0;
+  for (int J0 = I; J0 < jend; J0 += 32) {
+    const int J = J0 + lane;
+    const bool c = J < jend && box_candidate(a, il, ih, J);
+    cnt += __popc(__ballot_sync(kFull, c));
+  }
+  int base = 0;
+  if (lane == 0) base = atomicAdd(a.nitems, cnt);
+  base = __shfl_sync(kFull, base, 0);
+  if (base + cnt > a.capacity) {
+    if (lane == 0) atomicExch(a.overflow, 1);
+    return;
+  }
+  const int si = I * 32 + lane;
+  const unsigned vI = a.tile_valid[I];
+  const bool myvalid = (vI >> lane) & 1u;
+  const float4 hi_i = a.pos_hi[si], lo_i = a.pos_lo[si];
+  const bool frz_i = (a.param[si] >> 24) & 1;
+  const int ai = a.slot_atom[si];
+  const bool sys_frozen = a.sys_has_frozen[sys];
+  int k = base;
+  for (int J0 = I; J0 < jend; J0 += 32) {
+    const int J = J0 + lane;
+    unsigned bal = __ballot_sync(kFull, J < jend && box_candidate(a, il, ih, J));
+    while (bal) {
+      const int b = __ffs(bal) - 1;
+      bal &= bal - 1;
+      const int Jc = J0 + b;
+      // farthest corner distance of the two boxes
+      const float4 bl = a.box_lo[Jc], bh = a.box_hi[Jc];
+      const float mx = fmaxf(ih.x - bl.x, bh.x - il.x), my = fmaxf(ih.y - bl.y, bh.y - il.y),
+                  mz = fmaxf(ih.z - bl.z, bh.z - il.z);
+      const bool full = !sys_frozen && (mx * mx + my * my + mz * mz) < a.cut2f * 0.9999f - 1e-3f;
+      int ex = -1;
+      for (int e = a.excl_tile_start[I]; e < a.excl_tile_start[I + 1]; e++)
+        if (a.excl_tile_j[e] == Jc) { ex = a.excl_tile_idx[e]; break; }
+      int midx = -1;
+      if (!full) {
+        if (lane == 0) midx = atomicAdd(a.nmasks, 1);
+        midx = __shfl_sync(kFull, midx, 0);
+        if (midx >= a.mask_capacity) {
+          if (lane == 0) atomicExch(a.overflow, 2);
+          midx = -2;
+        } else {
+          const unsigned vJ = a.tile_valid[Jc];
+          unsigned row = 0;
+          for (int jj = 0; jj < 32 && myvalid; jj++) {
+            const int sjj = Jc * 32 + jj;
+            if (!((vJ >> jj) & 1u)) continue;
+            if (Jc == I && jj <= lane) continue;
+            const float4 h = a.pos_hi[sjj], l = a.pos_lo[sjj];
+            const float dx = (hi_i.x - h.x) + (lo_i.x - l.x);
+            const float dy = (hi_i.y - h.y) + (lo_i.y - l.y);
+            const float dz = (hi_i.z - h.z) + (lo_i.z - l.z);
+            const float r2 = dx * dx + dy * dy + dz * dz;
+            bool in;
+            if (r2 < a.cut2f * 0.99999f) {
+              in = true;
+            } else if (r2 > a.cut2f * 1.00001f) {
+              in = false;
+            } else {  // borderline: decide exactly as the reference does, in FP64
+              const int aj = a.slot_atom[sjj];
+              const double ddx = a.x[3 * ai] - a.x[3 * aj], ddy = a.x[3 * ai + 1] - a.x[3 * aj + 1],
+                           ddz = a.x[3 * ai + 2] - a.x[3 * aj + 2];
+              in = ddx * ddx + ddy * ddy + ddz * ddz < a.cut2;
+            }
+            if (in && frz_i && ((a.param[sjj] >> 24) & 1)) in = false;
+            if (in) row |= 1u << jj;
+          }
+          a.masks[static_cast<size_t>(midx) * 32 + lane] = row;
+        }
+      }
+      // (on mask overflow the host rebuilds with more room before any use)
+      if (lane == 0) a.items[k] = make_int4(I, Jc, midx < 0 ? -1 : midx, ex);
+      k++;
+    }
+  }
+}
+
+// ------------------------------------------------------------ Born radii
+// Effective Born radii from the descreening sums (src/sff/eff.c:1710-1727),
+// the diagonal self energy and its sumdeijda seed (eff.c:1884-1893).  FP64.
+struct FinishArgs {
+  const long long *acc_sumi;
+  long long *acc_sd;
+  long long *energy;
+  const int *slot_atom, *tile_sys, *sys_active, *param;
+  const double *rborn64, *q64, *alpha, *beta, *gamma;
+  double *reff64, *psi64, *chainfac;
+  float *reff32, *rinv2;
+  int nslot, gb;
+  double gboffset, kappa, epsext;
+};
+
+__global__ void k_born_finish(const FinishArgs a) {
+  const int slot = blockIdx.x * blockDim.x + threadIdx.x;
+  const int lane = threadIdx.x & 31;
+  if (slot - lane >= a.nslot) return;
+  const int sys = a.tile_sys[slot >> 5];
+  double ediag = 0.0;
+  if (slot < a.nslot) {
+    const int at = a.slot_atom[slot];
+    if (at >= 0 && a.sys_active[sys]) {
+      const double rb = a.rborn64[slot], ri = rb - a.gboffset;
+      const double sumi = -static_cast<double>(a.acc_sumi[slot]) * (1.0 / 1099511627776.0);
+      double reff, psi = 0.0, fac = 1.0;
+      if (a.gb == 1) {
+        reff = 1.0 / (1.0 / ri + sumi);
+        if (reff < 0.0) reff = 30.0;
+      } else {
+        psi = -ri * sumi;
+        const double al = a.alpha[slot], be = a.beta[slot], ga = a.gamma[slot];
+        const double th = tanh((al - be * psi + ga * psi * psi) * psi);
+        reff = 1.0 / (1.0 / ri - th / rb);
+        fac = (al - 2.0 * be * psi + 3.0 * ga * psi * psi) * (1.0 - th * th) * ri / rb;
+      }
+      a.reff64[slot] = reff;
+      a.psi64[slot] = psi;
+      a.chainfac[slot] = fac;
+      a.reff32[slot] = static_cast<float>(reff);
+      a.rinv2[slot] = static_cast<float>(kLog2eQuarterSqrt / reff);
+      double sd = 0.0;
+      if (!((a.param[slot] >> 24) & 1)) {
+        const double qi = a.q64[slot];
+        const double expmkf = exp(-kKscale * a.kappa * reff) / a.epsext;
+        const double dielfac = 1.0 - expmkf, qi2h = 0.5 * qi * qi, qid2h = qi2h * dielfac;
+        ediag = -qid2h / reff;
+        sd = qid2h - kKscale * a.kappa * qi2h * expmkf * reff;
+      }
+      a.acc_sd[slot] = __double2ll_rn(sd * 4294967296.0);
+    } else {
+      a.reff32[slot] = 1.0f;
+      a.rinv2[slot] = 0.0f;
+      a.acc_sd[slot] = 0;
+    }
+  }
+  // a tile never straddles systems, so the warp shares sys
+  const long long e = warp_sum_ll(__double2ll_rn(ediag * 4294967296.0));
+  if (lane == 0 && slot < a.nslot) atomic_add_ll(&a.energy[sys * 8 + 0], e);
+}
+
+// Chain-rule weight of each atom for pass 3 (src/sff/eff.c:2211-2231).
+__global__ void k_chain_prep(const long long *acc_sd, const double *chainfac, const int *param,
+                             const int *slot_atom, float *sumda32, int nslot) {
+  const int slot = blockIdx.x * blockDim.x + threadIdx.x;
+  if (slot >= nslot) return;
+  double v = 0.0;
+  if (slot_atom[slot] >= 0 && !((param[slot] >> 24) & 1))
+    v = static_cast<double>(acc_sd[slot]) * (1.0 / 4294967296.0) * chainfac[slot];
+  sumda32[slot] = static_cast<float>(v);
+}
+
+// ------------------------------------------------------------ bonded terms
+// FP64, one thread per term, forces scattered in fixed point.  Terms are
+// stored with batch-global atom indices, grouped by system.
+struct BondedArgs {
+  const double *x;
+  const int *atom_slot;
+  const int *atom_sys;
+  long long *acc_fx, *acc_fy, *acc_fz;
+  long long *energy;
+  const int *sys_active;
+};
+
+__device__ __forceinline__ void add_force(const BondedArgs &a, int atom, double gx, double gy, double gz) {
+  const int s = a.atom_slot[atom];
+  atomic_add_ll(&a.acc_fx[s], __double2ll_rn(gx * 4294967296.0));
+  atomic_add_ll(&a.acc_fy[s], __double2ll_rn(gy * 4294967296.0));
+  atomic_add_ll(&a.acc_fz[s], __double2ll_rn(gz * 4294967296.0));
+}
+
+// Adds each lane's energy into its system's slot; a warp whose lanes share
+// one system uses a single atomic.
+__device__ __forceinline__ void add_energy(const BondedArgs &a, int sys, int slot, double e) {
+  const long long v = __double2ll_rn(e * 4294967296.0);
+  const int s0 = __shfl_sync(kFull, sys, 0);
+  if (__all_sync(kFull, sys == s0 || sys < 0)) {
+    const long long t = warp_sum_ll(sys >= 0 ? v : 0);
+    if ((threadIdx.x & 31) == 0 && s0 >= 0) atomic_add_ll(&a.energy[s0 * 8 + slot], t);
+  } else if (sys >= 0) {
+    atomic_add_ll(&a.energy[sys * 8 + slot], v);
+  }
+}
+
+// Harmonic bonds: src/sff/eff.c:116-154.
+__global__ void k_bonds(const BondedArgs a, const int2 *atoms, const double2 *par, int n) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  int sys = -1;
+  double e = 0.0;
+  if (i < n) {
+    const int p = atoms[i].x, q = atoms[i].y;
+    sys = a.atom_sys[p];
+    if (!a.sys_active[sys]) {
+      sys = -1;
+    } else {
+      const double rx = a.x[3 * p] - a.x[3 * q], ry = a.x[3 * p + 1] - a.x[3 * q + 1], rz = a.x[3 * p + 2] - a.x[3 * q + 2];
+      const double r = sqrt(rx * rx + ry * ry + rz * rz);
+      const double db = r - par[i].y;
+      double df = par[i].x * db;
+      e = df * db;
+      df *= 2.0 / r;
+      add_force(a, p, rx * df, ry * df, rz * df);
+      add_force(a, q, -rx * df, -ry * df, -rz * df);
+    }
+  }
+  add_energy(a, sys, E_BOND, e);
+}
+
+// Harmonic angles: src/sff/eff.c:216-300.
+__global__ void k_angles(const BondedArgs a, const int4 *atoms, const double2 *par, int n) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  int sys = -1;
+  double e = 0.0;
+  if (i < n) {
+    const int p = atoms[i].x, q = atoms[i].y, r = atoms[i].z;
+    sys = a.atom_sys[p];
+    if (!a.sys_active[sys]) {
+      sys = -1;
+    } else {
+      const double dxi = a.x[3 * p] - a.x[3 * q], dyi = a.x[3 * p + 1] - a.x[3 * q + 1], dzi = a.x[3 * p + 2] - a.x[3 * q + 2];
+      const double dxj = a.x[3 * r] - a.x[3 * q], dyj = a.x[3 * r + 1] - a.x[3 * q + 1], dzj = a.x[3 * r + 2] - a.x[3 * q + 2];
+      const double ri = sqrt(dxi * dxi + dyi * dyi + dzi * dzi), rj = sqrt(dxj * dxj + dyj * dyj + dzj * dzj);
+      const double rir = 1.0 / ri, rjr = 1.0 / rj;
+      const double uxi = dxi * rir, uyi = dyi * rir, uzi = dzi * rir, uxj = dxj * rjr, uyj = dyj * rjr, uzj = dzj * rjr;
+      double cst = uxi * uxj + uyi * uyj + uzi * uzj;
+      cst = fmin(1.0, fmax(-1.0, cst));
+      const double at = acos(cst), da = at - par[i].y;
+      double df = da * par[i].x;
+      e = df * da;
+      df = df + df;
+      double sn = sin(at);
+      if (sn > 0 && sn < 1.e-3) sn = 1.e-3;
+      else if (sn < 0 && sn > -1.e-3) sn = -1.e-3;
+      df = -df / sn;
+      const double xa = df * rir * (uxj - cst * uxi), xc = df * rjr * (uxi - cst * uxj);
+      const double ya = df * rir * (uyj - cst * uyi), yc = df * rjr * (uyi - cst * uyj);
+      const double za = df * rir * (uzj - cst * uzi), zc = df * rjr * (uzi - cst * uzj);
+      add_force(a, p, xa, ya, za);
+      add_force(a, r, xc, yc, zc);
+      add_force(a, q, -(xa + xc), -(ya + yc), -(za + zc));
+    }
+  }
+  add_energy(a, sys, E_ANGLE, e);
+}
+
+// Cosine dihedrals: src/sff/eff.c:373-618 (one expanded term per thread).
+__global__ void k_dihedrals(const BondedArgs a, const int4 *atoms, const double4_32a *par, int n) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  int sys = -1;
+  double e = 0.0;
+  if (i < n) {
+    const int p = atoms[i].x, q = atoms[i].y, r = atoms[i].z, w = atoms[i].w;
+    sys = a.atom_sys[p];
+    if (!a.sys_active[sys]) {
+      sys = -1;
+    } else {
+      const double pk = par[i].x, pn = par[i].y, phase = par[i].z;
+      const double *x = a.x;
+      const double ax = x[3 * q] - x[3 * p], ay = x[3 * q + 1] - x[3 * p + 1], az = x[3 * q + 2] - x[3 * p + 2];
+      const double bx = x[3 * r] - x[3 * q], by = x[3 * r + 1] - x[3 * q + 1], bz = x[3 * r + 2] - x[3 * q + 2];
+      const double cx = x[3 * w] - x[3 * r], cy = x[3 * w + 1] - x[3 * r + 1], cz = x[3 * w + 2] - x[3 * r + 2];
+      const double ab = ax * bx + ay * by + az * bz, bc = bx * cx + by * cy + bz * cz, ac = ax * cx + ay * cy + az * cz;
+      const double aa = ax * ax + ay * ay + az * az, bb = bx * bx + by * by + bz * bz, cc = cx * cx + cy * cy + cz * cz;
+      const double uu = aa * bb - ab * ab, vv = bb * cc - bc * bc, uv = ab * bc - ac * bb;
+      const double den = uu == 0.0 ? 0.0 : 1.0 / sqrt(uu * vv);
+      const double co = uv * den, co1 = 0.5 * co * den;
+      const double a0x = -bc * bx + bb * cx, a0y = -bc * by + bb * cy, a0z = -bc * bz + bb * cz;
+      const double b0x = ab * cx + bc * ax - 2. * ac * bx, b0y = ab * cy + bc * ay - 2. * ac * by, b0z = ab * cz + bc * az - 2. * ac * bz;
+      const double c0x = ab * bx - bb * ax, c0y = ab * by - bb * ay, c0z = ab * bz - bb * az;
+      const double a1x = 2. * uu * (-cc * bx + bc * cx), a1y = 2. * uu * (-cc * by + bc * cy), a1z = 2. * uu * (-cc * bz + bc * cz);
+      const double b1x = 2. * uu * (bb * cx - bc * bx), b1y = 2. * uu * (bb * cy - bc * by), b1z = 2. * uu * (bb * cz - bc * bz);
+      const double a2x = -2. * vv * (bb * ax - ab * bx), a2y = -2. * vv * (bb * ay - ab * by), a2z = -2. * vv * (bb * az - ab * bz);
+      const double b2x = 2. * vv * (aa * bx - ab * ax), b2y = 2. * vv * (aa * by - ab * ay), b2z = 2. * vv * (aa * bz - ab * az);
+      double df;
+      if (fabs(phase - 3.142) > 0.01 && fabs(phase) > 0.01) {
+        const double c = fmin(1.0, fmax(-1.0, co));
+        double phi = acos(c);
+        const double ux = ay * bz - az * by, uy = az * bx - ax * bz, uz = ax * by - ay * bx;
+        const double vx = by * cz - bz * cy, vy = bz * cx - bx * cz, vz = bx * cy - by * cx;
+        const double sx = uy * vz - uz * vy, sy = uz * vx - ux * vz, sz = ux * vy - uy * vx;
+        if (sx * bx + sy * by + sz * bz < 0.0) phi = -phi;
+        const double delta = pn * phi - phase;
+        e = pk * (1.0 + cos(delta));
+        const double yy = sin(phi);
+        if (fabs(yy) > 0.001) df = pk * pn * sin(delta) / yy;
+        else if (phi > -1.0 && phi < 1.0) df = pk * pn * sin(delta) * 1000.;
+        else df = -pk * pn * sin(delta) * 1000.;
+      } else {
+        const double sg = fabs(phase - 3.142) < 0.01 ? -1.0 : 1.0, c2 = co * co;
+        switch (static_cast<int>(fabs(pn))) {
+          case 1: e = pk * (1.0 + sg * co); df = sg * pk; break;
+          case 2: e = pk * (1.0 + sg * (2. * c2 - 1.)); df = sg * pk * 4. * co; break;
+          case 3: e = pk * (1.0 + sg * co * (4. * c2 - 3.)); df = sg * pk * (12. * c2 - 3.); break;
+          case 4: e = pk * (1.0 + sg * (8. * c2 * (c2 - 1.) + 1.)); df = sg * pk * co * (32. * c2 - 16.); break;
+          case 5: e = pk * (1.0 + sg * (16. * c2 * c2 * co - 20. * c2 * co + 5. * co)); df = sg * pk * (80. * c2 * c2 - 60. * c2 + 5.); break;
+          case 6: e = pk * (1.0 + sg * (32. * c2 * c2 * c2 - 48. * c2 * c2 + 18. * c2 - 1.)); df = sg * pk * co * (192. * c2 * c2 - 192. * c2 + 36.); break;
+          default: e = 0.0; df = 0.0;  // rejected on the host
+        }
+      }
+      add_force(a, p, df * (a0x - a2x * co1) * den, df * (a0y - a2y * co1) * den, df * (a0z - a2z * co1) * den);
+      add_force(a, q, df * (-a0x - b0x - (a1x - a2x - b2x) * co1) * den, df * (-a0y - b0y - (a1y - a2y - b2y) * co1) * den,
+                df * (-a0z - b0z - (a1z - a2z - b2z) * co1) * den);
+      add_force(a, r, df * (b0x - c0x - (-a1x - b1x + b2x) * co1) * den, df * (b0y - c0y - (-a1y - b1y + b2y) * co1) * den,
+                df * (b0z - c0z - (-a1z - b1z + b2z) * co1) * den);
+      add_force(a, w, df * (c0x - b1x * co1) * den, df * (c0y - b1y * co1) * den, df * (c0z - b1z * co1) * den);
+    }
+  }
+  add_energy(a, sys, E_DIHED, e);
+}
+
+// Scaled 1-4 Coulomb and Lennard-Jones (nbond with N14 = 1, diel = C;
+// src/sff/eff.c:1212-1310).  atoms = (i, j, 10-12 flag, 0);
+// par = (q_i q_j scee, c12, c6, scnb).
+__global__ void k_pairs14(const BondedArgs a, const int4 *atoms, const double4_32a *par, int n) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  int sys = -1;
+  double eel = 0.0, evdw = 0.0;
+  if (i < n) {
+    const int p = atoms[i].x, q = atoms[i].y;
+    sys = a.atom_sys[p];
+    if (!a.sys_active[sys]) {
+      sys = -1;
+    } else {
+      const double xij = a.x[3 * p] - a.x[3 * q], yij = a.x[3 * p + 1] - a.x[3 * q + 1], zij = a.x[3 * p + 2] - a.x[3 * q + 2];
+      const double r2 = xij * xij + yij * yij + zij * zij, r2inv = 1.0 / r2, r = sqrt(r2), rinv = r * r2inv;
+      const double rs = par[i].x * rinv, scnb = par[i].w;
+      eel = rs;
+      double df;
+      if (atoms[i].z == 0) {
+        const double r6 = r2inv * r2inv * r2inv, f2 = par[i].z * r6, f1 = par[i].y * r6 * r6;
+        evdw = (f1 - f2) * scnb;
+        df = (-rs + (6.0 * f2 - 12.0 * f1) * scnb) * rinv;
+      } else {
+        const double r10 = r2inv * r2inv * r2inv * r2inv * r2inv, f2 = par[i].z * r10, f1 = par[i].y * r10 * r2inv;
+        evdw = (f1 - f2) * scnb;
+        df = (-rs + (10.0 * f2 - 12.0 * f1) * scnb) * rinv;
+      }
+      df *= rinv;
+      add_force(a, p, df * xij, df * yij, df * zij);
+      add_force(a, q, -df * xij, -df * yij, -df * zij);
+    }
+  }
+  add_energy(a, sys, E_EEL14, eel);
+  add_energy(a, sys, E_ENB14, evdw);
+}
+
+// Fixed-point forces -> FP64 gradient in the caller's atom order; frozen
+// atoms get zero (src/sff/eff.c:2826-2834).
+__global__ void k_gather_grad(const long long *acc_fx, const long long *acc_fy, const long long *acc_fz,
+                              const int *atom_slot, const int *atom_frozen, const int *atom_sys,
+                              const int *sys_active, double *grad, int natom) {
+  const int a = blockIdx.x * blockDim.x + threadIdx.x;
+  if (a >= natom || !sys_active[atom_sys[a]]) return;
+  const int s = atom_slot[a];
+  const double k = 1.0 / 4294967296.0;
+  const bool fz = atom_frozen[a];
+  grad[3 * a] = fz ? 0.0 : static_cast<double>(acc_fx[s]) * k;
+  grad[3 * a + 1] = fz ? 0.0 : static_cast<double>(acc_fy[s]) * k;
+  grad[3 * a + 2] = fz ? 0.0 : static_cast<double>(acc_fz[s]) * k;
+}
+
+// Total energy per system from the fixed-point slots, summed in the
+// reference's ene[1..12] order (src/sff/eff.c:2871-2874).
+__global__ void k_energy_total(const long long *energy, double *etot, int nsys) {
+  const int s = blockIdx.x * blockDim.x + threadIdx.x;
+  if (s >= nsys) return;
+  const double k = 1.0 / 4294967296.0;
+  const long long *e = energy + s * 8;
+  double ene[13] = {0};
+  ene[1] = e[E_EVDW] * k;
+  ene[2] = e[E_EEL] * k;
+  ene[3] = e[E_BOND] * k;
+  ene[4] = e[E_ANGLE] * k;
+  ene[5] = e[E_DIHED] * k;
+  ene[7] = e[E_ENB14] * k;
+  ene[8] = e[E_EEL14] * k;
+  ene[10] = e[E_EGB] * k;
+  double t = 0.0;
+  for (int i = 1; i <= 12; i++) t += ene[i];
+  etot[s] = t;
+}
+
+// ------------------------------------------------------------ dynamics
+// Counter-based normal deviates for device-side Langevin noise: Philox4x32
+// (Salmon et al., SC'11, 10 rounds) feeding a Box-Muller transform.
+__device__ __forceinline__ uint4 philox4x32(uint4 c, uint2 k) {
+#pragma unroll
+  for (int r = 0; r < 10; r++) {
+    const unsigned hi0 = __umulhi(0xD2511F53u, c.x), lo0 = 0xD2511F53u * c.x;
+    const unsigned hi1 = __umulhi(0xCD9E8D57u, c.z), lo1 = 0xCD9E8D57u * c.z;
+    c = make_uint4(hi1 ^ c.y ^ k.x, lo1, hi0 ^ c.w ^ k.y, lo0);
+    k.x += 0x9E3779B9u;
+    k.y += 0xBB67AE85u;
+  }
+  return c;
+}
+
+__device__ __forceinline__ double normal_from(unsigned a, unsigned b) {
+  const double u1 = (static_cast<double>(a) + 1.0) * (1.0 / 4294967296.0);
+  const double u2 = static_cast<double>(b) * (1.0 / 4294967296.0);
+  return sqrt(-2.0 * log(u1)) * cospi(2.0 * u2);
+}
+
+struct MdArgs {
+  double *x, *v, *accel;
+  const double *grad, *minv, *sqrmass;
+  const int *atom_frozen, *atom_sys, *sys_active;
+  const double *noise;  // reference-stream draws (per coordinate) or null
+  double *tscal;        // per system (Berendsen)
+  long long *ekin;      // per system, fixed point 2^32
+  int n3;
+  double dtx, dt5, c_explic, c_implic, sdfac, vlimit, gammai;
+  unsigned long long seed;
+  unsigned step;
+};
+
+// First half of a step (src/sff/sff.c:2243-2248): half-kick and drift.
+__global__ void k_md_drift(const MdArgs a) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= a.n3) return;
+  const int sys = a.atom_sys[i / 3];
+  if (!a.sys_active[sys]) return;
+  double v = a.v[i];
+  v = a.gammai == 0.0 ? (v + a.accel[i]) * a.tscal[sys] : a.c_explic * v + a.accel[i];
+  v = fmin(a.vlimit, fmax(-a.vlimit, v));
+  a.v[i] = v;
+  a.x[i] += v * a.dtx;
+}
+
+// Force kick after the new gradient (src/sff/sff.c:2262-2276) and the
+// kinetic energy (2294-2306).  init = 1 only sets the accelerations of the
+// first force evaluation (2197-2215).
+__global__ void k_md_kick(const MdArgs a, int init) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  int sys = -1;
+  double ek = 0.0;
+  if (i < a.n3) {
+    const int at = i / 3;
+    sys = a.atom_sys[at];
+    if (!a.sys_active[sys]) {
+      sys = -1;
+    } else {
+      const double g = a.grad[i], minv = a.minv[i];
+      double v = a.v[i];
+      if (a.gammai == 0.0) {
+        const double acc = -g * minv * a.dt5;
+        a.accel[i] = acc;
+        if (!init) v = (v + acc) * a.tscal[sys];
+      } else if (!a.atom_frozen[at]) {
+        double z;
+        if (a.noise) {
+          z = a.noise[i];
+        } else {
+          const uint4 r = philox4x32(make_uint4(static_cast<unsigned>(i), a.step, 0x51u, 0u),
+                                     make_uint2(static_cast<unsigned>(a.seed), static_cast<unsigned>(a.seed >> 32)));
+          z = normal_from(r.x, r.y);
+        }
+        const double sd = a.sdfac * a.sqrmass[i];
+        const double acc = (-g + sd * z) * minv * a.dt5;
+        a.accel[i] = acc;
+        if (!init) v = (v + acc) * a.c_implic;
+      } else if (init) {
+        a.accel[i] = 0.0;
+      }
+      a.v[i] = v;
+      ek = v * v / minv;
+    }
+  }
+  // kinetic energy per system, fixed point; warps of one system use one atomic
+  const long long t = __double2ll_rn(ek * 4294967296.0);
+  const int s0 = __shfl_sync(kFull, sys, 0);
+  if (__all_sync(kFull, sys == s0 || sys < 0)) {
+    const long long tt = warp_sum_ll(sys >= 0 ? t : 0);
+    if ((threadIdx.x & 31) == 0 && s0 >= 0) atomic_add_ll(&a.ekin[s0], tt);
+  } else if (sys >= 0) {
+    atomic_add_ll(&a.ekin[sys], t);
+  }
+}
+
+}  // namespace sffg

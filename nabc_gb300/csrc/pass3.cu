@@ -1,0 +1,12 @@
+// Pass 3 of egb(): chain rule through the Born radii
+// (src/sff/eff.c:2131-2405).
+#include "passes.h"
+
+namespace sffg {
+
+void launch_chain(bool neck, int grid, cudaStream_t st, const DevTables &t) {
+  if (neck) k_chain<true><<<grid, 256, 0, st>>>(t);
+  else k_chain<false><<<grid, 256, 0, st>>>(t);
+}
+
+}  // namespace sffg

@@ -5,8 +5,9 @@
 // 2.5 A to an atom it is not bonded to (its two chain predecessors are
 // exempt), or outside the sphere of radius (3N/(4 pi 0.09))^(1/3) A, is
 // rejected.  When no placement works the chain backs up a few atoms and
-// regrows; when that keeps failing the sphere is enlarged by 1% (the
-// realised radius is reported).  Atom types C/N/O/H are drawn with
+// regrows; when that keeps failing the sphere is enlarged by 1% (a density
+// of 0.09/A^3 cannot be packed under the 2.5 A rule, so the realised radius
+// is reported and the realised density is lower).  Atom types C/N/O/H are drawn with
 // probabilities 0.32/0.09/0.09/0.50 with LJ (R*, eps) = (1.908, 0.086),
 // (1.824, 0.17), (1.6612, 0.21), (0.6, 0.0157); charges are N(0, 0.4^2)
 // shifted to net zero; intrinsic GB radii 1.7/1.55/1.5/1.2 A and screening
@@ -139,9 +140,11 @@ double synth_chain(int n, uint64_t seed, std::vector<V3> &pos) {
     }
   }
   for (int i = 0; i < n && i < 3; i++) grid.add(i, pos[i]);
-  int i = 3, consecutive_fail = 0;
-  long total_fail = 0;
-  const int tries = 48;
+  // Backtracking doubles (up to 64 atoms) while the chain fails to pass the
+  // furthest point it has reached; after kStall failures without progress
+  // the confining sphere grows by 1%.
+  int i = 3, consecutive_fail = 0, best = 3, stall = 0;
+  const int tries = 64, kStall = 48;
   while (i < n) {
     bool ok = false;
     for (int t = 0; t < tries; t++) {
@@ -154,16 +157,20 @@ double synth_chain(int n, uint64_t seed, std::vector<V3> &pos) {
     }
     if (ok) {
       i++;
-      if (consecutive_fail > 0) consecutive_fail--;
+      if (i > best) {
+        best = i;
+        stall = 0;
+        consecutive_fail = 0;
+      }
       continue;
     }
-    consecutive_fail++;
-    total_fail++;
-    if (total_fail > 20L * n + 1000) {
+    if (++stall > kStall) {
       radius *= 1.01;
-      total_fail = 0;
+      stall = 0;
+      consecutive_fail = 0;
     }
     int back = 1 << (consecutive_fail < 6 ? consecutive_fail : 6);
+    consecutive_fail++;
     for (int k = 0; k < back && i > 3; k++) {
       i--;
       grid.remove(i, pos[i]);

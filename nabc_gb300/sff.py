@@ -113,6 +113,25 @@ def lib():
     return L
 
 
+def set_output(path):
+    """Point the library's nabout stream (the reference's global output
+    FILE*) at a file; returns the previous FILE* value."""
+    libc = C.CDLL(None)
+    libc.fopen.restype = C.c_void_p
+    libc.fopen.argtypes = [C.c_char_p, C.c_char_p]
+    fp = libc.fopen(os.fsencode(path), b"a")
+    var = C.c_void_p.in_dll(lib(), "nabout")
+    old = var.value
+    var.value = fp
+    return old
+
+
+def flush_output():
+    libc = C.CDLL(None)
+    libc.fflush.argtypes = [C.c_void_p]
+    libc.fflush(C.c_void_p.in_dll(lib(), "nabout"))
+
+
 def dptr(a):
     return a.ctypes.data_as(REAL_P)
 

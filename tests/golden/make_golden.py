@@ -1,0 +1,190 @@
+"""Regenerate the golden fixtures under tests/golden/.
+
+Run in the development container, where the reference tree is mounted:
+
+    make -C oracle ref
+    python tests/golden/make_golden.py /root/reference
+
+It produces
+  ref/          the reference's own test inputs for the GB path (prmtops,
+                PDB/restart coordinates), copied unchanged;
+  checks.json   the reference's expected outputs parsed from its shipped
+                .check files (test/nab/{gbrna,gbtrx,gb5trx,gb7trx,gb8trx},
+                test/nab/aspgb8.out).  test/txmin.out.check is not used: its
+                driver evaluates through mme_rattle, which first moves the
+                atoms onto the RATTLE constraints;
+  synth/        small synthetic molecules (parm7 + rst7) from the
+                benchmark generator;
+  refrun.npz    outputs of the reference library itself (oracle/_ref/sffref,
+                compiled from the reference sources) on those inputs:
+                energy components, full gradients, conjgrad traces and a
+                short Langevin trajectory.
+"""
+import json
+import os
+import re
+import shutil
+import subprocess
+import sys
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+ROOT = os.path.dirname(os.path.dirname(HERE))
+sys.path.insert(0, ROOT)
+
+SFFREF = os.path.join(ROOT, "oracle", "_ref", "sffref")
+
+# (name, prmtop, coordinates, options, conjgrad args) for the reference's
+# GB regression tests (test/nab/*.nab, test/txmin.c)
+REF_CASES = [
+    ("gbrna", "nab/gbrna.prmtop", "nab/gbrna.pdb",
+     "ntpr=1, gb=1, kappa=0.10395, rgbmax=99., cut=99.0, diel=C", "gbrna.out.check"),
+    ("gbtrx", "nab/prmtop.gb2", "nab/trxox.2.4ns.pdb",
+     "ntpr=1, gb=2, kappa=0.14701, rgbmax=99.0, cut=99.0, diel=C", "gbtrx.out.check"),
+    ("gb5trx", "nab/prmtop.gb2", "nab/trxox.2.4ns.pdb",
+     "ntpr=1, gb=5, kappa=0.14701, rgbmax=99.0, cut=99.0, diel=C", "gb5trx.out.check"),
+    ("gb7trx", "nab/prmtop.gb2", "nab/trxox.2.4ns.pdb",
+     "ntpr=1, gb=7, rgbmax=15.0, cut=99.0, diel=C, e_debug=0", "gb7trx.out.check"),
+    ("gb8trx", "nab/prmtop.gb2", "nab/trxox.2.4ns.pdb",
+     "ntpr=1, gb=8, rgbmax=15.0, cut=99.0, diel=C, e_debug=0", "gb8trx.out.check"),
+]
+EXTRA_INPUTS = ["nab/asp.top", "nab/asp.pdb", "xfin.parm7", "xfin.rst7"]
+
+BREAKDOWN = ["bond", "angle", "dihedral", "enb14", "eel14", "enb", "eel", "egb", "econs", "esurf", "Total",
+             "frms"]
+
+# synthetic cases: (name, natom, seed, options)
+SYNTH = [
+    ("s300_gb1", 300, 11, "gb=1, cut=999.0, rgbmax=15.0"),
+    ("s300_gb2", 300, 11, "gb=2, cut=999.0, rgbmax=15.0"),
+    ("s300_gb5", 300, 11, "gb=5, cut=999.0, rgbmax=15.0"),
+    ("s300_gb7", 300, 11, "gb=7, cut=999.0, rgbmax=15.0"),
+    ("s300_gb8", 300, 11, "gb=8, cut=999.0, rgbmax=25.0"),
+    ("s1000_gb5_cut", 1000, 12, "gb=5, cut=12.0, rgbmax=10.0, nsnb=10"),
+    ("s1000_gb8_cut", 1000, 12, "gb=8, cut=14.0, rgbmax=12.0, nsnb=10"),
+    ("s1000_gb1_kappa", 1000, 13, "gb=1, cut=999.0, rgbmax=15.0, kappa=0.10395"),
+]
+
+
+def run(args, cwd=None):
+    r = subprocess.run(args, capture_output=True, text=True, cwd=cwd)
+    if r.returncode != 0:
+        raise RuntimeError(f"{args}: {r.stderr}")
+    return r.stdout
+
+
+def parse_ff(text):
+    rows = []
+    for line in text.splitlines():
+        if line.startswith("ff:"):
+            f = line.split()
+            rows.append([int(f[1])] + [float(v) for v in f[2:]])
+    return rows
+
+
+def parse_breakdown(text):
+    out = {}
+    for line in text.splitlines():
+        m = re.match(r"\s*(\w+):\s+([-+0-9.eE]+)\s*$", line)
+        if m and m.group(1) in BREAKDOWN and m.group(1) not in out:
+            out[m.group(1)] = float(m.group(2))
+    return out
+
+
+def read_dump(path):
+    with open(path, "rb") as f:
+        n = int(np.frombuffer(f.read(4), np.int32)[0])
+        e = float(np.frombuffer(f.read(8), np.float64)[0])
+        x = np.frombuffer(f.read(24 * n), np.float64).copy()
+        g = np.frombuffer(f.read(24 * n), np.float64).copy()
+    return n, e, x, g
+
+
+def main():
+    refroot = sys.argv[1] if len(sys.argv) > 1 else "/root/reference"
+    test = os.path.join(refroot, "test")
+    if not os.path.exists(SFFREF):
+        raise SystemExit("build the reference first: make -C oracle ref")
+    os.makedirs(os.path.join(HERE, "ref"), exist_ok=True)
+    os.makedirs(os.path.join(HERE, "synth"), exist_ok=True)
+    files = sorted({c[1] for c in REF_CASES} | {c[2] for c in REF_CASES} | set(EXTRA_INPUTS))
+    for rel in files:
+        shutil.copyfile(os.path.join(test, rel), os.path.join(HERE, "ref", os.path.basename(rel)))
+    checks = {}
+    arrays = {}
+    tmp = os.path.join(HERE, "_tmp.bin")
+    # reference regression tests: shipped .check outputs and our runs of the reference
+    for name, prm, crd, opts, check in REF_CASES:
+        text = open(os.path.join(test, "nab", check)).read()
+        checks[name] = {"prmtop": os.path.basename(prm), "coords": os.path.basename(crd), "options": opts,
+                        "ff": parse_ff(text),
+                        "conjgrad_returns": int(re.search(r"conjgrad returns (-?\d+)", text).group(1))}
+        out = run([SFFREF, os.path.join(HERE, "ref", os.path.basename(prm)),
+                   os.path.join(HERE, "ref", os.path.basename(crd)), "sp", opts, tmp])
+        n, e, x, g = read_dump(tmp)
+        checks[name]["sp"] = parse_breakdown(out)
+        arrays[f"{name}_x"] = x
+        arrays[f"{name}_g"] = g
+    # xfin (418 atoms, gb=1, kappa, all pairs) through the reference library
+    opts = "ntpr=1, gb=1, kappa=0.10395, rgbmax=99., cut=99.0, diel=C"
+    out = run([SFFREF, os.path.join(HERE, "ref", "xfin.parm7"), os.path.join(HERE, "ref", "xfin.rst7"), "sp",
+               opts, tmp])
+    n, e, x, g = read_dump(tmp)
+    checks["xfin"] = {"prmtop": "xfin.parm7", "coords": "xfin.rst7", "options": opts, "sp": parse_breakdown(out)}
+    arrays["xfin_x"] = x
+    arrays["xfin_g"] = g
+    # aspgb8: per-atom Born radii and breakdown (test/nab/aspgb8.out, which
+    # the current reference reproduces; the .check file is stale)
+    text = open(os.path.join(test, "nab", "aspgb8.out")).read()
+    radii = {}
+    for line in text.splitlines():
+        m = re.match(r"(\d+)\t\s*([0-9.]+)\t\s*([0-9.]+)$", line)
+        if m:
+            radii[int(m.group(1))] = float(m.group(3))
+    checks["aspgb8"] = {"prmtop": "asp.top", "coords": "asp.pdb",
+                        "options": "rgbmax=100., cut=100.0, nsnb=999, gb=8, diel=C",
+                        "reff": [radii[i + 1] for i in range(len(radii))], "sp": parse_breakdown(text)}
+    # synthetic molecules through the reference library
+    from nabc_gb300 import sff
+    L = sff.lib()
+    for name, natom, seed, opts in SYNTH:
+        prm, x, radius = sff.synth_molecule(natom, seed)
+        base = os.path.join(HERE, "synth", f"n{natom}_s{seed}")
+        if not os.path.exists(base + ".parm7"):
+            L.wrparm(prm, (base + ".parm7").encode())
+            L.putxv((base + ".rst7").encode(), b"synthetic", natom, 0.0, sff.dptr(x), None)
+        sff.free_prm(prm)
+        out = run([SFFREF, base + ".parm7", base + ".rst7", "sp", opts, tmp])
+        n, e, xr, g = read_dump(tmp)
+        checks[name] = {"prmtop": os.path.basename(base) + ".parm7", "coords": os.path.basename(base) + ".rst7",
+                        "options": opts, "sp": parse_breakdown(out), "natom": natom}
+        arrays[f"{name}_x"] = xr
+        arrays[f"{name}_g"] = g
+    # conjgrad and Langevin dynamics of one synthetic molecule
+    base = os.path.join(HERE, "synth", "n300_s11")
+    opts = "gb=5, cut=999.0, rgbmax=15.0, ntpr=1"
+    out = run([SFFREF, base + ".parm7", base + ".rst7", "cg", opts, "20", "1.0", "0.01", tmp])
+    n, e, x, g = read_dump(tmp)
+    checks["s300_cg"] = {"prmtop": "n300_s11.parm7", "coords": "n300_s11.rst7", "options": opts,
+                         "ff": parse_ff(out), "maxiter": 20, "dfpred": 1.0, "rmsgrad": 0.01,
+                         "conjgrad_returns": int(re.search(r"conjgrad returns (-?\d+)", out).group(1)),
+                         "energy": e}
+    arrays["s300_cg_x"] = x
+    opts = "gb=5, cut=999.0, rgbmax=15.0, ntpr=10, gamma_ln=5.0, temp0=300.0, dt=0.001, ntpr_md=1, zerov=1"
+    out = run([SFFREF, base + ".parm7", base + ".rst7", "md", opts, "20", tmp])
+    n, e, x, v = read_dump(tmp)
+    md_lines = [[float(t) for t in line.split()[1:]] for line in out.splitlines() if line.startswith("md:")]
+    checks["s300_md"] = {"prmtop": "n300_s11.parm7", "coords": "n300_s11.rst7", "options": opts,
+                         "nsteps": 20, "md": md_lines}
+    arrays["s300_md_x"] = x
+    arrays["s300_md_v"] = v
+    os.remove(tmp)
+    with open(os.path.join(HERE, "checks.json"), "w") as f:
+        json.dump(checks, f, indent=1)
+    np.savez_compressed(os.path.join(HERE, "refrun.npz"), **arrays)
+    print("wrote", len(checks), "cases")
+
+
+if __name__ == "__main__":
+    main()
