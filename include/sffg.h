@@ -40,6 +40,12 @@ extern "C" {
 
 const char *sffg_last_error(void);
 
+/* Restores every mm_options() setting to the reference's defaults
+ * (src/sff/sff.c:68-199).  mm_options() settings are cumulative, as in the
+ * reference; this gives test harnesses and long-lived services a clean
+ * start. */
+void sffg_options_reset(void);
+
 /* ---- synthetic molecules (benchmarks and tests) ------------------------ */
 
 /* A compact self-avoiding chain molecule of natom atoms generated from seed

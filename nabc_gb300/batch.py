@@ -1,0 +1,103 @@
+"""Python handle for the batched C API (include/sffg.h)."""
+import ctypes as C
+
+import numpy as np
+
+from . import sff
+
+
+class SffgError(RuntimeError):
+    pass
+
+
+def _check(rc, what):
+    if rc != 0:
+        msg = sff.lib().sffg_last_error()
+        raise SffgError(f"{what}: status {rc}: {msg.decode() if msg else ''}")
+
+
+class Batch:
+    """Many independent systems resident on the GPU, evaluated together."""
+
+    def __init__(self, opts):
+        L = sff.lib()
+        self.h = C.c_void_p()
+        _check(L.sffg_batch_create(opts.encode(), C.byref(self.h)), "sffg_batch_create")
+        self.natoms = []
+
+    def add(self, prm, x, frozen=None):
+        L = sff.lib()
+        idx = C.c_int(-1)
+        fz = None if frozen is None else sff.iptr(np.ascontiguousarray(frozen, np.int32))
+        x = np.ascontiguousarray(x, np.float64)
+        _check(L.sffg_batch_add_system(self.h, prm, fz, sff.dptr(x), C.byref(idx)), "add_system")
+        self.natoms.append(prm.contents.Natom)
+        return idx.value
+
+    def finalize(self):
+        _check(sff.lib().sffg_batch_finalize(self.h), "finalize")
+        return self
+
+    def set_coords(self, s, x, stream=None):
+        x = np.ascontiguousarray(x, np.float64)
+        _check(sff.lib().sffg_batch_set_coords(self.h, s, sff.dptr(x), stream), "set_coords")
+
+    def coords(self, s):
+        x = np.zeros(3 * self.natoms[s])
+        _check(sff.lib().sffg_batch_get_coords(self.h, s, sff.dptr(x), None), "get_coords")
+        return x
+
+    def eval(self, rebuild=False, stream=None):
+        _check(sff.lib().sffg_batch_eval(self.h, int(rebuild), stream), "eval")
+
+    def energy(self, s):
+        e = np.zeros(13)
+        _check(sff.lib().sffg_batch_get_energy(self.h, s, sff.dptr(e), None), "get_energy")
+        return e
+
+    def grad(self, s):
+        g = np.zeros(3 * self.natoms[s])
+        _check(sff.lib().sffg_batch_get_grad(self.h, s, sff.dptr(g), None), "get_grad")
+        return g
+
+    def reff(self, s):
+        r = np.zeros(self.natoms[s])
+        _check(sff.lib().sffg_batch_get_reff(self.h, s, sff.dptr(r), None), "get_reff")
+        return r
+
+    def velocities(self, s):
+        v = np.zeros(3 * self.natoms[s])
+        _check(sff.lib().sffg_batch_get_velocities(self.h, s, sff.dptr(v), None), "get_velocities")
+        return v
+
+    def set_velocities(self, s, v):
+        v = np.ascontiguousarray(v, np.float64)
+        _check(sff.lib().sffg_batch_set_velocities(self.h, s, sff.dptr(v), None), "set_velocities")
+
+    def num_pairs(self, s):
+        return sff.lib().sffg_batch_num_pairs(self.h, s)
+
+    def md(self, nsteps, stream=None):
+        _check(sff.lib().sffg_batch_md(self.h, nsteps, stream), "md")
+
+    def cg(self, maxiter, rmsgrad, dfpred=1.0, stream=None):
+        n = len(self.natoms)
+        st = np.zeros(n, np.int32)
+        en = np.zeros(n)
+        _check(sff.lib().sffg_batch_cg(self.h, maxiter, rmsgrad, dfpred, sff.iptr(st), sff.dptr(en), stream),
+               "cg")
+        return st, en
+
+    def device_bytes(self):
+        return sff.lib().sffg_batch_device_bytes(self.h)
+
+    def close(self):
+        if self.h:
+            sff.lib().sffg_batch_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass

@@ -204,7 +204,7 @@ int Batch::upload() {
   std::vector<int> slot_atom(nslot_, -1), param(nslot_, 0), tile_sys(ntile_, 0);
   std::vector<unsigned> tile_valid(ntile_, 0u);
   std::vector<float> q32(nslot_, 0.f);
-  std::vector<float4> gbpar(nslot_, make_float4(1.f, 0.f, 1.f, 1.f));
+  std::vector<float4> gbpar(nslot_, make_float4(1.f, 0.f, 1.f, 0.f));
   std::vector<double> rb64(nslot_, 1.0), q64(nslot_, 0.0), al(nslot_, 0.0), be(nslot_, 0.0), ga(nslot_, 0.0);
   std::vector<int> atom_slot(natom_total_), atom_sys(natom_total_), atom_frozen(natom_total_);
   std::vector<double> x(3 * static_cast<size_t>(natom_total_)), minv(3 * static_cast<size_t>(natom_total_)),
@@ -254,9 +254,10 @@ int Batch::upload() {
       atom_slot[a] = sl;
       atom_sys[a] = s;
       atom_frozen[a] = hs.frozen[i];
-      const double rho = hs.rborn[i] - off;
-      gbpar[sl] = make_float4(static_cast<float>(rho), static_cast<float>(hs.fs[i] * rho),
-                              static_cast<float>(hs.rborn[i]), static_cast<float>(1.0 / rho));
+      const double rho = hs.rborn[i] - off, sd = hs.fs[i] * rho;
+      const float sf = static_cast<float>(sd);
+      const float scorr = sf != 0.0f ? static_cast<float>(3.0 * (sd - static_cast<double>(sf)) / sf) : 0.0f;
+      gbpar[sl] = make_float4(static_cast<float>(rho), sf, static_cast<float>(hs.rborn[i]), scorr);
       param[sl] = (hs.type[i] & 0xffff) | (hs.neck[i] << 16) | (hs.frozen[i] ? (1 << 24) : 0);
       q32[sl] = static_cast<float>(hs.q[i]);
       q64[sl] = hs.q[i];

@@ -29,7 +29,7 @@ struct DevTables {
   // per slot
   const float4 *pos_hi;   // x, y, z (high part), q
   const float4 *pos_lo;   // x, y, z (low part), 0
-  const float4 *gbpar;    // rho = rborn - offset, s = fs * rho, rborn, 1/rho
+  const float4 *gbpar;    // rho = rborn - offset, s = fs * rho, rborn, 3 (s - fl(s)) / fl(s)
   const int *param;       // LJ type | neck index << 16 | frozen << 24
   const float *reff32;    // effective Born radius (pass 2)
   const float *rinv2;     // sqrt(log2(e)/4) / reff (pass 2)
@@ -144,7 +144,7 @@ __global__ void __launch_bounds__(256, 2) k_born(const DevTables t) {
   const int nitems = *t.nitems;
   const float cut2 = t.born.cutoff2 * 1.0001f + 1e-3f;
   int cur_I = -1;
-  float xi = 0, yi = 0, zi = 0, xli = 0, yli = 0, zli = 0, rhoi = 1, si = 0, rbi = 0, rhoinvi = 1;
+  float xi = 0, yi = 0, zi = 0, xli = 0, yli = 0, zli = 0, rhoi = 1, si = 0, rbi = 0, sci = 0;
   int nki = 0;
   long long sumi64 = 0;
   for (;;) {
@@ -163,7 +163,7 @@ __global__ void __launch_bounds__(256, 2) k_born(const DevTables t) {
         const int sl = I * 32 + lane;
         const float4 h = t.pos_hi[sl], l = t.pos_lo[sl], g = t.gbpar[sl];
         xi = h.x; yi = h.y; zi = h.z; xli = l.x; yli = l.y; zli = l.z;
-        rhoi = g.x; si = g.y; rbi = g.z; rhoinvi = g.w;
+        rhoi = g.x; si = g.y; rbi = g.z; sci = g.w;
         nki = (t.param[sl] >> 16) & 0xff;
       }
       const int sj = J * 32 + lane;
@@ -188,8 +188,10 @@ __global__ void __launch_bounds__(256, 2) k_born(const DevTables t) {
           const bool in = ((row >> j) & 1u) && r2 <= t.born.cutoff2;
           const float dij1i = rsqrt_nr(r2);
           const float dij = r2 * dij1i;
-          float ti = descreen(t.born, dij, r2, dij1i, rhoi, rhoinvi, gp.y);
-          float tj = descreen(t.born, dij, r2, dij1i, gp.x, gp.w, si);
+          float ti = descreen(t.born, dij, r2, dij1i, rhoi, gp.y);
+          float tj = descreen(t.born, dij, r2, dij1i, gp.x, si);
+          ti = fmaf(ti, gp.w, ti);
+          tj = fmaf(tj, sci, tj);
           if (NECK) {
             if (dij < rbi + gp.z + 6.8f) {
               const int nkj = (sm_par[w][j] >> 16) & 0xff;
@@ -354,7 +356,7 @@ __global__ void __launch_bounds__(256, 2) k_chain(const DevTables t) {
   const float cut2 = t.born.cutoff2 * 1.0001f + 1e-3f;
   const float FS = 4294967296.0f;
   int cur_I = -1;
-  float xi = 0, yi = 0, zi = 0, xli = 0, yli = 0, zli = 0, rhoi = 1, si = 0, rbi = 0, rhoinvi = 1, sdai = 0;
+  float xi = 0, yi = 0, zi = 0, xli = 0, yli = 0, zli = 0, rhoi = 1, si = 0, rbi = 0, sci = 0, sdai = 0;
   int nki = 0;
   long long fx64 = 0, fy64 = 0, fz64 = 0;
   auto flush_i = [&]() {
@@ -379,7 +381,7 @@ __global__ void __launch_bounds__(256, 2) k_chain(const DevTables t) {
         const int sl = I * 32 + lane;
         const float4 h = t.pos_hi[sl], l = t.pos_lo[sl], g = t.gbpar[sl];
         xi = h.x; yi = h.y; zi = h.z; xli = l.x; yli = l.y; zli = l.z;
-        rhoi = g.x; si = g.y; rbi = g.z; rhoinvi = g.w;
+        rhoi = g.x; si = g.y; rbi = g.z; sci = g.w;
         sdai = t.sumda32[sl];
         nki = (t.param[sl] >> 16) & 0xff;
       }
@@ -409,8 +411,10 @@ __global__ void __launch_bounds__(256, 2) k_chain(const DevTables t) {
           const bool in = ((row >> j) & 1u) && r2 <= t.born.cutoff2;
           const float dij1i = rsqrt_nr(r2);
           const float dij = r2 * dij1i;
-          float di = descreen_deriv(t.born, dij, r2, dij1i, rhoi, rhoinvi, gp.y);
-          float dj = descreen_deriv(t.born, dij, r2, dij1i, gp.x, gp.w, si);
+          float di = descreen_deriv(t.born, dij, r2, dij1i, rhoi, gp.y);
+          float dj = descreen_deriv(t.born, dij, r2, dij1i, gp.x, si);
+          di = fmaf(di, gp.w, di);
+          dj = fmaf(dj, sci, dj);
           if (NECK) {
             if (dij < rbi + gp.z + 6.8f) {
               const int nkj = (sm_par[w][j] >> 16) & 0xff;

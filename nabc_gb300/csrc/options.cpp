@@ -230,6 +230,8 @@ int parse_options(const char *opts, Options &o, bool echo, bool fail_stop, std::
 
 }  // namespace sffg
 
+extern "C" void sffg_options_reset(void) { sffg::options() = sffg::Options(); }
+
 extern "C" INT_T mm_options(STRING_T *opts) {
   sffg::parse_options(opts, sffg::options(), true, true, nullptr);
   return 0;

@@ -89,6 +89,8 @@ def lib():
         L.conjgrad.restype = C.c_int
         L.mme_timer.argtypes = []
         L.mme_timer.restype = C.c_int
+        L.sffg_options_reset.argtypes = []
+        L.sffg_options_reset.restype = None
         L.sffg_last_error.argtypes = []
         L.sffg_last_error.restype = C.c_char_p
         vp = C.c_void_p
@@ -188,13 +190,19 @@ def read_pdb_coords(path, n):
 
 
 class Session:
-    """The legacy single-system session: mm_options + mme_init_sff + mme."""
+    """The legacy single-system session: mm_options + mme_init_sff + mme.
 
-    def __init__(self, prm, opts, frozen=None):
+    Like the reference's mme_init_sff, the library borrows the frozen and
+    constrained arrays for the life of the session: keep this object alive
+    while the session is in use."""
+
+    def __init__(self, prm, opts, frozen=None, reset=True):
         L = lib()
         n = natom(prm)
         self.prm = prm
         self.n = n
+        if reset:
+            L.sffg_options_reset()
         L.mm_options(opts.encode())
         self.frozen = np.zeros(n, np.int32) if frozen is None else np.asarray(frozen, np.int32)
         self.constrained = np.zeros(n, np.int32)

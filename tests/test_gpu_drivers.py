@@ -1,0 +1,108 @@
+"""GPU: batches, the legacy drop-in entry points (mme / conjgrad / md) and
+the minimiser and integrator against the oracle."""
+import ctypes as C
+
+import numpy as np
+import pytest
+
+from conftest import load_case
+
+pytestmark = pytest.mark.gpu
+
+
+def test_batch_equals_individual(lib):
+    """A system's result is bit-identical alone and inside a mixed batch."""
+    from nabc_gb300 import sff
+    from nabc_gb300.batch import Batch
+    opts = "gb=5, cut=30.0, rgbmax=25.0"
+    mols = [sff.synth_molecule(n, 40 + n) for n in (150, 700, 1234, 64)]
+    alone = []
+    for prm, x, _ in mols:
+        b = Batch(opts)
+        b.add(prm, x)
+        b.finalize()
+        b.eval(rebuild=True)
+        alone.append((b.energy(0), b.grad(0)))
+        b.close()
+    b = Batch(opts)
+    for prm, x, _ in mols:
+        b.add(prm, x)
+    b.finalize()
+    b.eval(rebuild=True)
+    for s, (e, g) in enumerate(alone):
+        assert np.array_equal(b.energy(s), e)
+        assert np.array_equal(b.grad(s), g)
+    b.close()
+
+
+def test_legacy_mme_matches_oracle(lib, oracle_mod, checks):
+    """mm_options + mme_init_sff + mme(iter=-1), the reference's drop-in path."""
+    from nabc_gb300 import sff
+    c = checks["gb8trx"]
+    prm, x = load_case(c)
+    s = sff.Session(prm, c["options"])
+    e, g = s.mme(x, it=-1)
+    prm2, _ = load_case(c)
+    o = oracle_mod.Oracle(prm2, c["options"])
+    e0, ene0, g0, _ = o.mme(x)
+    assert abs(e - e0) <= 1e-6 * abs(e0)
+    assert np.sqrt(((g - g0) ** 2).mean()) <= 1e-5
+
+
+@pytest.mark.parametrize("name", ["gbrna", "gb5trx", "gb8trx"])
+def test_legacy_conjgrad_matches_check(lib, checks, name):
+    """conjgrad(..., mme, ...) reproduces the reference's 11 ff: totals
+    (printed with two decimals) and return code."""
+    from nabc_gb300 import sff
+    c = checks[name]
+    prm, x = load_case(c)
+    session = sff.Session(prm, c["options"])  # keeps the borrowed frozen/constrained arrays alive
+    L = sff.lib()
+    n = C.c_int(3 * prm.contents.Natom)
+    f = C.c_double(0.0)
+    rms = C.c_double(3 * prm.contents.Natom * 0.0001)
+    dfp = C.c_double(10.0)
+    maxit = C.c_int(10)
+    ret = L.conjgrad(sff.dptr(x), C.byref(n), C.byref(f), C.cast(L.mme, C.c_void_p), C.byref(rms),
+                     C.byref(dfp), C.byref(maxit))
+    assert ret == c["conjgrad_returns"]
+    assert f.value == pytest.approx(c["ff"][-1][1], abs=0.011)
+    del session
+
+
+def test_batched_conjgrad_matches_oracle(lib, oracle_mod, checks, refrun):
+    from nabc_gb300 import sff
+    from nabc_gb300.batch import Batch
+    c = checks["s300_cg"]
+    prm, x = load_case(c)
+    b = Batch(c["options"])
+    b.add(prm, x)
+    b.add(prm, x + 0.01)
+    b.finalize()
+    st, en = b.cg(c["maxiter"], c["rmsgrad"], c["dfpred"])
+    assert st[0] == c["conjgrad_returns"]
+    assert en[0] == pytest.approx(c["energy"], rel=1e-6)
+    o = oracle_mod.Oracle(prm, c["options"])
+    ret, f1, x1, _ = o.conjgrad(x + 0.01, c["rmsgrad"], c["dfpred"], c["maxiter"])
+    assert st[1] == ret
+    assert en[1] == pytest.approx(f1, rel=1e-6)
+    b.close()
+
+
+def test_legacy_md_reference_noise(lib, oracle_mod, checks, refrun):
+    """md(..., mme) on the device with the reference's noise stream tracks
+    the reference trajectory (20 Langevin steps)."""
+    from nabc_gb300 import sff
+    c = checks["s300_md"]
+    prm, x = load_case(c)
+    session = sff.Session(prm, c["options"])
+    L = sff.lib()
+    seed = C.c_int(-1)
+    L.setseed(C.byref(seed))
+    n = 3 * prm.contents.Natom
+    v = np.zeros(n)
+    f = np.zeros(n)
+    L.md(n, c["nsteps"], sff.dptr(x), sff.dptr(f), sff.dptr(v), C.cast(L.mme, C.c_void_p))
+    assert np.abs(x - refrun["s300_md_x"]).max() < 1e-5
+    assert np.abs(v - refrun["s300_md_v"]).max() < 1e-4
+    del session
