@@ -87,6 +87,11 @@ long long sffg_batch_num_pairs(sffg_batch *b, int sys);
  * integrator, src/sff/sff.c:2223-2354, options dt/temp0/gamma_ln/...).
  * Velocities start at zero unless set with sffg_batch_set_velocities. */
 int sffg_batch_md(sffg_batch *b, int nsteps, void *stream);
+/* The same integrator split for callers that drive it step by step: md_begin
+ * evaluates the first force and initial accelerations; md_steps advances
+ * nsteps steps numbered step0+1 .. step0+nsteps. */
+int sffg_batch_md_begin(sffg_batch *b, void *stream);
+int sffg_batch_md_steps(sffg_batch *b, int step0, int nsteps, void *stream);
 int sffg_batch_set_velocities(sffg_batch *b, int sys, const double *v, void *stream);
 int sffg_batch_get_velocities(sffg_batch *b, int sys, double *v, void *stream);
 
@@ -97,6 +102,16 @@ int sffg_batch_get_velocities(sffg_batch *b, int sys, double *v, void *stream);
  * energy; either may be NULL. */
 int sffg_batch_cg(sffg_batch *b, int maxiter, double rmsgrad, double dfpred, int *status,
                   double *energy, void *stream);
+
+/* Kernel launches issued by this batch since it was created. */
+long long sffg_batch_launch_count(const sffg_batch *b);
+/* With profiling on, the three pair passes of every evaluation are
+ * bracketed by CUDA events on the launching stream; kernel_times returns
+ * the accumulated device milliseconds of pass 1 (Born radii), pass 2 (GB +
+ * Coulomb + LJ) and pass 3 (chain rule) and the number of evaluations
+ * timed, then clears the accumulators. */
+int sffg_batch_set_profiling(sffg_batch *b, int on);
+int sffg_batch_kernel_times(sffg_batch *b, double *ms3, long long *nevals);
 
 /* Device memory the batch holds, in bytes. */
 size_t sffg_batch_device_bytes(const sffg_batch *b);

@@ -88,6 +88,24 @@ class Batch:
                "cg")
         return st, en
 
+    def md_begin(self, stream=None):
+        _check(sff.lib().sffg_batch_md_begin(self.h, stream), "md_begin")
+
+    def md_steps(self, step0, nsteps, stream=None):
+        _check(sff.lib().sffg_batch_md_steps(self.h, step0, nsteps, stream), "md_steps")
+
+    def launches(self):
+        return sff.lib().sffg_batch_launch_count(self.h)
+
+    def set_profiling(self, on=True):
+        _check(sff.lib().sffg_batch_set_profiling(self.h, int(on)), "set_profiling")
+
+    def kernel_times(self):
+        ms = (C.c_double * 3)()
+        n = C.c_longlong(0)
+        _check(sff.lib().sffg_batch_kernel_times(self.h, ms, C.byref(n)), "kernel_times")
+        return list(ms), n.value
+
     def device_bytes(self):
         return sff.lib().sffg_batch_device_bytes(self.h)
 

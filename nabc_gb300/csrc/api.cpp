@@ -112,6 +112,22 @@ extern "C" int sffg_batch_cg(sffg_batch *b, int maxiter, double rmsgrad, double 
   return SFFG_OK;
 }
 
+extern "C" int sffg_batch_md_begin(sffg_batch *b, void *stream) {
+  SFFG_WRAP(b->impl->md_begin(false, nullptr, nullptr, stream));
+}
+
+extern "C" int sffg_batch_md_steps(sffg_batch *b, int step0, int nsteps, void *stream) {
+  SFFG_WRAP(b->impl->md_steps(step0, nsteps, nullptr, nullptr, stream));
+}
+
+extern "C" long long sffg_batch_launch_count(const sffg_batch *b) { return b ? b->impl->launches() : 0; }
+
+extern "C" int sffg_batch_set_profiling(sffg_batch *b, int on) { SFFG_WRAP(b->impl->set_profiling(on != 0)); }
+
+extern "C" int sffg_batch_kernel_times(sffg_batch *b, double *ms3, long long *nevals) {
+  SFFG_WRAP(b->impl->kernel_times(ms3, nevals));
+}
+
 extern "C" size_t sffg_batch_device_bytes(const sffg_batch *b) { return b ? b->impl->device_bytes() : 0; }
 
 extern "C" int sffg_batch_destroy(sffg_batch *b) {

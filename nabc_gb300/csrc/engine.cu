@@ -81,13 +81,24 @@ struct DeviceState {
   // model tables
   DBuf<float> neck_pos, neck_val;
   // dynamics
-  DBuf<double> tscal, noise;
+  DBuf<double> tscal, noise, rndf;
   DBuf<long long> ekin;
   // minimisation
   DBuf<double> cg_w;
   DBuf<CgState> cg_state;
+  // per-pass timing: a ring of event pairs, read back lazily so that
+  // timing never stalls the host between evaluations
+  static constexpr int kRing = 64;
+  cudaEvent_t events[kRing][3][2] = {};
+  long long ev_head = 0, ev_tail = 0;  // recorded / collected evaluations
+  double pass_ms[3] = {0, 0, 0};
+  long long timed_evals = 0;
 
   ~DeviceState() {
+    for (auto &ring : events)
+      for (auto &pe : ring)
+        for (auto &e : pe)
+          if (e) cudaEventDestroy(e);
     if (stream) cudaStreamDestroy(stream);
     // DBuf members release in their own destructors? they are PODs: free here
     auto rel = [](auto &b) { b.release(); };
@@ -101,7 +112,7 @@ struct DeviceState {
     rel(minv); rel(sqrmass); rel(atom_slot); rel(atom_sys); rel(atom_frozen); rel(bond_atoms);
     rel(bond_par); rel(angle_par); rel(angle_atoms); rel(dih_atoms); rel(p14_atoms); rel(dih_par);
     rel(p14_par); rel(items); rel(masks); rel(counters); rel(neck_pos); rel(neck_val); rel(tscal);
-    rel(noise); rel(ekin); rel(cg_w); rel(cg_state);
+    rel(noise); rel(rndf); rel(ekin); rel(cg_w); rel(cg_state);
   }
 };
 
@@ -443,6 +454,16 @@ int Batch::upload() {
   SFFG_CK(cudaMemset(d.counters.p, 0, d.counters.bytes()));
   SFFG_CK(d.tscal.alloc(nsys));
   SFFG_CK(d.ekin.alloc(nsys));
+  {
+    // kinetic degrees of freedom per system: 3N minus frozen (sff.c:2142)
+    std::vector<double> rndf(nsys);
+    for (int s = 0; s < nsys; s++) {
+      int nf = 0;
+      for (int f : sys_[s].frozen) nf += f != 0;
+      rndf[s] = 3.0 * sys_[s].natom - 3.0 * nf;
+    }
+    SFFG_CK(up(d.rndf, rndf));
+  }
   std::vector<double> onesd(nsys, 1.0);
   SFFG_CK(cudaMemcpy(d.tscal.p, onesd.data(), nsys * sizeof(double), cudaMemcpyHostToDevice));
   d.grid_pair = d.nsm * pair_blocks_per_sm();
@@ -644,6 +665,7 @@ int Batch::build_lists(void *stream) {
     const int blocks = static_cast<int>((warps * 32 + threads - 1) / threads);
     k_build_list<<<blocks, threads, 0, st>>>(a);
     SFFG_CK(cudaGetLastError());
+    launches_++;
     int c[3];
     SFFG_CK(cudaMemcpyAsync(c, d.counters.p, sizeof(c), cudaMemcpyDeviceToHost, st));
     SFFG_CK(cudaStreamSynchronize(st));
@@ -702,11 +724,17 @@ int Batch::run_eval(bool rebuild, void *stream) {
   SFFG_CK(cudaGetLastError());
   // pass 1
   const bool neck = mp_.gb == 7 || mp_.gb == 8;
+  const int ring = static_cast<int>(d.ev_head % DeviceState::kRing);
+  if (profile_) {
+    if (d.ev_head - d.ev_tail >= DeviceState::kRing) collect_pass_times(d, 1);
+    SFFG_CK(cudaEventRecord(d.events[ring][0][0], st));
+  }
   {
     DevTables t = make_tables(d, mp_, fsmax, 3);
     launch_born(neck, d.grid_pair, st, t);
     SFFG_CK(cudaGetLastError());
   }
+  if (profile_) SFFG_CK(cudaEventRecord(d.events[ring][0][1], st));
   // Born radii, diagonal terms
   {
     FinishArgs f;
@@ -736,24 +764,34 @@ int Batch::run_eval(bool rebuild, void *stream) {
     SFFG_CK(cudaGetLastError());
   }
   // pass 2
+  if (profile_) SFFG_CK(cudaEventRecord(d.events[ring][1][0], st));
   {
     DevTables t = make_tables(d, mp_, fsmax, 4);
     launch_gbpair(mp_.kappa != 0.0, d.grid_pair, st, t);
     SFFG_CK(cudaGetLastError());
   }
+  if (profile_) SFFG_CK(cudaEventRecord(d.events[ring][1][1], st));
   k_chain_prep<<<(nslot_ + 255) / 256, 256, 0, st>>>(d.acc_sd.p, d.chainfac.p, d.param.p, d.slot_atom.p,
                                                      d.sumda32.p, nslot_);
   // pass 3
+  if (profile_) SFFG_CK(cudaEventRecord(d.events[ring][2][0], st));
   {
     DevTables t = make_tables(d, mp_, fsmax, 5);
     launch_chain(neck, d.grid_pair, st, t);
     SFFG_CK(cudaGetLastError());
+  }
+  if (profile_) {
+    SFFG_CK(cudaEventRecord(d.events[ring][2][1], st));
+    d.ev_head++;
   }
   k_gather_grad<<<(natom_total_ + 255) / 256, 256, 0, st>>>(d.acc_fx.p, d.acc_fy.p, d.acc_fz.p, d.atom_slot.p,
                                                             d.atom_frozen.p, d.atom_sys.p, d.sys_active.p,
                                                             d.grad.p, natom_total_);
   k_energy_total<<<(nsys + 127) / 128, 128, 0, st>>>(d.energy.p, d.etot.p, nsys);
   SFFG_CK(cudaGetLastError());
+  // pack, four bonded kinds (when present), three passes, Born finish,
+  // chain prep, gather, energy total
+  launches_ += 9 + (d.bond_atoms.n > 0) + (d.angle_atoms.n > 0) + (d.dih_atoms.n > 0) + (d.p14_atoms.n > 0);
   timers().nevals++;
   return SFFG_OK;
 }
@@ -783,6 +821,49 @@ long long Batch::num_pairs(int s) {
     }
   }
   return n;
+}
+
+// Reads back up to max_evals of the oldest recorded evaluations (all when
+// max_evals < 0).
+void Batch::collect_pass_times(DeviceState &d, long long max_evals) {
+  long long n = 0;
+  while (d.ev_tail < d.ev_head && (max_evals < 0 || n < max_evals)) {
+    const int r = static_cast<int>(d.ev_tail % DeviceState::kRing);
+    for (int k = 0; k < 3; k++) {
+      float ms = 0.f;
+      if (cudaEventSynchronize(d.events[r][k][1]) == cudaSuccess &&
+          cudaEventElapsedTime(&ms, d.events[r][k][0], d.events[r][k][1]) == cudaSuccess)
+        d.pass_ms[k] += ms;
+    }
+    d.timed_evals++;
+    d.ev_tail++;
+    n++;
+  }
+}
+
+int Batch::set_profiling(bool on) {
+  if (!finalized_) return SFFG_ESTATE;
+  DeviceState &d = *d_;
+  if (on && !d.events[0][0][0]) {
+    for (auto &ring : d.events)
+      for (auto &pe : ring)
+        for (auto &e : pe) SFFG_CK(cudaEventCreate(&e));
+  }
+  profile_ = on;
+  return SFFG_OK;
+}
+
+int Batch::kernel_times(double ms[3], long long *nevals) {
+  if (!finalized_) return SFFG_ESTATE;
+  DeviceState &d = *d_;
+  collect_pass_times(d, -1);
+  for (int k = 0; k < 3; k++) {
+    ms[k] = d.pass_ms[k];
+    d.pass_ms[k] = 0.0;
+  }
+  if (nevals) *nevals = d.timed_evals;
+  d.timed_evals = 0;
+  return SFFG_OK;
 }
 
 // ------------------------------------------------------------------ md
@@ -870,6 +951,7 @@ int Batch::md_begin(bool rebuild, NoiseFn noise, void *noise_ctx, void *stream) 
   const int nb = (a.n3 + 255) / 256;
   k_md_kick<<<nb, 256, 0, st>>>(a, 1);
   SFFG_CK(cudaGetLastError());
+  launches_++;
   return SFFG_OK;
 }
 
@@ -882,16 +964,7 @@ int Batch::md_steps(int step0, int k, NoiseFn noise, void *noise_ctx, void *stre
   double c_ave;
   md_args(*this, d, opts_, natom_total_, a, c_ave);
   const double boltz2 = 9.93595e-4;
-  std::vector<double> rndf(nsys), h;
-  for (int s = 0; s < nsys; s++) {
-    int nf = 0;
-    for (int f : sys_[s].frozen) nf += f != 0;
-    rndf[s] = 3.0 * sys_[s].natom - 3.0 * nf;
-  }
-  DBuf<double> d_rndf;
-  SFFG_CK(d_rndf.alloc(nsys));
-  SFFG_CK(cudaMemcpyAsync(d_rndf.p, rndf.data(), nsys * sizeof(double), cudaMemcpyHostToDevice, st));
-  if (d.etot.n && d.noise.n == 0 && noise) SFFG_CK(d.noise.alloc(a.n3));
+  std::vector<double> h;
   const int nb = (a.n3 + 255) / 256;
   int rc = SFFG_OK;
   for (int i = 1; i <= k; i++) {
@@ -906,13 +979,12 @@ int Batch::md_steps(int step0, int k, NoiseFn noise, void *noise_ctx, void *stre
     a.step = static_cast<unsigned>(nstep);
     SFFG_CK(cudaMemsetAsync(d.ekin.p, 0, d.ekin.bytes(), st));
     k_md_kick<<<nb, 256, 0, st>>>(a, 0);
+    launches_ += 3;  // drift, kick, tscal
     k_md_tscal<<<(nsys + 127) / 128, 128, 0, st>>>(d.ekin.p, d.tscal.p, nullptr, nsys,
-                                                   boltz2 * opts_.temp0, d_rndf.p, opts_.dt / opts_.tautp, c_ave,
+                                                   boltz2 * opts_.temp0, d.rndf.p, opts_.dt / opts_.tautp, c_ave,
                                                    a.gammai == 0.0);
     SFFG_CK(cudaGetLastError());
   }
-  SFFG_CK(cudaStreamSynchronize(st));
-  d_rndf.release();
   return rc;
 }
 
@@ -1225,6 +1297,7 @@ int Batch::cg(int maxiter, double rmsgrad, double dfpred, bool first_rebuild, st
     if (after_eval && (rc = after_eval(turn))) break;
     k_cg_post<<<nsys, kCgThreads, 0, st>>>(a);
     SFFG_CK(cudaGetLastError());
+    launches_++;
     if ((turn & 7) == 7 || turn == maxiter) {
       int na = 0;
       SFFG_CK(cudaMemcpyAsync(&na, nactive.p, sizeof(int), cudaMemcpyDeviceToHost, st));

@@ -94,6 +94,11 @@ class Batch {
   size_t device_bytes() const;
   std::string last_error;
 
+  // Launch counting and per-pass CUDA-event timing.
+  long long launches() const { return launches_; }
+  int set_profiling(bool on);
+  int kernel_times(double ms[3], long long *nevals);
+
   // Raw device views used by the legacy session.
   double *d_coords();
   double *d_grad();
@@ -103,13 +108,15 @@ class Batch {
   int upload();
   int build_lists(void *stream);
   int run_eval(bool rebuild, void *stream);
+  void collect_pass_times(DeviceState &d, long long max_evals);
   Options opts_;
   ModelParams mp_;
   std::vector<SystemInfo> sys_;
   std::vector<HostSystem> host_;
   std::vector<std::vector<double>> x0_;
   int natom_total_ = 0, nslot_ = 0, ntile_ = 0;
-  bool finalized_ = false, have_list_ = false;
+  bool finalized_ = false, have_list_ = false, profile_ = false;
+  long long launches_ = 0;
   std::unique_ptr<DeviceState> d_;
 };
 

@@ -108,6 +108,12 @@ def lib():
         L.sffg_batch_num_pairs.restype = C.c_longlong
         L.sffg_batch_md.argtypes = [vp, C.c_int, vp]
         L.sffg_batch_cg.argtypes = [vp, C.c_int, C.c_double, C.c_double, INT_P, REAL_P, vp]
+        L.sffg_batch_md_begin.argtypes = [vp, vp]
+        L.sffg_batch_md_steps.argtypes = [vp, C.c_int, C.c_int, vp]
+        L.sffg_batch_launch_count.argtypes = [vp]
+        L.sffg_batch_launch_count.restype = C.c_longlong
+        L.sffg_batch_set_profiling.argtypes = [vp, C.c_int]
+        L.sffg_batch_kernel_times.argtypes = [vp, C.POINTER(C.c_double), C.POINTER(C.c_longlong)]
         L.sffg_batch_device_bytes.argtypes = [vp]
         L.sffg_batch_device_bytes.restype = C.c_size_t
         L.sffg_batch_destroy.argtypes = [vp]
