@@ -176,7 +176,10 @@ def main():
     b = Batch(OPTS)
     b.add(prm, x)
     b.finalize()
-    stream = torch.cuda.current_stream()
+    # one explicit stream carries the flush, the timing events and every
+    # kernel of the library
+    stream = torch.cuda.Stream()
+    torch.cuda.set_stream(stream)
     sp = C.c_void_p(stream.cuda_stream)
     flush = torch.empty(256 * 1024 * 1024 // 4, dtype=torch.float32, device="cuda")
 

@@ -489,8 +489,10 @@ double *Batch::d_coords() { return d_ ? d_->x.p : nullptr; }
 double *Batch::d_grad() { return d_ ? d_->grad.p : nullptr; }
 void *Batch::default_stream() { return d_ ? d_->stream : nullptr; }
 
+// NULL selects the legacy default stream, as documented in sffg.h.
 static cudaStream_t pick(DeviceState &d, void *stream) {
-  return stream ? static_cast<cudaStream_t>(stream) : d.stream;
+  (void)d;
+  return stream ? static_cast<cudaStream_t>(stream) : cudaStreamLegacy;
 }
 
 int Batch::set_coords(int s, const double *x, void *stream) {

@@ -172,6 +172,7 @@ __global__ void __launch_bounds__(256, 2) k_born(const DevTables t) {
       sm_gb[w][lane] = t.gbpar[sj];
       if (NECK) sm_par[w][lane] = t.param[sj];
       const unsigned row = row_mask(t, it, lane);
+      const unsigned cols = __reduce_or_sync(kFull, row);
       __syncwarp();
       float acc_i = 0.0f, acc_j = 0.0f;
 #pragma unroll 1
@@ -180,12 +181,15 @@ __global__ void __launch_bounds__(256, 2) k_born(const DevTables t) {
 #pragma unroll
         for (int s = 0; s < 8; s++) {
           const int j = g * 8 + s;
+          aj[s] = 0.0f;
+          if (!((cols >> j) & 1u)) continue;  // j listed for no lane
           const float4 h = sm_hi[w][j], l = sm_lo[w][j], gp = sm_gb[w][j];
           const float dx = (xi - h.x) + (xli - l.x);
           const float dy = (yi - h.y) + (yli - l.y);
           const float dz = (zi - h.z) + (zli - l.z);
           const float r2 = fmaf(dx, dx, fmaf(dy, dy, dz * dz));
           const bool in = ((row >> j) & 1u) && r2 <= t.born.cutoff2;
+          if (!__any_sync(kFull, in)) continue;  // every lane out of range
           const float dij1i = rsqrt_nr(r2);
           const float dij = r2 * dij1i;
           float ti = descreen(t.born, dij, r2, dij1i, rhoi, gp.y);
@@ -278,6 +282,7 @@ __global__ void __launch_bounds__(256, 2) k_gbpair(const DevTables t) {
         sm_aux[w][lane] = make_float2(t.rinv2[sj], __int_as_float(t.param[sj] & 0xffff));
       }
       const unsigned row = row_mask(t, it, lane);
+      const unsigned cols = __reduce_or_sync(kFull, row);
       const unsigned exr = it.w < 0 ? 0u : t.excl_masks[static_cast<size_t>(it.w) * 32 + lane];
       __syncwarp();
       float fix = 0, fiy = 0, fiz = 0, sdi = 0, ep = 0, ee = 0, ev = 0;
@@ -288,6 +293,8 @@ __global__ void __launch_bounds__(256, 2) k_gbpair(const DevTables t) {
 #pragma unroll
         for (int s = 0; s < 8; s++) {
           const int j = g * 8 + s;
+          ax[s] = ay[s] = az[s] = as[s] = 0.0f;
+          if (!((cols >> j) & 1u)) continue;  // j listed for no lane
           const float4 h = sm_hi[w][j], l = sm_lo[w][j];
           const float2 au = sm_aux[w][j];
           const float dx = (xi - h.x) + (xli - l.x);
@@ -395,6 +402,7 @@ __global__ void __launch_bounds__(256, 2) k_chain(const DevTables t) {
         if (NECK) sm_par[w][lane] = t.param[sj];
       }
       const unsigned row = row_mask(t, it, lane);
+      const unsigned cols = __reduce_or_sync(kFull, row);
       __syncwarp();
       float fix = 0, fiy = 0, fiz = 0, jx = 0, jy = 0, jz = 0;
 #pragma unroll 1
@@ -403,12 +411,15 @@ __global__ void __launch_bounds__(256, 2) k_chain(const DevTables t) {
 #pragma unroll
         for (int s = 0; s < 8; s++) {
           const int j = g * 8 + s;
+          ax[s] = ay[s] = az[s] = 0.0f;
+          if (!((cols >> j) & 1u)) continue;
           const float4 h = sm_hi[w][j], l = sm_lo[w][j], gp = sm_gb[w][j];
           const float dx = (xi - h.x) + (xli - l.x);
           const float dy = (yi - h.y) + (yli - l.y);
           const float dz = (zi - h.z) + (zli - l.z);
           const float r2 = fmaf(dx, dx, fmaf(dy, dy, dz * dz));
           const bool in = ((row >> j) & 1u) && r2 <= t.born.cutoff2;
+          if (!__any_sync(kFull, in)) continue;
           const float dij1i = rsqrt_nr(r2);
           const float dij = r2 * dij1i;
           float di = descreen_deriv(t.born, dij, r2, dij1i, rhoi, gp.y);
