@@ -117,6 +117,46 @@ int sffg_batch_kernel_times(sffg_batch *b, double *ms3, long long *nevals);
 size_t sffg_batch_device_bytes(const sffg_batch *b);
 int sffg_batch_destroy(sffg_batch *b);
 
+/* ---- Born radii without allocation ------------------------------------- */
+
+/* Largest molecule sffg_born_radii_static accepts: its scratch is one fixed
+ * device array of SFFG_STATIC_MAX_ATOMS x 104 bytes (about 0.85 MB). */
+#define SFFG_STATIC_MAX_ATOMS 8192
+
+/* Effective Born radii of one molecule, every pair listed (pass 1 of the
+ * reference's egb() and its HCT/OBC radius formula, src/sff/eff.c:1566-1733,
+ * as when cut exceeds the molecule's extent).  No counterpart in the
+ * reference, which keeps the radii internal to egb().
+ *
+ * It allocates nothing: no cudaMalloc/cudaFree and no other allocating
+ * routine.  It is meant for callers that cannot allocate -- a host whose
+ * device memory is all owned by its own pool or budget, where one more
+ * cudaMalloc can fail or fragment it, or a loop that must not stall, which
+ * cudaFree would do by synchronising the device.  Every working buffer
+ * lives in one statically sized device array.
+ *
+ * x: 3*natom coordinates; rborn, fs: the topology's RADII and SCREEN values
+ * (PARMSTRUCT_T Rborn and Fs); gb: 1 (HCT), 2 (OBC I) or 5 (OBC II), with
+ * the reference's offset 0.09; reff: natom radii out.  All four are host
+ * arrays.  The call is ordered on stream (NULL: the legacy default stream)
+ * and returns once reff is written.
+ *
+ * The first call on a device does a one-time set-up with that device
+ * current: it looks up the device address of the static array.  Make that
+ * first call before any stream capture begins on the device.
+ *
+ * All calls on one device share the one array: calls whose GPU work
+ * overlaps (different streams or threads) race and corrupt each other's
+ * results, so serialise them.
+ *
+ * Returns SFFG_OK; SFFG_ENOMEM when natom > SFFG_STATIC_MAX_ATOMS (the
+ * molecule does not fit the static scratch); SFFG_EINVAL for natom < 1, a
+ * NULL array, another gb or rgbmax <= 0; SFFG_ENODEV / SFFG_ECUDA when no
+ * device is current or a CUDA call fails.  It does not update
+ * sffg_last_error(), which would need a host allocation. */
+int sffg_born_radii_static(int natom, const double *x, const double *rborn, const double *fs, int gb,
+                           double rgbmax, double *reff, void *stream);
+
 #ifdef __cplusplus
 }
 #endif
