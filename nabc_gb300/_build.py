@@ -13,7 +13,10 @@ import subprocess
 
 PKG = os.path.dirname(os.path.abspath(__file__))
 CSRC = os.path.join(PKG, "csrc")
-OUT = os.path.join(PKG, "_lib")
+# SFFG_BUILD_DIR and SFFG_NVCC_EXTRA build a variant (e.g. another tuning
+# constant, -DSFFG_GROUP=8) into another directory; load it with
+# SFFG_LIBRARY=<dir>/libsffg.so.
+OUT = os.environ.get("SFFG_BUILD_DIR", os.path.join(PKG, "_lib"))
 ROOT = os.path.dirname(PKG)
 
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
@@ -44,7 +47,8 @@ def _compile(src, obj, force):
             os.path.getmtime(obj) >= max(os.path.getmtime(src), _newest_header()):
         return None
     if src.endswith(".cu"):
-        cmd = [_nvcc()] + ARCH + NVCC_FLAGS + ["-I", CSRC, "-c", src, "-o", obj]
+        cmd = [_nvcc()] + ARCH + NVCC_FLAGS + os.environ.get("SFFG_NVCC_EXTRA", "").split() + \
+            ["-I", CSRC, "-c", src, "-o", obj]
     else:
         cmd = ["g++"] + CXX_FLAGS + ["-I", CSRC, "-I", "/usr/local/cuda/include", "-c", src, "-o", obj]
     r = subprocess.run(cmd, capture_output=True, text=True)

@@ -166,14 +166,36 @@ int Batch::add_system(PARMSTRUCT_T *prm, const int *frozen, const double *x, boo
 
 namespace {
 
-// Morton (Z-order) code of a point quantised to 10 bits per axis.
-uint32_t spread10(uint32_t v) {
-  v &= 0x3ff;
-  v = (v | (v << 16)) & 0x030000FF;
-  v = (v | (v << 8)) & 0x0300F00F;
-  v = (v | (v << 4)) & 0x030C30C3;
-  v = (v | (v << 2)) & 0x09249249;
-  return v;
+// Tile order: recursive balanced bisection of the atoms along the longest
+// extent of each group, the first part holding a whole number of 32-atom
+// tiles (about half).  Leaves are the tiles: compact boxes (about 9.5 A
+// across at protein-like densities, against 16 x 14 x 11 A for runs of a
+// Morton order), so far fewer tile pairs fall within a cutoff.  The one
+// short tile, if natom is not a multiple of 32, is the last.
+void bisect_tiles(const double *x, int *idx, int cnt) {
+  if (cnt <= 32) return;
+  double lo[3] = {1e300, 1e300, 1e300}, hi[3] = {-1e300, -1e300, -1e300};
+  for (int k = 0; k < cnt; k++)
+    for (int d = 0; d < 3; d++) {
+      const double v = x[3 * idx[k] + d];
+      if (!std::isfinite(v)) continue;
+      lo[d] = std::min(lo[d], v);
+      hi[d] = std::max(hi[d], v);
+    }
+  int ax = 0;
+  for (int d = 1; d < 3; d++)
+    if (hi[d] - lo[d] > hi[ax] - lo[ax]) ax = d;
+  const int nleft = ((cnt / 32 + 1) / 2) * 32;
+  auto key = [&](int a) {
+    const double v = x[3 * a + ax];
+    return std::isfinite(v) ? v : 0.0;  // a strict weak order even for NaN input
+  };
+  std::nth_element(idx, idx + nleft, idx + cnt, [&](int a, int b) {
+    const double xa = key(a), xb = key(b);
+    return xa < xb || (xa == xb && a < b);
+  });
+  bisect_tiles(x, idx, nleft);
+  bisect_tiles(x, idx + nleft, cnt - nleft);
 }
 
 }  // namespace
@@ -237,27 +259,13 @@ int Batch::upload() {
     const HostSystem &hs = host_[s];
     const std::vector<double> &xs = x0_[s];
     const int n = si.natom;
-    // spatial order: Morton code of the initial coordinates
-    double lo[3] = {1e300, 1e300, 1e300}, hi[3] = {-1e300, -1e300, -1e300};
-    for (int i = 0; i < n; i++)
-      for (int k = 0; k < 3; k++) {
-        lo[k] = std::min(lo[k], xs[3 * i + k]);
-        hi[k] = std::max(hi[k], xs[3 * i + k]);
-      }
-    double ext = std::max({hi[0] - lo[0], hi[1] - lo[1], hi[2] - lo[2], 1e-6});
-    std::vector<std::pair<uint32_t, int>> key(n);
-    for (int i = 0; i < n; i++) {
-      uint32_t c[3];
-      for (int k = 0; k < 3; k++) {
-        double u = (xs[3 * i + k] - lo[k]) / ext;
-        if (!(u >= 0.0)) u = 0.0;
-        c[k] = static_cast<uint32_t>(std::min(1023.0, u * 1023.0));
-      }
-      key[i] = {spread10(c[0]) | (spread10(c[1]) << 1) | (spread10(c[2]) << 2), i};
-    }
-    std::sort(key.begin(), key.end());
+    // spatial order: tiles from a balanced bisection of the initial
+    // coordinates
+    std::vector<int> order(n);
+    for (int i = 0; i < n; i++) order[i] = i;
+    bisect_tiles(xs.data(), order.data(), n);
     std::vector<int> local_slot(n);
-    for (int k = 0; k < n; k++) local_slot[key[k].second] = k;
+    for (int k = 0; k < n; k++) local_slot[order[k]] = k;
     for (int i = 0; i < n; i++) {
       const int sl = si.slot_off + local_slot[i];
       const int a = si.atom_off + i;

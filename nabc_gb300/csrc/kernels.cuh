@@ -63,31 +63,44 @@ __device__ __forceinline__ long long to_fixed(float v, float scale) {
   return __float2ll_rn(v * scale);
 }
 
-// Sum of v[e] over the 32 lanes for e = 0..7, delivered to lane 8*g + e
-// (zero in the other lanes).
-__device__ __forceinline__ float reduce8_to_lane(const float (&v)[8], int g, int lane) {
-  const bool b4 = lane & 16, b3 = lane & 8, b2 = lane & 4;
-  float a[4];
+// Steps per group of the pair loops: j-side partial sums are kept in
+// registers for kGroup steps, then folded across the warp.  Fewer steps per
+// group keep the unrolled loop body (and the instruction-cache footprint)
+// small at the cost of more shuffles per step.
+#ifndef SFFG_GROUP
+#define SFFG_GROUP 4
+#endif
+constexpr int kGroup = SFFG_GROUP;
+constexpr int kGroupLog2 = kGroup == 8 ? 3 : kGroup == 4 ? 2 : 1;
+static_assert(kGroup == 2 || kGroup == 4 || kGroup == 8, "group of 2, 4 or 8 steps");
+
+// Sum of v[e] over the 32 lanes for e = 0..K-1, delivered to lane K*g + e
+// (zero in the other lanes): log2(K) transposing shuffle stages (each lane
+// keeps half of its values and sends the other half across), then a plain
+// butterfly over the remaining lane bits.  After the transposing stages
+// lane L holds element L >> (5 - log2 K).
+__device__ __forceinline__ float reduce_to_lane(const float (&v)[kGroup], int g, int lane) {
+  float a[kGroup];
 #pragma unroll
-  for (int k = 0; k < 4; k++) {
-    float send = b4 ? v[k] : v[k + 4];
-    float keep = b4 ? v[k + 4] : v[k];
-    a[k] = keep + __shfl_xor_sync(kFull, send, 16);
-  }
-  float b[2];
+  for (int k = 0; k < kGroup; k++) a[k] = v[k];
+  int m = kGroup, dist = 16;
 #pragma unroll
-  for (int k = 0; k < 2; k++) {
-    float send = b3 ? a[k] : a[k + 2];
-    float keep = b3 ? a[k + 2] : a[k];
-    b[k] = keep + __shfl_xor_sync(kFull, send, 8);
+  for (int st = 0; st < kGroupLog2; st++) {
+    const bool b = lane & dist;
+    m >>= 1;
+#pragma unroll
+    for (int k = 0; k < m; k++) {
+      const float send = b ? a[k] : a[k + m];
+      const float keep = b ? a[k + m] : a[k];
+      a[k] = keep + __shfl_xor_sync(kFull, send, dist);
+    }
+    dist >>= 1;
   }
-  float send = b2 ? b[0] : b[1];
-  float keep = b2 ? b[1] : b[0];
-  float c = keep + __shfl_xor_sync(kFull, send, 4);
-  c += __shfl_xor_sync(kFull, c, 2);
-  c += __shfl_xor_sync(kFull, c, 1);
-  float r = __shfl_sync(kFull, c, (lane & 7) << 2);
-  return ((lane >> 3) == g) ? r : 0.0f;
+  float c = a[0];
+#pragma unroll
+  for (int d = 16 >> kGroupLog2; d > 0; d >>= 1) c += __shfl_xor_sync(kFull, c, d);
+  const float r = __shfl_sync(kFull, c, (lane & (kGroup - 1)) << (5 - kGroupLog2));
+  return (lane >> kGroupLog2) == g ? r : 0.0f;
 }
 
 __device__ __forceinline__ long long warp_sum_ll(long long v) {
@@ -123,6 +136,34 @@ __device__ __forceinline__ float box_dist2(const DevTables &t, int I, int J) {
   float dy = fmaxf(0.0f, fmaxf(al.y - bh.y, bl.y - ah.y));
   float dz = fmaxf(0.0f, fmaxf(al.z - bh.z, bl.z - ah.z));
   return dx * dx + dy * dy + dz * dz;
+}
+
+// Both directions of the descreening of one pair (value, or for DERIV the
+// derivative / dij): vi is atom i descreened by sphere j, vj the converse.
+// Only warp-uniform branches: the far-field Taylor form is evaluated for
+// every lane, the rgbmax-tail quadrature when any lane of the warp needs
+// it, and the near field (rare) out of line for the lanes that need it, so
+// a warp walks one short code path instead of a divergent ladder.
+template <bool DERIV>
+__device__ __forceinline__ void descreen_pair(const BornConst &c, bool in, float dij, float r2, float d1,
+                                              float rho_i, float s_i, float rho_j, float s_j, float &vi,
+                                              float &vj) {
+  vi = DERIV ? far_deriv(d1, s_j) : far_term(d1, s_j);
+  vj = DERIV ? far_deriv(d1, s_i) : far_term(d1, s_i);
+  const bool ti = dij > c.rgbmax - s_j, tj = dij > c.rgbmax - s_i;
+  if (__any_sync(kFull, in && (ti || tj))) {
+    const float qi = tail_quad<DERIV>(c.rgbmax, r2, dij, d1, s_j);
+    const float qj = tail_quad<DERIV>(c.rgbmax, r2, dij, d1, s_i);
+    vi = ti ? qi : vi;
+    vj = tj ? qj : vj;
+  }
+  const bool ni = in && !ti && dij <= 4.0f * s_j, nj = in && !tj && dij <= 4.0f * s_i;
+  if (__any_sync(kFull, ni || nj)) {
+    if (ni) vi = DERIV ? descreen_deriv_near(dij, r2, d1, rho_i, s_j) : descreen_near(dij, r2, d1, rho_i, s_j);
+    if (nj) vj = DERIV ? descreen_deriv_near(dij, r2, d1, rho_j, s_i) : descreen_near(dij, r2, d1, rho_j, s_i);
+  }
+  vi = dij > c.rgbmax + s_j ? 0.0f : vi;
+  vj = dij > c.rgbmax + s_i ? 0.0f : vj;
 }
 
 // ------------------------------------------------------------------ pass 1
@@ -176,11 +217,11 @@ __global__ void __launch_bounds__(256, 2) k_born(const DevTables t) {
       __syncwarp();
       float acc_i = 0.0f, acc_j = 0.0f;
 #pragma unroll 1
-      for (int g = 0; g < 4; g++) {
-        float aj[8];
+      for (int g = 0; g < 32 / kGroup; g++) {
+        float aj[kGroup];
 #pragma unroll
-        for (int s = 0; s < 8; s++) {
-          const int j = g * 8 + s;
+        for (int s = 0; s < kGroup; s++) {
+          const int j = g * kGroup + s;
           aj[s] = 0.0f;
           if (!((cols >> j) & 1u)) continue;  // j listed for no lane
           const float4 h = sm_hi[w][j], l = sm_lo[w][j], gp = sm_gb[w][j];
@@ -192,21 +233,24 @@ __global__ void __launch_bounds__(256, 2) k_born(const DevTables t) {
           if (!__any_sync(kFull, in)) continue;  // every lane out of range
           const float dij1i = rsqrt_nr(r2);
           const float dij = r2 * dij1i;
-          float ti = descreen(t.born, dij, r2, dij1i, rhoi, gp.y);
-          float tj = descreen(t.born, dij, r2, dij1i, gp.x, si);
+          float ti, tj;
+          descreen_pair<false>(t.born, in, dij, r2, dij1i, rhoi, si, gp.x, gp.y, ti, tj);
           ti = fmaf(ti, gp.w, ti);
           tj = fmaf(tj, sci, tj);
           if (NECK) {
-            if (dij < rbi + gp.z + 6.8f) {
+            const bool nk = in && dij < rbi + gp.z + 6.8f;
+            if (__any_sync(kFull, nk)) {
               const int nkj = (sm_par[w][j] >> 16) & 0xff;
-              ti += neck_term(dij, s_npos[nki * 21 + nkj], s_nval[nki * 21 + nkj], t.neck_scale);
-              tj += neck_term(dij, s_npos[nkj * 21 + nki], s_nval[nkj * 21 + nki], t.neck_scale);
+              const float a = neck_term(dij, s_npos[nki * 21 + nkj], s_nval[nki * 21 + nkj], t.neck_scale);
+              const float b = neck_term(dij, s_npos[nkj * 21 + nki], s_nval[nkj * 21 + nki], t.neck_scale);
+              ti += nk ? a : 0.0f;
+              tj += nk ? b : 0.0f;
             }
           }
           acc_i += in ? ti : 0.0f;
           aj[s] = in ? tj : 0.0f;
         }
-        acc_j += reduce8_to_lane(aj, g, lane);
+        acc_j += reduce_to_lane(aj, g, lane);
       }
       sumi64 += to_fixed(acc_i, 1099511627776.0f);
       if ((t.tile_valid[J] >> lane) & 1u) atomic_add_ll(&t.acc_sumi[sj], to_fixed(acc_j, 1099511627776.0f));
@@ -288,11 +332,11 @@ __global__ void __launch_bounds__(256, 2) k_gbpair(const DevTables t) {
       float fix = 0, fiy = 0, fiz = 0, sdi = 0, ep = 0, ee = 0, ev = 0;
       float jx = 0, jy = 0, jz = 0, jsd = 0;
 #pragma unroll 1
-      for (int g = 0; g < 4; g++) {
-        float ax[8], ay[8], az[8], as[8];
+      for (int g = 0; g < 32 / kGroup; g++) {
+        float ax[kGroup], ay[kGroup], az[kGroup], as[kGroup];
 #pragma unroll
-        for (int s = 0; s < 8; s++) {
-          const int j = g * 8 + s;
+        for (int s = 0; s < kGroup; s++) {
+          const int j = g * kGroup + s;
           ax[s] = ay[s] = az[s] = as[s] = 0.0f;
           if (!((cols >> j) & 1u)) continue;  // j listed for no lane
           const float4 h = sm_hi[w][j], l = sm_lo[w][j];
@@ -318,10 +362,10 @@ __global__ void __launch_bounds__(256, 2) k_gbpair(const DevTables t) {
           ee += in ? o.eel : 0.0f;
           ev += in ? o.evdw : 0.0f;
         }
-        jx += reduce8_to_lane(ax, g, lane);
-        jy += reduce8_to_lane(ay, g, lane);
-        jz += reduce8_to_lane(az, g, lane);
-        jsd += reduce8_to_lane(as, g, lane);
+        jx += reduce_to_lane(ax, g, lane);
+        jy += reduce_to_lane(ay, g, lane);
+        jz += reduce_to_lane(az, g, lane);
+        jsd += reduce_to_lane(as, g, lane);
       }
       fx64 += to_fixed(fix, FS);
       fy64 += to_fixed(fiy, FS);
@@ -406,11 +450,11 @@ __global__ void __launch_bounds__(256, 2) k_chain(const DevTables t) {
       __syncwarp();
       float fix = 0, fiy = 0, fiz = 0, jx = 0, jy = 0, jz = 0;
 #pragma unroll 1
-      for (int g = 0; g < 4; g++) {
-        float ax[8], ay[8], az[8];
+      for (int g = 0; g < 32 / kGroup; g++) {
+        float ax[kGroup], ay[kGroup], az[kGroup];
 #pragma unroll
-        for (int s = 0; s < 8; s++) {
-          const int j = g * 8 + s;
+        for (int s = 0; s < kGroup; s++) {
+          const int j = g * kGroup + s;
           ax[s] = ay[s] = az[s] = 0.0f;
           if (!((cols >> j) & 1u)) continue;
           const float4 h = sm_hi[w][j], l = sm_lo[w][j], gp = sm_gb[w][j];
@@ -422,15 +466,18 @@ __global__ void __launch_bounds__(256, 2) k_chain(const DevTables t) {
           if (!__any_sync(kFull, in)) continue;
           const float dij1i = rsqrt_nr(r2);
           const float dij = r2 * dij1i;
-          float di = descreen_deriv(t.born, dij, r2, dij1i, rhoi, gp.y);
-          float dj = descreen_deriv(t.born, dij, r2, dij1i, gp.x, si);
+          float di, dj;
+          descreen_pair<true>(t.born, in, dij, r2, dij1i, rhoi, si, gp.x, gp.y, di, dj);
           di = fmaf(di, gp.w, di);
           dj = fmaf(dj, sci, dj);
           if (NECK) {
-            if (dij < rbi + gp.z + 6.8f) {
+            const bool nk = in && dij < rbi + gp.z + 6.8f;
+            if (__any_sync(kFull, nk)) {
               const int nkj = (sm_par[w][j] >> 16) & 0xff;
-              di += neck_deriv(dij, s_npos[nki * 21 + nkj], s_nval[nki * 21 + nkj], t.neck_scale);
-              dj += neck_deriv(dij, s_npos[nkj * 21 + nki], s_nval[nkj * 21 + nki], t.neck_scale);
+              const float a = neck_deriv(dij, s_npos[nki * 21 + nkj], s_nval[nki * 21 + nkj], t.neck_scale);
+              const float b = neck_deriv(dij, s_npos[nkj * 21 + nki], s_nval[nkj * 21 + nki], t.neck_scale);
+              di += nk ? a : 0.0f;
+              dj += nk ? b : 0.0f;
             }
           }
           const float gg = in ? fmaf(sdai, di, l.w * dj) : 0.0f;
@@ -441,9 +488,9 @@ __global__ void __launch_bounds__(256, 2) k_chain(const DevTables t) {
           ay[s] = gg * dy;
           az[s] = gg * dz;
         }
-        jx += reduce8_to_lane(ax, g, lane);
-        jy += reduce8_to_lane(ay, g, lane);
-        jz += reduce8_to_lane(az, g, lane);
+        jx += reduce_to_lane(ax, g, lane);
+        jy += reduce_to_lane(ay, g, lane);
+        jz += reduce_to_lane(az, g, lane);
       }
       fx64 += to_fixed(fix, FS);
       fy64 += to_fixed(fiy, FS);
