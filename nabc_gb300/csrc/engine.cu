@@ -11,6 +11,7 @@
 #include "engine.h"
 #include "gbneck_tables.h"
 #include "kernels_aux.cuh"
+#include "lists.cuh"
 #include "passes.h"
 
 namespace sffg {
@@ -74,9 +75,15 @@ struct DeviceState {
   DBuf<double2> bond_par, angle_par;
   DBuf<int4> angle_atoms, dih_atoms, p14_atoms;
   DBuf<double4_32a> dih_par, p14_par;
-  // lists and work counters: 0 nitems, 1 nmasks, 2 overflow, 3..5 pass queues
-  DBuf<Item> items;
-  DBuf<unsigned> masks;
+  // pair lists (lists.cuh) and work counters: 0 candidates, 1 overflow,
+  // 2 chunks of list A, 3 chunks of list B, 4 list-B rebuild flag, 5..7
+  // pass queues
+  DBuf<int2> cand, cand_n, cand_off;
+  DBuf<unsigned> colA, colB, colE;
+  DBuf<int> cand_start, cand_count, chunksA, chunksB, chunk0A, chunk0B;
+  DBuf<int> chunkA_i, entA_slot, chunkB_i, entB_slot;
+  DBuf<unsigned> entA_col, entA_exc, entB_col;
+  DBuf<float4> xb;
   DBuf<int> counters;
   // model tables
   DBuf<float> neck_pos, neck_val;
@@ -111,7 +118,10 @@ struct DeviceState {
     rel(sys_atom_off); rel(lj); rel(energy); rel(etot); rel(x); rel(grad); rel(v); rel(accel);
     rel(minv); rel(sqrmass); rel(atom_slot); rel(atom_sys); rel(atom_frozen); rel(bond_atoms);
     rel(bond_par); rel(angle_par); rel(angle_atoms); rel(dih_atoms); rel(p14_atoms); rel(dih_par);
-    rel(p14_par); rel(items); rel(masks); rel(counters); rel(neck_pos); rel(neck_val); rel(tscal);
+    rel(p14_par); rel(cand); rel(cand_n); rel(cand_off); rel(colA); rel(colB); rel(colE);
+    rel(cand_start); rel(cand_count); rel(chunksA); rel(chunksB); rel(chunk0A); rel(chunk0B);
+    rel(chunkA_i); rel(entA_slot); rel(chunkB_i); rel(entB_slot); rel(entA_col); rel(entA_exc);
+    rel(entB_col); rel(xb); rel(counters); rel(neck_pos); rel(neck_val); rel(tscal);
     rel(noise); rel(rndf); rel(ekin); rel(cg_w); rel(cg_state);
   }
 };
@@ -360,27 +370,12 @@ int Batch::upload() {
     }
   }
   excl_tile_start[ntile_] = static_cast<int>(excl_tile_j.size());
-  // list capacities: every tile pair of a system could be listed
+  // candidate tile pairs: every tile pair of a system could be one
   long long cap = 0;
-  for (auto &s : sys_) cap += static_cast<long long>(s.ntile) * (s.ntile + 1) / 2;
-  if (cap > (1LL << 31) - 64) {
+  for (auto &sy : sys_) cap += static_cast<long long>(sy.ntile) * (sy.ntile + 1) / 2;
+  if (cap > (1LL << 31) / 32 - 64) {
     last_error = "batch too large for one pair list";
     return SFFG_ENOMEM;
-  }
-  // masks are needed only for tile pairs straddling the cutoff
-  long long mcap = 0;
-  for (int s = 0; s < nsys; s++) {
-    const std::vector<double> &xs = x0_[s];
-    double lo[3] = {1e300, 1e300, 1e300}, hi[3] = {-1e300, -1e300, -1e300};
-    for (int i = 0; i < sys_[s].natom; i++)
-      for (int k = 0; k < 3; k++) {
-        lo[k] = std::min(lo[k], xs[3 * i + k]);
-        hi[k] = std::max(hi[k], xs[3 * i + k]);
-      }
-    const double diag = std::sqrt((hi[0] - lo[0]) * (hi[0] - lo[0]) + (hi[1] - lo[1]) * (hi[1] - lo[1]) +
-                                  (hi[2] - lo[2]) * (hi[2] - lo[2]));
-    if (sys_[s].has_frozen || diag + 20.0 > mp_.cut)
-      mcap += static_cast<long long>(sys_[s].ntile) * (sys_[s].ntile + 1) / 2;
   }
   auto up = [&](auto &buf, const auto &vec) -> cudaError_t {
     cudaError_t e = buf.alloc(vec.size());
@@ -456,8 +451,14 @@ int Batch::upload() {
   SFFG_CK(cudaMemset(d.v.p, 0, d.v.bytes()));
   SFFG_CK(cudaMemset(d.accel.p, 0, d.accel.bytes()));
   SFFG_CK(cudaMemset(d.nonfinite.p, 0, d.nonfinite.bytes()));
-  SFFG_CK(d.items.alloc(static_cast<size_t>(cap)));
-  SFFG_CK(d.masks.alloc(static_cast<size_t>(std::max<long long>(mcap, 1)) * 32));
+  cand_max_ = cap;
+  SFFG_CK(d.cand_start.alloc(ntile_));
+  SFFG_CK(d.cand_count.alloc(ntile_));
+  SFFG_CK(d.chunksA.alloc(ntile_));
+  SFFG_CK(d.chunksB.alloc(ntile_));
+  SFFG_CK(d.chunk0A.alloc(ntile_));
+  SFFG_CK(d.chunk0B.alloc(ntile_));
+  SFFG_CK(d.xb.alloc(nslot_));
   SFFG_CK(d.counters.alloc(8));
   SFFG_CK(cudaMemset(d.counters.p, 0, d.counters.bytes()));
   SFFG_CK(d.tscal.alloc(nsys));
@@ -486,7 +487,10 @@ size_t Batch::device_bytes() const {
   b += d.q32.bytes() + d.reff32.bytes() + d.rinv2.bytes() + d.sumda32.bytes() + d.rborn64.bytes();
   b += d.q64.bytes() + d.alpha.bytes() + d.beta.bytes() + d.gamma.bytes() + d.reff64.bytes();
   b += d.psi64.bytes() + d.chainfac.bytes() + d.acc_sumi.bytes() + d.acc_sd.bytes() + d.acc_fx.bytes();
-  b += d.acc_fy.bytes() + d.acc_fz.bytes() + d.items.bytes() + d.masks.bytes() + d.x.bytes();
+  b += d.acc_fy.bytes() + d.acc_fz.bytes() + d.x.bytes();
+  b += d.cand.bytes() + d.cand_n.bytes() + d.cand_off.bytes() + d.colA.bytes() + d.colB.bytes() + d.colE.bytes();
+  b += d.chunkA_i.bytes() + d.entA_slot.bytes() + d.entA_col.bytes() + d.entA_exc.bytes();
+  b += d.chunkB_i.bytes() + d.entB_slot.bytes() + d.entB_col.bytes() + d.xb.bytes();
   b += d.grad.bytes() + d.v.bytes() + d.accel.bytes() + d.minv.bytes() + d.sqrmass.bytes();
   b += d.excl_masks.bytes() + d.cg_w.bytes() + d.noise.bytes();
   b += d.bond_par.bytes() + d.angle_par.bytes() + d.dih_par.bytes() + d.p14_par.bytes();
@@ -607,18 +611,21 @@ DevTables make_tables(DeviceState &d, const ModelParams &mp, double fsmax, int q
   t.reff32 = d.reff32.p;
   t.rinv2 = d.rinv2.p;
   t.sumda32 = d.sumda32.p;
-  t.tile_valid = d.tile_valid.p;
   t.tile_sys = d.tile_sys.p;
-  t.box_lo = d.box_lo.p;
-  t.box_hi = d.box_hi.p;
   t.sys_active = d.sys_active.p;
   t.sys_lj_off = d.sys_lj_off.p;
   t.sys_ntypes = d.sys_ntypes.p;
   t.lj = d.lj.p;
-  t.items = d.items.p;
-  t.nitems = d.counters.p + 0;
-  t.masks = d.masks.p;
-  t.excl_masks = d.excl_masks.p;
+  t.la.chunk_i = d.chunkA_i.p;
+  t.la.slot = d.entA_slot.p;
+  t.la.col = d.entA_col.p;
+  t.la.exc = d.entA_exc.p;
+  t.la.nchunk = d.counters.p + 2;
+  t.lb.chunk_i = d.chunkB_i.p;
+  t.lb.slot = d.entB_slot.p;
+  t.lb.col = d.entB_col.p;
+  t.lb.exc = nullptr;
+  t.lb.nchunk = d.counters.p + 3;
   t.counter = d.counters.p + queue;
   t.acc_sumi = d.acc_sumi.p;
   t.acc_sd = d.acc_sd.p;
@@ -639,57 +646,159 @@ DevTables make_tables(DeviceState &d, const ModelParams &mp, double fsmax, int q
   return t;
 }
 
+namespace {
+
+// Squared list-B cutoff: rgbmax + Fsmax + skin.
+double list_b_cut2(const ModelParams &mp, double fsmax) {
+  const double c = mp.rgbmax + fsmax + kListSkin;
+  return c * c;
+}
+
+template <class T>
+cudaError_t ensure(DBuf<T> &b, size_t n) {
+  if (b.n >= n) return cudaSuccess;
+  return b.alloc(std::max(n, b.n + b.n / 4));
+}
+
+}  // namespace
+
+ListArgs Batch::list_args(double fsmax) {
+  DeviceState &d = *d_;
+  ListArgs a;
+  a.pos_hi = d.pos_hi.p;
+  a.pos_lo = d.pos_lo.p;
+  a.box_lo = d.box_lo.p;
+  a.box_hi = d.box_hi.p;
+  a.x = d.x.p;
+  a.slot_atom = d.slot_atom.p;
+  a.param = d.param.p;
+  a.tile_valid = d.tile_valid.p;
+  a.tile_sys = d.tile_sys.p;
+  a.sys_tile_end = d.sys_tile_end.p;
+  a.sys_active = d.sys_active.p;
+  a.excl_tile_start = d.excl_tile_start.p;
+  a.excl_tile_j = d.excl_tile_j.p;
+  a.excl_tile_idx = d.excl_tile_idx.p;
+  a.excl_masks = d.excl_masks.p;
+  a.ntile = ntile_;
+  a.cut2f = static_cast<float>(mp_.cut * mp_.cut);
+  a.cut2 = mp_.cut * mp_.cut;
+  a.gbb2f = static_cast<float>(std::min(list_b_cut2(mp_, fsmax), 1e30));
+  a.cand = d.cand.p;
+  a.cand_cap = static_cast<int>(d.cand.n);
+  a.ncand = d.counters.p + 0;
+  a.overflow = d.counters.p + 1;
+  a.cand_start = d.cand_start.p;
+  a.cand_count = d.cand_count.p;
+  a.colA = d.colA.p;
+  a.colB = d.colB.p;
+  a.colE = d.colE.p;
+  a.cand_n = d.cand_n.p;
+  a.cand_off = d.cand_off.p;
+  a.chunksA = d.chunksA.p;
+  a.chunksB = d.chunksB.p;
+  a.chunk0A = d.chunk0A.p;
+  a.chunk0B = d.chunk0B.p;
+  a.nchunkA = d.counters.p + 2;
+  a.nchunkB = d.counters.p + 3;
+  a.chunkA_i = d.chunkA_i.p;
+  a.entA_slot = d.entA_slot.p;
+  a.entA_col = d.entA_col.p;
+  a.entA_exc = d.entA_exc.p;
+  a.chunkB_i = d.chunkB_i.p;
+  a.entB_slot = d.entB_slot.p;
+  a.entB_col = d.entB_col.p;
+  a.flagB = d.counters.p + 4;
+  a.xb = d.xb.p;
+  return a;
+}
+
+double Batch::fsmax_all() const {
+  double f = 0.0;
+  for (auto &sy : sys_) f = std::max(f, sy.fsmax);
+  return f;
+}
+
+// Both pair lists from the current coordinates (lists.cuh, stages 1-6).
+// The host reads two counts back (candidates, chunks) to size the stores.
 int Batch::build_lists(void *stream) {
   DeviceState &d = *d_;
   cudaStream_t st = pick(d, stream);
-  for (int attempt = 0; attempt < 4; attempt++) {
-    SFFG_CK(cudaMemsetAsync(d.counters.p, 0, 3 * sizeof(int), st));
-    ListArgs a;
-    a.pos_hi = d.pos_hi.p;
-    a.pos_lo = d.pos_lo.p;
-    a.box_lo = d.box_lo.p;
-    a.box_hi = d.box_hi.p;
-    a.x = d.x.p;
-    a.slot_atom = d.slot_atom.p;
-    a.param = d.param.p;
-    a.tile_valid = d.tile_valid.p;
-    a.tile_sys = d.tile_sys.p;
-    a.sys_tile_end = d.sys_tile_end.p;
-    a.sys_has_frozen = d.sys_has_frozen.p;
-    a.sys_active = d.sys_active.p;
-    a.excl_tile_start = d.excl_tile_start.p;
-    a.excl_tile_j = d.excl_tile_j.p;
-    a.excl_tile_idx = d.excl_tile_idx.p;
-    a.ntile = ntile_;
-    a.cut2f = static_cast<float>(mp_.cut * mp_.cut);
-    a.cut2 = mp_.cut * mp_.cut;
-    a.items = d.items.p;
-    a.nitems = d.counters.p + 0;
-    a.capacity = static_cast<int>(d.items.n);
-    a.masks = d.masks.p;
-    a.nmasks = d.counters.p + 1;
-    a.mask_capacity = static_cast<int>(d.masks.n / 32);
-    a.overflow = d.counters.p + 2;
-    const int threads = 128;
-    const long long warps = ntile_;
-    const int blocks = static_cast<int>((warps * 32 + threads - 1) / threads);
-    k_build_list<<<blocks, threads, 0, st>>>(a);
+  const double fsmax = fsmax_all();
+  const int tile_blocks = (ntile_ * 32 + 255) / 256;
+  if (d.cand.n == 0) SFFG_CK(d.cand.alloc(static_cast<size_t>(std::min<long long>(cand_max_, 64LL * ntile_ + 1024))));
+  int c[2] = {0, 0};
+  for (int attempt = 0;; attempt++) {
+    SFFG_CK(cudaMemsetAsync(d.counters.p, 0, 2 * sizeof(int), st));
+    k_list_candidates<<<tile_blocks, 256, 0, st>>>(list_args(fsmax));
     SFFG_CK(cudaGetLastError());
     launches_++;
-    int c[3];
     SFFG_CK(cudaMemcpyAsync(c, d.counters.p, sizeof(c), cudaMemcpyDeviceToHost, st));
     SFFG_CK(cudaStreamSynchronize(st));
-    if (!c[2]) {
-      have_list_ = true;
-      return SFFG_OK;
+    if (!c[1]) break;
+    if (attempt >= 3) {
+      last_error = "pair list build did not fit";
+      return SFFG_ENOMEM;
     }
-    // overflow: grow the mask store (items are sized for the worst case)
-    size_t want = std::max<size_t>(static_cast<size_t>(c[1]) + 1024, d.masks.n / 32 * 2);
-    want = std::min<size_t>(want, d.items.n);
-    SFFG_CK(d.masks.alloc(want * 32));
+    SFFG_CK(d.cand.alloc(static_cast<size_t>(std::min<long long>(cand_max_, c[0] + c[0] / 4 + 1024))));
   }
-  last_error = "pair list build did not fit";
-  return SFFG_ENOMEM;
+  ncand_ = c[0];
+  const size_t nc = std::max(1, ncand_);
+  SFFG_CK(ensure(d.colA, nc * 32));
+  SFFG_CK(ensure(d.colB, nc * 32));
+  SFFG_CK(ensure(d.colE, nc * 32));
+  SFFG_CK(ensure(d.cand_n, nc));
+  SFFG_CK(ensure(d.cand_off, nc));
+  const int cand_blocks = static_cast<int>(std::min<long long>((static_cast<long long>(nc) * 32 + 255) / 256, 16LL * d.nsm));
+  {
+    const ListArgs a = list_args(fsmax);
+    k_list_columns<false><<<cand_blocks, 256, 0, st>>>(a);
+    k_list_offsets<false><<<tile_blocks, 256, 0, st>>>(a);
+    k_list_scan<false><<<1, 1024, 0, st>>>(a);
+    SFFG_CK(cudaGetLastError());
+    launches_ += 3;
+  }
+  int nch = 0;
+  SFFG_CK(cudaMemcpyAsync(&nch, d.counters.p + 2, sizeof(int), cudaMemcpyDeviceToHost, st));
+  SFFG_CK(cudaStreamSynchronize(st));
+  // list B is a subset of list A: the same capacity serves both, also when
+  // list B is remade later
+  const size_t ne = static_cast<size_t>(std::max(1, nch)) * 32;
+  SFFG_CK(ensure(d.entA_slot, ne));
+  SFFG_CK(ensure(d.entA_col, ne));
+  SFFG_CK(ensure(d.entA_exc, ne));
+  SFFG_CK(ensure(d.entB_slot, ne));
+  SFFG_CK(ensure(d.entB_col, ne));
+  SFFG_CK(ensure(d.chunkA_i, ne / 32));
+  SFFG_CK(ensure(d.chunkB_i, ne / 32));
+  {
+    const ListArgs a = list_args(fsmax);
+    k_list_fill<false><<<cand_blocks, 256, 0, st>>>(a);
+    k_list_pad<false><<<tile_blocks, 256, 0, st>>>(a);
+    k_list_done<<<1, 1, 0, st>>>(a.flagB);
+    SFFG_CK(cudaGetLastError());
+    launches_ += 3;
+  }
+  have_list_ = true;
+  return SFFG_OK;
+}
+
+// Remakes list B from list A when k_pack found an atom that moved too far
+// since list B was made; every launch returns at once otherwise.
+void Batch::rebuild_list_b(void *stream) {
+  DeviceState &d = *d_;
+  cudaStream_t st = pick(d, stream);
+  const size_t nc = std::max(1, ncand_);
+  const int tile_blocks = (ntile_ * 32 + 255) / 256;
+  const int cand_blocks = static_cast<int>(std::min<long long>((static_cast<long long>(nc) * 32 + 255) / 256, 16LL * d.nsm));
+  const ListArgs a = list_args(fsmax_all());
+  k_list_columns<true><<<cand_blocks, 256, 0, st>>>(a);
+  k_list_offsets<true><<<tile_blocks, 256, 0, st>>>(a);
+  k_list_scan<true><<<1, 1024, 0, st>>>(a);
+  k_list_fill<true><<<cand_blocks, 256, 0, st>>>(a);
+  k_list_pad<true><<<tile_blocks, 256, 0, st>>>(a);
+  k_list_done<<<1, 1, 0, st>>>(a.flagB);
+  launches_ += 6;
 }
 
 int Batch::eval(bool rebuild, void *stream) {
@@ -704,18 +813,21 @@ int Batch::run_eval(bool rebuild, void *stream) {
   DeviceState &d = *d_;
   cudaStream_t st = pick(d, stream);
   const int nsys = num_systems();
-  SFFG_CK(cudaMemsetAsync(d.counters.p + 3, 0, 3 * sizeof(int), st));
+  SFFG_CK(cudaMemsetAsync(d.counters.p + 5, 0, 3 * sizeof(int), st));
   SFFG_CK(cudaMemsetAsync(d.energy.p, 0, d.energy.bytes(), st));
   k_pack<<<(nslot_ + 255) / 256, 256, 0, st>>>(d.x.p, d.slot_atom.p, d.q32.p, d.tile_valid.p, nslot_, d.pos_hi.p,
                                                d.pos_lo.p, d.box_lo.p, d.box_hi.p, d.acc_sumi.p, d.acc_fx.p,
-                                               d.acc_fy.p, d.acc_fz.p, d.nonfinite.p, d.tile_sys.p);
+                                               d.acc_fy.p, d.acc_fz.p, d.nonfinite.p, d.tile_sys.p, d.xb.p,
+                                               0.2025f * kListSkin * kListSkin, d.counters.p + 4);
   SFFG_CK(cudaGetLastError());
   if (rebuild) {
     const int rc = build_lists(st);
     if (rc) return rc;
+  } else {
+    rebuild_list_b(st);
+    SFFG_CK(cudaGetLastError());
   }
-  double fsmax = 0.0;
-  for (auto &s : sys_) fsmax = std::max(fsmax, s.fsmax);
+  const double fsmax = fsmax_all();
   // bonded and 1-4 terms (FP64)
   BondedArgs ba;
   ba.x = d.x.p;
@@ -740,7 +852,7 @@ int Batch::run_eval(bool rebuild, void *stream) {
     SFFG_CK(cudaEventRecord(d.events[ring][0][0], st));
   }
   {
-    DevTables t = make_tables(d, mp_, fsmax, 3);
+    DevTables t = make_tables(d, mp_, fsmax, 5);
     launch_born(neck, d.grid_pair, st, t);
     SFFG_CK(cudaGetLastError());
   }
@@ -776,7 +888,7 @@ int Batch::run_eval(bool rebuild, void *stream) {
   // pass 2
   if (profile_) SFFG_CK(cudaEventRecord(d.events[ring][1][0], st));
   {
-    DevTables t = make_tables(d, mp_, fsmax, 4);
+    DevTables t = make_tables(d, mp_, fsmax, 6);
     launch_gbpair(mp_.kappa != 0.0, d.grid_pair, st, t);
     SFFG_CK(cudaGetLastError());
   }
@@ -786,7 +898,7 @@ int Batch::run_eval(bool rebuild, void *stream) {
   // pass 3
   if (profile_) SFFG_CK(cudaEventRecord(d.events[ring][2][0], st));
   {
-    DevTables t = make_tables(d, mp_, fsmax, 5);
+    DevTables t = make_tables(d, mp_, fsmax, 7);
     launch_chain(neck, d.grid_pair, st, t);
     SFFG_CK(cudaGetLastError());
   }
@@ -807,28 +919,24 @@ int Batch::run_eval(bool rebuild, void *stream) {
 }
 
 long long Batch::num_pairs(int s) {
-  // Count listed pairs of system s from the device list (diagnostic path).
+  // Count the pairs of system s on list A (the reference's list; a
+  // diagnostic path, synchronous).
   if (!finalized_ || !have_list_) return -1;
   DeviceState &d = *d_;
-  int c[2];
-  if (cudaMemcpy(c, d.counters.p, sizeof(c), cudaMemcpyDeviceToHost) != cudaSuccess) return -1;
-  std::vector<Item> items(c[0]);
-  std::vector<unsigned> masks(static_cast<size_t>(c[1]) * 32);
-  std::vector<unsigned> valid(ntile_);
+  int nch = 0;
+  if (cudaMemcpy(&nch, d.counters.p + 2, sizeof(int), cudaMemcpyDeviceToHost) != cudaSuccess) return -1;
+  std::vector<int> owner(nch);
+  std::vector<unsigned> col(static_cast<size_t>(nch) * 32);
   std::vector<int> tsys(ntile_);
-  cudaMemcpy(items.data(), d.items.p, items.size() * sizeof(Item), cudaMemcpyDeviceToHost);
-  if (!masks.empty()) cudaMemcpy(masks.data(), d.masks.p, masks.size() * sizeof(unsigned), cudaMemcpyDeviceToHost);
-  cudaMemcpy(valid.data(), d.tile_valid.p, valid.size() * sizeof(unsigned), cudaMemcpyDeviceToHost);
+  if (nch > 0) {
+    cudaMemcpy(owner.data(), d.chunkA_i.p, owner.size() * sizeof(int), cudaMemcpyDeviceToHost);
+    cudaMemcpy(col.data(), d.entA_col.p, col.size() * sizeof(unsigned), cudaMemcpyDeviceToHost);
+  }
   cudaMemcpy(tsys.data(), d.tile_sys.p, tsys.size() * sizeof(int), cudaMemcpyDeviceToHost);
   long long n = 0;
-  for (auto &it : items) {
-    if (tsys[it.x] != s) continue;
-    for (int l = 0; l < 32; l++) {
-      unsigned row = it.z < 0 ? valid[it.y] : masks[static_cast<size_t>(it.z) * 32 + l];
-      if (!((valid[it.x] >> l) & 1u)) row = 0;
-      if (it.x == it.y) row &= l < 31 ? (0xffffffffu << (l + 1)) : 0u;
-      n += __builtin_popcount(row);
-    }
+  for (int k = 0; k < nch; k++) {
+    if (tsys[owner[k]] != s) continue;
+    for (int l = 0; l < 32; l++) n += __builtin_popcount(col[static_cast<size_t>(k) * 32 + l]);
   }
   return n;
 }

@@ -21,6 +21,7 @@
 namespace sffg {
 
 struct DeviceState;  // defined in engine.cu
+struct ListArgs;     // defined in lists.cuh
 
 struct SystemInfo {
   int natom = 0, atom_off = 0, slot_off = 0, tile_off = 0, ntile = 0;
@@ -107,6 +108,9 @@ class Batch {
  private:
   int upload();
   int build_lists(void *stream);
+  void rebuild_list_b(void *stream);
+  ListArgs list_args(double fsmax);
+  double fsmax_all() const;
   int run_eval(bool rebuild, void *stream);
   void collect_pass_times(DeviceState &d, long long max_evals);
   Options opts_;
@@ -115,6 +119,8 @@ class Batch {
   std::vector<HostSystem> host_;
   std::vector<std::vector<double>> x0_;
   int natom_total_ = 0, nslot_ = 0, ntile_ = 0;
+  long long cand_max_ = 0;  // candidate tile pairs the batch could ever need
+  int ncand_ = 0;           // candidates of the current pair list
   bool finalized_ = false, have_list_ = false, profile_ = false;
   long long launches_ = 0;
   std::unique_ptr<DeviceState> d_;

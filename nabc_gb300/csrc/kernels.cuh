@@ -1,15 +1,16 @@
 // Device kernels of the generalized-Born path (sm_103a).
 //
 // The three pair passes of the reference's egb() (src/sff/eff.c:1566-1733,
-// 1770-2066, 2131-2405) run over a list of 32x32 atom-tile pairs.  A warp
-// owns one tile pair at a time: lane l holds i-atom l of the i-tile in
+// 1770-2066, 2131-2405) run over compacted pair-list chunks (lists.cuh): a
+// chunk is an i-tile of 32 atoms and 32 packed j-atoms with a column mask
+// each.  A warp owns one chunk at a time: lane l holds i-atom l in
 // registers; the 32 j-atoms are staged in shared memory and read by
 // broadcast, so at step s every lane pairs its i-atom with j-atom s.  Both
 // directions of each unordered pair are handled in one visit (Newton's
 // third law); the j-side partial sums, spread over the 32 lanes, are folded
-// with a shuffle transpose-reduction every 8 steps.  Per tile pair the FP32
+// with a shuffle transpose-reduction every few steps.  Per chunk the FP32
 // partial sums are converted to 64-bit fixed point, so the totals do not
-// depend on how tile pairs are scheduled.
+// depend on how chunks are scheduled.
 #pragma once
 
 #include <cstdint>
@@ -19,11 +20,16 @@
 namespace sffg {
 
 constexpr unsigned kFull = 0xffffffffu;
-constexpr int kChunk = 4;  // tile pairs a warp claims per work-queue grab
+constexpr int kChunk = 4;  // list chunks a warp claims per work-queue grab
 
-// Work item: i-tile, j-tile (j >= i), index of the in-list bit mask (-1:
-// every valid pair is on the list) and of the exclusion bit mask (-1: none).
-using Item = int4;
+// One compacted pair list (built by lists.cuh).
+struct ChunkList {
+  const int *chunk_i;   // i-tile of each chunk
+  const int *slot;      // 32 j slots per chunk
+  const unsigned *col;  // per entry, bit i: the pair with lane i of the i-tile is listed
+  const unsigned *exc;  // per entry, bit i: the pair is excluded from Coulomb/LJ (cutoff list)
+  const int *nchunk;
+};
 
 struct DevTables {
   // per slot
@@ -35,19 +41,15 @@ struct DevTables {
   const float *rinv2;     // sqrt(log2(e)/4) / reff (pass 2)
   const float *sumda32;   // chain-rule weight (pass 3)
   // per tile
-  const unsigned *tile_valid;
   const int *tile_sys;
-  const float4 *box_lo, *box_hi;
   // per system
   const int *sys_active;
   const int *sys_lj_off;
   const int *sys_ntypes;
   const float2 *lj;       // (A, B) per type pair, per system blocks
-  // lists
-  const Item *items;
-  const int *nitems;
-  const unsigned *masks;
-  const unsigned *excl_masks;
+  // lists: la (r < cut) for pass 2, lb (r < rgbmax + Fsmax + skin) for
+  // passes 1 and 3
+  ChunkList la, lb;
   int *counter;
   // accumulators
   long long *acc_sumi, *acc_sd, *acc_fx, *acc_fy, *acc_fz;
@@ -120,24 +122,6 @@ __device__ __forceinline__ int claim_chunk(int *counter, int lane) {
   return __shfl_sync(kFull, base, 0);
 }
 
-// Rows of the in-list mask for this lane's i-atom against the j-tile.
-__device__ __forceinline__ unsigned row_mask(const DevTables &t, const Item &it, int lane) {
-  const unsigned vI = t.tile_valid[it.x];
-  unsigned row = it.z < 0 ? t.tile_valid[it.y] : t.masks[static_cast<size_t>(it.z) * 32 + lane];
-  if (!((vI >> lane) & 1u)) row = 0u;
-  if (it.x == it.y) row &= lane < 31 ? (kFull << (lane + 1)) : 0u;
-  return row;
-}
-
-// Squared distance between two tiles' bounding boxes.
-__device__ __forceinline__ float box_dist2(const DevTables &t, int I, int J) {
-  const float4 al = t.box_lo[I], ah = t.box_hi[I], bl = t.box_lo[J], bh = t.box_hi[J];
-  float dx = fmaxf(0.0f, fmaxf(al.x - bh.x, bl.x - ah.x));
-  float dy = fmaxf(0.0f, fmaxf(al.y - bh.y, bl.y - ah.y));
-  float dz = fmaxf(0.0f, fmaxf(al.z - bh.z, bl.z - ah.z));
-  return dx * dx + dy * dy + dz * dz;
-}
-
 // Both directions of the descreening of one pair (value, or for DERIV the
 // derivative / dij): vi is atom i descreened by sphere j, vj the converse.
 // Only warp-uniform branches: the far-field Taylor form is evaluated for
@@ -166,13 +150,23 @@ __device__ __forceinline__ void descreen_pair(const BornConst &c, bool in, float
   vj = dij > c.rgbmax + s_i ? 0.0f : vj;
 }
 
+// Stages the j-entries of chunk k in shared memory: lane l loads entry l.
+// Returns this lane's j slot (padding entries point at a real slot of the
+// i-tile and have an empty column).
+__device__ __forceinline__ int chunk_entry(const ChunkList &L, int k, int lane, unsigned &col) {
+  const size_t e = static_cast<size_t>(k) * 32 + lane;
+  col = L.col[e];
+  return L.slot[e];
+}
+
 // ------------------------------------------------------------------ pass 1
 // Born-radius descreening sums (src/sff/eff.c:1566-1709): both directions
-// of every listed pair within rgbmax + Fsmax.
+// of every pair of list B within rgbmax + Fsmax.
 template <bool NECK>
 __global__ void __launch_bounds__(256, 2) k_born(const DevTables t) {
   __shared__ float4 sm_hi[8][32], sm_lo[8][32], sm_gb[8][32];
-  __shared__ int sm_par[8][32];
+  __shared__ unsigned sm_col[8][32];
+  __shared__ int sm_par[8][NECK ? 32 : 1];
   __shared__ float s_npos[NECK ? 441 : 1], s_nval[NECK ? 441 : 1];
   if (NECK) {
     for (int i = threadIdx.x; i < 441; i += blockDim.x) {
@@ -182,21 +176,18 @@ __global__ void __launch_bounds__(256, 2) k_born(const DevTables t) {
     __syncthreads();
   }
   const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
-  const int nitems = *t.nitems;
-  const float cut2 = t.born.cutoff2 * 1.0001f + 1e-3f;
+  const int nchunk = *t.lb.nchunk;
   int cur_I = -1;
   float xi = 0, yi = 0, zi = 0, xli = 0, yli = 0, zli = 0, rhoi = 1, si = 0, rbi = 0, sci = 0;
   int nki = 0;
   long long sumi64 = 0;
   for (;;) {
     const int base = claim_chunk(t.counter, lane);
-    if (base >= nitems) break;
-    const int end = min(base + kChunk, nitems);
+    if (base >= nchunk) break;
+    const int end = min(base + kChunk, nchunk);
     for (int k = base; k < end; k++) {
-      const Item it = t.items[k];
-      const int I = it.x, J = it.y;
+      const int I = t.lb.chunk_i[k];
       if (!t.sys_active[t.tile_sys[I]]) continue;
-      if (box_dist2(t, I, J) > cut2) continue;
       if (I != cur_I) {
         if (cur_I >= 0) atomic_add_ll(&t.acc_sumi[cur_I * 32 + lane], sumi64);
         cur_I = I;
@@ -207,13 +198,14 @@ __global__ void __launch_bounds__(256, 2) k_born(const DevTables t) {
         rhoi = g.x; si = g.y; rbi = g.z; sci = g.w;
         nki = (t.param[sl] >> 16) & 0xff;
       }
-      const int sj = J * 32 + lane;
+      unsigned mycol;
+      const int sj = chunk_entry(t.lb, k, lane, mycol);
       sm_hi[w][lane] = t.pos_hi[sj];
       sm_lo[w][lane] = t.pos_lo[sj];
       sm_gb[w][lane] = t.gbpar[sj];
+      sm_col[w][lane] = mycol;
       if (NECK) sm_par[w][lane] = t.param[sj];
-      const unsigned row = row_mask(t, it, lane);
-      const unsigned cols = __reduce_or_sync(kFull, row);
+      const unsigned cols = __ballot_sync(kFull, mycol != 0u);
       __syncwarp();
       float acc_i = 0.0f, acc_j = 0.0f;
 #pragma unroll 1
@@ -223,13 +215,13 @@ __global__ void __launch_bounds__(256, 2) k_born(const DevTables t) {
         for (int s = 0; s < kGroup; s++) {
           const int j = g * kGroup + s;
           aj[s] = 0.0f;
-          if (!((cols >> j) & 1u)) continue;  // j listed for no lane
+          if (!((cols >> j) & 1u)) continue;  // padding entry
           const float4 h = sm_hi[w][j], l = sm_lo[w][j], gp = sm_gb[w][j];
           const float dx = (xi - h.x) + (xli - l.x);
           const float dy = (yi - h.y) + (yli - l.y);
           const float dz = (zi - h.z) + (zli - l.z);
           const float r2 = fmaf(dx, dx, fmaf(dy, dy, dz * dz));
-          const bool in = ((row >> j) & 1u) && r2 <= t.born.cutoff2;
+          const bool in = ((sm_col[w][j] >> lane) & 1u) && r2 <= t.born.cutoff2;
           if (!__any_sync(kFull, in)) continue;  // every lane out of range
           const float dij1i = rsqrt_nr(r2);
           const float dij = r2 * dij1i;
@@ -253,7 +245,7 @@ __global__ void __launch_bounds__(256, 2) k_born(const DevTables t) {
         acc_j += reduce_to_lane(aj, g, lane);
       }
       sumi64 += to_fixed(acc_i, 1099511627776.0f);
-      if ((t.tile_valid[J] >> lane) & 1u) atomic_add_ll(&t.acc_sumi[sj], to_fixed(acc_j, 1099511627776.0f));
+      if (mycol) atomic_add_ll(&t.acc_sumi[sj], to_fixed(acc_j, 1099511627776.0f));
       __syncwarp();
     }
   }
@@ -262,13 +254,14 @@ __global__ void __launch_bounds__(256, 2) k_born(const DevTables t) {
 
 // ------------------------------------------------------------------ pass 2
 // GB + Coulomb + Lennard-Jones pair energies, dE/dr and sumdeijda
-// (src/sff/eff.c:1902-2063).
+// (src/sff/eff.c:1902-2063) over list A.
 template <bool KAPPA>
 __global__ void __launch_bounds__(256, 2) k_gbpair(const DevTables t) {
   __shared__ float4 sm_hi[8][32], sm_lo[8][32];
   __shared__ float2 sm_aux[8][32];
+  __shared__ unsigned sm_col[8][32], sm_exc[8][32];
   const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
-  const int nitems = *t.nitems;
+  const int nchunk = *t.la.nchunk;
   int cur_I = -1, cur_sys = -1;
   float xi = 0, yi = 0, zi = 0, xli = 0, yli = 0, zli = 0, qi = 0, ri = 1, rvi = 0;
   int ti = 0, nt = 1;
@@ -293,11 +286,10 @@ __global__ void __launch_bounds__(256, 2) k_gbpair(const DevTables t) {
   };
   for (;;) {
     const int base = claim_chunk(t.counter, lane);
-    if (base >= nitems) break;
-    const int end = min(base + kChunk, nitems);
+    if (base >= nchunk) break;
+    const int end = min(base + kChunk, nchunk);
     for (int k = base; k < end; k++) {
-      const Item it = t.items[k];
-      const int I = it.x, J = it.y;
+      const int I = t.la.chunk_i[k];
       const int sys = t.tile_sys[I];
       if (!t.sys_active[sys]) continue;
       if (sys != cur_sys) {
@@ -317,17 +309,18 @@ __global__ void __launch_bounds__(256, 2) k_gbpair(const DevTables t) {
         rvi = t.rinv2[sl];
         ti = (t.param[sl] & 0xffff) * nt;
       }
-      const int sj = J * 32 + lane;
+      unsigned mycol;
+      const int sj = chunk_entry(t.la, k, lane, mycol);
       {
         float4 l = t.pos_lo[sj];
         l.w = t.reff32[sj];
         sm_hi[w][lane] = t.pos_hi[sj];
         sm_lo[w][lane] = l;
         sm_aux[w][lane] = make_float2(t.rinv2[sj], __int_as_float(t.param[sj] & 0xffff));
+        sm_col[w][lane] = mycol;
+        sm_exc[w][lane] = t.la.exc[static_cast<size_t>(k) * 32 + lane];
       }
-      const unsigned row = row_mask(t, it, lane);
-      const unsigned cols = __reduce_or_sync(kFull, row);
-      const unsigned exr = it.w < 0 ? 0u : t.excl_masks[static_cast<size_t>(it.w) * 32 + lane];
+      const unsigned cols = __ballot_sync(kFull, mycol != 0u);
       __syncwarp();
       float fix = 0, fiy = 0, fiz = 0, sdi = 0, ep = 0, ee = 0, ev = 0;
       float jx = 0, jy = 0, jz = 0, jsd = 0;
@@ -338,15 +331,15 @@ __global__ void __launch_bounds__(256, 2) k_gbpair(const DevTables t) {
         for (int s = 0; s < kGroup; s++) {
           const int j = g * kGroup + s;
           ax[s] = ay[s] = az[s] = as[s] = 0.0f;
-          if (!((cols >> j) & 1u)) continue;  // j listed for no lane
+          if (!((cols >> j) & 1u)) continue;  // padding entry
           const float4 h = sm_hi[w][j], l = sm_lo[w][j];
           const float2 au = sm_aux[w][j];
           const float dx = (xi - h.x) + (xli - l.x);
           const float dy = (yi - h.y) + (yli - l.y);
           const float dz = (zi - h.z) + (zli - l.z);
           const float r2 = fmaf(dx, dx, fmaf(dy, dy, dz * dz));
-          const bool in = (row >> j) & 1u;
-          const bool coul = !((exr >> j) & 1u);
+          const bool in = (sm_col[w][j] >> lane) & 1u;
+          const bool coul = !((sm_exc[w][j] >> lane) & 1u);
           const float2 ab = lj[ti + __float_as_int(au.y)];
           const PairOut o = gb_pair<KAPPA>(t.pair, r2, qi * h.w, ri, l.w, rvi, au.x, coul, ab.x, ab.y);
           const float de = in ? o.de : 0.0f;
@@ -374,7 +367,7 @@ __global__ void __launch_bounds__(256, 2) k_gbpair(const DevTables t) {
       ep64 += to_fixed(ep, FS);
       ee64 += to_fixed(ee, FS);
       ev64 += to_fixed(ev, FS);
-      if ((t.tile_valid[J] >> lane) & 1u) {
+      if (mycol) {
         atomic_add_ll(&t.acc_fx[sj], to_fixed(jx, FS));
         atomic_add_ll(&t.acc_fy[sj], to_fixed(jy, FS));
         atomic_add_ll(&t.acc_fz[sj], to_fixed(jz, FS));
@@ -388,12 +381,14 @@ __global__ void __launch_bounds__(256, 2) k_gbpair(const DevTables t) {
 }
 
 // ------------------------------------------------------------------ pass 3
-// Chain rule through the Born radii (src/sff/eff.c:2241-2395): for each
-// listed pair, g = sumda_i d_ij + sumda_j d_ji, f_i -= g r_ij, f_j += g r_ij.
+// Chain rule through the Born radii (src/sff/eff.c:2241-2395) over list B:
+// for each pair within rgbmax + Fsmax, g = sumda_i d_ij + sumda_j d_ji,
+// f_i -= g r_ij, f_j += g r_ij.
 template <bool NECK>
 __global__ void __launch_bounds__(256, 2) k_chain(const DevTables t) {
   __shared__ float4 sm_hi[8][32], sm_lo[8][32], sm_gb[8][32];
-  __shared__ int sm_par[8][32];
+  __shared__ unsigned sm_col[8][32];
+  __shared__ int sm_par[8][NECK ? 32 : 1];
   __shared__ float s_npos[NECK ? 441 : 1], s_nval[NECK ? 441 : 1];
   if (NECK) {
     for (int i = threadIdx.x; i < 441; i += blockDim.x) {
@@ -403,8 +398,7 @@ __global__ void __launch_bounds__(256, 2) k_chain(const DevTables t) {
     __syncthreads();
   }
   const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
-  const int nitems = *t.nitems;
-  const float cut2 = t.born.cutoff2 * 1.0001f + 1e-3f;
+  const int nchunk = *t.lb.nchunk;
   const float FS = 4294967296.0f;
   int cur_I = -1;
   float xi = 0, yi = 0, zi = 0, xli = 0, yli = 0, zli = 0, rhoi = 1, si = 0, rbi = 0, sci = 0, sdai = 0;
@@ -418,13 +412,11 @@ __global__ void __launch_bounds__(256, 2) k_chain(const DevTables t) {
   };
   for (;;) {
     const int base = claim_chunk(t.counter, lane);
-    if (base >= nitems) break;
-    const int end = min(base + kChunk, nitems);
+    if (base >= nchunk) break;
+    const int end = min(base + kChunk, nchunk);
     for (int k = base; k < end; k++) {
-      const Item it = t.items[k];
-      const int I = it.x, J = it.y;
+      const int I = t.lb.chunk_i[k];
       if (!t.sys_active[t.tile_sys[I]]) continue;
-      if (box_dist2(t, I, J) > cut2) continue;
       if (I != cur_I) {
         if (cur_I >= 0) flush_i();
         cur_I = I;
@@ -436,17 +428,18 @@ __global__ void __launch_bounds__(256, 2) k_chain(const DevTables t) {
         sdai = t.sumda32[sl];
         nki = (t.param[sl] >> 16) & 0xff;
       }
-      const int sj = J * 32 + lane;
+      unsigned mycol;
+      const int sj = chunk_entry(t.lb, k, lane, mycol);
       {
         float4 l = t.pos_lo[sj];
         l.w = t.sumda32[sj];
         sm_hi[w][lane] = t.pos_hi[sj];
         sm_lo[w][lane] = l;
         sm_gb[w][lane] = t.gbpar[sj];
+        sm_col[w][lane] = mycol;
         if (NECK) sm_par[w][lane] = t.param[sj];
       }
-      const unsigned row = row_mask(t, it, lane);
-      const unsigned cols = __reduce_or_sync(kFull, row);
+      const unsigned cols = __ballot_sync(kFull, mycol != 0u);
       __syncwarp();
       float fix = 0, fiy = 0, fiz = 0, jx = 0, jy = 0, jz = 0;
 #pragma unroll 1
@@ -462,7 +455,7 @@ __global__ void __launch_bounds__(256, 2) k_chain(const DevTables t) {
           const float dy = (yi - h.y) + (yli - l.y);
           const float dz = (zi - h.z) + (zli - l.z);
           const float r2 = fmaf(dx, dx, fmaf(dy, dy, dz * dz));
-          const bool in = ((row >> j) & 1u) && r2 <= t.born.cutoff2;
+          const bool in = ((sm_col[w][j] >> lane) & 1u) && r2 <= t.born.cutoff2;
           if (!__any_sync(kFull, in)) continue;
           const float dij1i = rsqrt_nr(r2);
           const float dij = r2 * dij1i;
@@ -495,7 +488,7 @@ __global__ void __launch_bounds__(256, 2) k_chain(const DevTables t) {
       fx64 += to_fixed(fix, FS);
       fy64 += to_fixed(fiy, FS);
       fz64 += to_fixed(fiz, FS);
-      if ((t.tile_valid[J] >> lane) & 1u) {
+      if (mycol) {
         atomic_add_ll(&t.acc_fx[sj], to_fixed(jx, FS));
         atomic_add_ll(&t.acc_fy[sj], to_fixed(jy, FS));
         atomic_add_ll(&t.acc_fz[sj], to_fixed(jz, FS));

@@ -18,7 +18,8 @@ __global__ void k_pack(const double *__restrict__ x, const int *__restrict__ slo
                        const float *__restrict__ q32, const unsigned *__restrict__ tile_valid,
                        int nslot, float4 *pos_hi, float4 *pos_lo, float4 *box_lo, float4 *box_hi,
                        long long *acc_sumi, long long *acc_fx, long long *acc_fy, long long *acc_fz,
-                       int *nonfinite_sys, const int *tile_sys) {
+                       int *nonfinite_sys, const int *tile_sys, const float4 *xb, float xb_lim2,
+                       int *flagB) {
   const int slot = blockIdx.x * blockDim.x + threadIdx.x;
   const int lane = threadIdx.x & 31;
   if (slot - lane >= nslot) return;  // whole warp beyond the last tile
@@ -33,6 +34,11 @@ __global__ void k_pack(const double *__restrict__ x, const int *__restrict__ slo
     const float hx = static_cast<float>(X), hy = static_cast<float>(Y), hz = static_cast<float>(Z);
     hi = make_float4(hx, hy, hz, q32[slot]);
     lo = make_float4(static_cast<float>(X - hx), static_cast<float>(Y - hy), static_cast<float>(Z - hz), 0.f);
+    // list B stays valid while no atom has moved more than sqrt(xb_lim2)
+    // since it was made (a NaN also asks for a rebuild)
+    const float4 q = xb[slot];
+    const float mx = hx - q.x, my = hy - q.y, mz = hz - q.z;
+    if (!(mx * mx + my * my + mz * mz <= xb_lim2)) *flagB = 1;
     if (!bad) {
       bx0 = bx1 = hx;
       by0 = by1 = hy;
@@ -65,126 +71,6 @@ __global__ void k_pack(const double *__restrict__ x, const int *__restrict__ slo
     if (anybad) nonfinite_sys[tile_sys[tile]] = 1;
   }
   (void)tile_valid;
-}
-
-// ------------------------------------------------------------ pair lists
-struct ListArgs {
-  const float4 *pos_hi, *pos_lo, *box_lo, *box_hi;
-  const double *x;
-  const int *slot_atom, *param;
-  const unsigned *tile_valid;
-  const int *tile_sys, *sys_tile_end, *sys_has_frozen, *sys_active;
-  const int *excl_tile_start;  // per tile: range into excl_tile_j / excl_tile_idx
-  const int *excl_tile_j, *excl_tile_idx;
-  int ntile;
-  float cut2f;
-  double cut2;
-  Item *items;
-  int *nitems;
-  int capacity;
-  unsigned *masks;
-  int *nmasks;
-  int mask_capacity;
-  int *overflow;
-};
-
-__device__ __forceinline__ bool box_candidate(const ListArgs &a, float4 il, float4 ih, int J) {
-  const float4 bl = a.box_lo[J], bh = a.box_hi[J];
-  float dx = fmaxf(0.0f, fmaxf(il.x - bh.x, bl.x - ih.x));
-  float dy = fmaxf(0.0f, fmaxf(il.y - bh.y, bl.y - ih.y));
-  float dz = fmaxf(0.0f, fmaxf(il.z - bh.z, bl.z - ih.z));
-  return dx * dx + dy * dy + dz * dz < a.cut2f * 1.0001f + 1e-3f;
-}
-
-// One warp per i-tile: writes every (I, J >= I) tile pair that can hold a
-// listed pair -- r^2 < cut^2 at build time, two frozen atoms never
-// (src/sff/nblist.c:726-746) -- with a per-row bit mask unless the whole
-// tile pair is certainly inside the cutoff.
-__global__ void k_build_list(const ListArgs a) {
-  const int lane = threadIdx.x & 31;
-  const int I = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
-  if (I >= a.ntile) return;
-  const int sys = a.tile_sys[I];
-  if (!a.sys_active[sys]) return;
-  const int jend = a.sys_tile_end[sys];
-  const float4 il = a.box_lo[I], ih = a.box_hi[I];
-  int cnt = 0;
-  for (int J0 = I; J0 < jend; J0 += 32) {
-    const int J = J0 + lane;
-    const bool c = J < jend && box_candidate(a, il, ih, J);
-    cnt += __popc(__ballot_sync(kFull, c));
-  }
-  int base = 0;
-  if (lane == 0) base = atomicAdd(a.nitems, cnt);
-  base = __shfl_sync(kFull, base, 0);
-  if (base + cnt > a.capacity) {
-    if (lane == 0) atomicExch(a.overflow, 1);
-    return;
-  }
-  const int si = I * 32 + lane;
-  const unsigned vI = a.tile_valid[I];
-  const bool myvalid = (vI >> lane) & 1u;
-  const float4 hi_i = a.pos_hi[si], lo_i = a.pos_lo[si];
-  const bool frz_i = (a.param[si] >> 24) & 1;
-  const int ai = a.slot_atom[si];
-  const bool sys_frozen = a.sys_has_frozen[sys];
-  int k = base;
-  for (int J0 = I; J0 < jend; J0 += 32) {
-    const int J = J0 + lane;
-    unsigned bal = __ballot_sync(kFull, J < jend && box_candidate(a, il, ih, J));
-    while (bal) {
-      const int b = __ffs(bal) - 1;
-      bal &= bal - 1;
-      const int Jc = J0 + b;
-      // farthest corner distance of the two boxes
-      const float4 bl = a.box_lo[Jc], bh = a.box_hi[Jc];
-      const float mx = fmaxf(ih.x - bl.x, bh.x - il.x), my = fmaxf(ih.y - bl.y, bh.y - il.y),
-                  mz = fmaxf(ih.z - bl.z, bh.z - il.z);
-      const bool full = !sys_frozen && (mx * mx + my * my + mz * mz) < a.cut2f * 0.9999f - 1e-3f;
-      int ex = -1;
-      for (int e = a.excl_tile_start[I]; e < a.excl_tile_start[I + 1]; e++)
-        if (a.excl_tile_j[e] == Jc) { ex = a.excl_tile_idx[e]; break; }
-      int midx = -1;
-      if (!full) {
-        if (lane == 0) midx = atomicAdd(a.nmasks, 1);
-        midx = __shfl_sync(kFull, midx, 0);
-        if (midx >= a.mask_capacity) {
-          if (lane == 0) atomicExch(a.overflow, 2);
-          midx = -2;
-        } else {
-          const unsigned vJ = a.tile_valid[Jc];
-          unsigned row = 0;
-          for (int jj = 0; jj < 32 && myvalid; jj++) {
-            const int sjj = Jc * 32 + jj;
-            if (!((vJ >> jj) & 1u)) continue;
-            if (Jc == I && jj <= lane) continue;
-            const float4 h = a.pos_hi[sjj], l = a.pos_lo[sjj];
-            const float dx = (hi_i.x - h.x) + (lo_i.x - l.x);
-            const float dy = (hi_i.y - h.y) + (lo_i.y - l.y);
-            const float dz = (hi_i.z - h.z) + (lo_i.z - l.z);
-            const float r2 = dx * dx + dy * dy + dz * dz;
-            bool in;
-            if (r2 < a.cut2f * 0.99999f) {
-              in = true;
-            } else if (r2 > a.cut2f * 1.00001f) {
-              in = false;
-            } else {  // borderline: decide exactly as the reference does, in FP64
-              const int aj = a.slot_atom[sjj];
-              const double ddx = a.x[3 * ai] - a.x[3 * aj], ddy = a.x[3 * ai + 1] - a.x[3 * aj + 1],
-                           ddz = a.x[3 * ai + 2] - a.x[3 * aj + 2];
-              in = ddx * ddx + ddy * ddy + ddz * ddz < a.cut2;
-            }
-            if (in && frz_i && ((a.param[sjj] >> 24) & 1)) in = false;
-            if (in) row |= 1u << jj;
-          }
-          a.masks[static_cast<size_t>(midx) * 32 + lane] = row;
-        }
-      }
-      // (on mask overflow the host rebuilds with more room before any use)
-      if (lane == 0) a.items[k] = make_int4(I, Jc, midx < 0 ? -1 : midx, ex);
-      k++;
-    }
-  }
 }
 
 // ------------------------------------------------------------ Born radii

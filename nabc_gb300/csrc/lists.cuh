@@ -1,0 +1,352 @@
+// Pair lists: the reference's neighbour list (src/sff/nblist.c:813-1240,
+// pairs with r < cut at build time, excluded pairs included, pairs of two
+// frozen atoms left out, nblist.c:726-746) stored as compacted chunks.
+//
+// For every i-tile (32 slots) the j-atoms of tiles J >= I that pair with at
+// least one of its atoms are packed, 32 per chunk, each with a column mask
+// (bit i: the pair with lane i of the i-tile is listed) and, for the cutoff
+// list, an exclusion column mask.  A warp of a pair pass takes one chunk:
+// its lanes hold the i-tile, its steps walk the 32 packed j-atoms.  Packing
+// j-atoms instead of whole 32-atom tiles keeps ~50-60% of the lane-steps
+// busy at protein densities, against ~20-35% for tile pairs.
+//
+// Two lists share one build:
+//   list A, pairs with r < cut: pass 2 (GB + Coulomb + LJ) -- exactly the
+//           reference's list, rebuilt every nsnb evaluations;
+//   list B, the pairs of list A with r < rgbmax + Fsmax + skin: passes 1
+//           and 3 (Born radii and chain rule), which the reference runs
+//           over list A skipping pairs beyond rgbmax + Fsmax at every
+//           evaluation.  List B is rebuilt from list A (on the device, with
+//           no host round trip) as soon as any atom has moved more than
+//           0.45 skin since list B was made, so every pair of list A that
+//           is within rgbmax + Fsmax now is on list B.
+//
+// Build stages (one launch each):
+//   1 candidates   warp per i-tile: tile pairs (I, J >= I) whose bounding
+//                  boxes are within cut
+//   2 columns      warp per candidate: column masks of both lists and the
+//                  exclusion columns; entry counts
+//   3 offsets      warp per i-tile: entry offsets of each candidate within
+//                  the i-tile, chunks per i-tile
+//   4 scan         one block: first chunk of every i-tile, chunk totals
+//   5 fill         warp per candidate: the entries
+//   6 pad          warp per i-tile: padding entries and chunk owners
+// Stages 2-6 also run in "list B only" mode when the displacement check
+// fires; each of those launches returns at once unless the flag is set.
+#pragma once
+
+#include "kernels.cuh"
+
+namespace sffg {
+
+constexpr float kListSkin = 0.6f;  // list B margin beyond rgbmax + Fsmax, in Angstrom
+
+struct ListArgs {
+  const float4 *pos_hi, *pos_lo, *box_lo, *box_hi;
+  const double *x;
+  const int *slot_atom, *param;
+  const unsigned *tile_valid;
+  const int *tile_sys, *sys_tile_end, *sys_active;
+  const int *excl_tile_start;  // per tile: range into excl_tile_j / excl_tile_idx
+  const int *excl_tile_j, *excl_tile_idx;
+  const unsigned *excl_masks;  // per tile pair with exclusions: 32 rows (bit = j lane)
+  int ntile;
+  float cut2f;   // cut^2 (list A), FP32
+  double cut2;   // cut^2, exact FP64 decision for borderline pairs
+  float gbb2f;   // (rgbmax + Fsmax + skin)^2 (list B)
+  // candidates
+  int2 *cand;
+  int cand_cap;
+  int *ncand, *overflow;
+  int *cand_start, *cand_count;  // per i-tile
+  unsigned *colA, *colB, *colE;  // per candidate x 32 lanes
+  int2 *cand_n;                  // entries of (A, B) per candidate
+  int2 *cand_off;                // their offsets within the i-tile
+  int *chunksA, *chunksB;        // per i-tile
+  int *chunk0A, *chunk0B;        // first chunk of each i-tile
+  int *nchunkA, *nchunkB;
+  // the lists
+  int *chunkA_i, *entA_slot;
+  unsigned *entA_col, *entA_exc;
+  int *chunkB_i, *entB_slot;
+  unsigned *entB_col;
+  // list-B rebuild flag (set by the displacement check) and the positions
+  // list B was made from
+  int *flagB;
+  float4 *xb;
+};
+
+// ---- stage 1 -------------------------------------------------------------
+__global__ void k_list_candidates(const ListArgs a) {
+  const int lane = threadIdx.x & 31;
+  const int I = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+  if (I >= a.ntile) return;
+  const int sys = a.tile_sys[I];
+  if (!a.sys_active[sys]) {
+    if (lane == 0) {
+      a.cand_start[I] = 0;
+      a.cand_count[I] = 0;
+    }
+    return;
+  }
+  const int jend = a.sys_tile_end[sys];
+  const float4 il = a.box_lo[I], ih = a.box_hi[I];
+  const float lim = a.cut2f * 1.0001f + 1e-3f;
+  auto near = [&](int J) {
+    if (J >= jend) return false;
+    const float4 bl = a.box_lo[J], bh = a.box_hi[J];
+    const float dx = fmaxf(0.0f, fmaxf(il.x - bh.x, bl.x - ih.x));
+    const float dy = fmaxf(0.0f, fmaxf(il.y - bh.y, bl.y - ih.y));
+    const float dz = fmaxf(0.0f, fmaxf(il.z - bh.z, bl.z - ih.z));
+    return dx * dx + dy * dy + dz * dz < lim;
+  };
+  int cnt = 0;
+  for (int J0 = I; J0 < jend; J0 += 32) cnt += __popc(__ballot_sync(kFull, near(J0 + lane)));
+  int base = 0;
+  if (lane == 0) base = atomicAdd(a.ncand, cnt);
+  base = __shfl_sync(kFull, base, 0);
+  if (base + cnt > a.cand_cap) {  // the host grows the store and runs this stage again
+    if (lane == 0) {
+      atomicExch(a.overflow, 1);
+      a.cand_start[I] = 0;
+      a.cand_count[I] = 0;
+    }
+    return;
+  }
+  int k = base;
+  for (int J0 = I; J0 < jend; J0 += 32) {
+    const bool c = near(J0 + lane);
+    const unsigned bal = __ballot_sync(kFull, c);
+    if (c) a.cand[k + __popc(bal & ((1u << lane) - 1u))] = make_int2(I, J0 + lane);
+    k += __popc(bal);
+  }
+  if (lane == 0) {
+    a.cand_start[I] = base;
+    a.cand_count[I] = cnt;
+  }
+}
+
+// ---- stage 2 -------------------------------------------------------------
+// Lane l takes j-atom l of tile J and walks the 32 atoms of tile I.
+// list A: r^2 < cut^2, decided in FP64 from the double coordinates when
+// the FP32 distance is within 1e-5 of the cutoff, as the reference decides
+// (nblist.c:726-746); upper triangle within a tile; no pair of two frozen
+// atoms.  list B: list A pairs with r^2 < (rgbmax + Fsmax + skin)^2.
+// B_ONLY: list A stays as built; list B is remade from its columns.
+template <bool B_ONLY>
+__global__ void k_list_columns(const ListArgs a) {
+  __shared__ float4 s_hi[8][32], s_lo[8][32];
+  __shared__ int s_atom[8][32];
+  if (B_ONLY && !*a.flagB) return;
+  const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+  const int ncand = *a.ncand, nwarps = (gridDim.x * blockDim.x) >> 5;
+  for (int c = (blockIdx.x * blockDim.x + threadIdx.x) >> 5; c < ncand; c += nwarps) {
+  const int2 p = a.cand[c];
+  const int I = p.x, J = p.y;
+  const int si = I * 32 + lane, sj = J * 32 + lane;
+  s_hi[w][lane] = a.pos_hi[si];
+  s_lo[w][lane] = a.pos_lo[si];
+  s_atom[w][lane] = a.slot_atom[si];
+  const unsigned vI = a.tile_valid[I];
+  const unsigned frzI = __ballot_sync(kFull, (a.param[si] >> 24) & 1);
+  const float4 hj = a.pos_hi[sj], lj = a.pos_lo[sj];
+  const bool vj = (a.tile_valid[J] >> lane) & 1u;
+  const bool frzj = (a.param[sj] >> 24) & 1;
+  const int aj = a.slot_atom[sj];
+  int ex = -1;
+  if (!B_ONLY)
+    for (int e = a.excl_tile_start[I]; e < a.excl_tile_start[I + 1]; e++)
+      if (a.excl_tile_j[e] == J) {
+        ex = a.excl_tile_idx[e];
+        break;
+      }
+  __syncwarp();
+  const unsigned prevA = B_ONLY ? a.colA[static_cast<size_t>(c) * 32 + lane] : 0u;
+  unsigned colA = 0, colB = 0, colE = 0;
+  const float gbb = a.gbb2f * 1.0001f + 1e-3f;
+  for (int i = 0; i < 32; i++) {
+    if (!((vI >> i) & 1u)) continue;  // warp-uniform
+    const float4 hi = s_hi[w][i], li = s_lo[w][i];
+    const float dx = (hi.x - hj.x) + (li.x - lj.x);
+    const float dy = (hi.y - hj.y) + (li.y - lj.y);
+    const float dz = (hi.z - hj.z) + (li.z - lj.z);
+    const float r2 = dx * dx + dy * dy + dz * dz;
+    bool in;
+    if (B_ONLY) {
+      in = (prevA >> i) & 1u;
+    } else {
+      if (!vj) {
+        in = false;
+      } else if (r2 < a.cut2f * 0.99999f) {
+        in = true;
+      } else if (r2 > a.cut2f * 1.00001f) {
+        in = false;
+      } else {  // borderline: decide exactly as the reference does, in FP64
+        const int ai = s_atom[w][i];
+        const double ddx = a.x[3 * ai] - a.x[3 * aj], ddy = a.x[3 * ai + 1] - a.x[3 * aj + 1],
+                     ddz = a.x[3 * ai + 2] - a.x[3 * aj + 2];
+        in = ddx * ddx + ddy * ddy + ddz * ddz < a.cut2;
+      }
+      in = in && vj && !(I == J && i >= lane) && !(((frzI >> i) & 1u) && frzj);
+      if (ex >= 0) colE |= ((a.excl_masks[static_cast<size_t>(ex) * 32 + i] >> lane) & 1u) << i;
+    }
+    colA |= static_cast<unsigned>(in) << i;
+    colB |= static_cast<unsigned>(in && r2 < gbb) << i;
+  }
+  const size_t e = static_cast<size_t>(c) * 32 + lane;
+  if (!B_ONLY) {
+    a.colA[e] = colA;
+    a.colE[e] = colE;
+  }
+  a.colB[e] = colB;
+  const int nA = __popc(__ballot_sync(kFull, colA != 0u)), nB = __popc(__ballot_sync(kFull, colB != 0u));
+  if (lane == 0) a.cand_n[c] = make_int2(nA, nB);
+  __syncwarp();  // the staged i-tile is rewritten by the next candidate
+  }
+}
+
+// ---- stage 3 -------------------------------------------------------------
+template <bool B_ONLY>
+__global__ void k_list_offsets(const ListArgs a) {
+  if (B_ONLY && !*a.flagB) return;
+  const int lane = threadIdx.x & 31;
+  const int I = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+  if (I >= a.ntile) return;
+  const int c0 = a.cand_start[I], n = a.cand_count[I];
+  int runA = 0, runB = 0;
+  for (int k0 = 0; k0 < n; k0 += 32) {
+    const int k = k0 + lane;
+    int2 v = k < n ? a.cand_n[c0 + k] : make_int2(0, 0);
+    int sA = v.x, sB = v.y;  // inclusive warp scan
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+      const int tA = __shfl_up_sync(kFull, sA, o), tB = __shfl_up_sync(kFull, sB, o);
+      if (lane >= o) {
+        sA += tA;
+        sB += tB;
+      }
+    }
+    if (k < n) {
+      int2 off = make_int2(runA + sA - v.x, runB + sB - v.y);
+      if (B_ONLY) off.x = a.cand_off[c0 + k].x;
+      a.cand_off[c0 + k] = off;
+    }
+    runA += __shfl_sync(kFull, sA, 31);
+    runB += __shfl_sync(kFull, sB, 31);
+  }
+  if (lane == 0) {
+    if (!B_ONLY) a.chunksA[I] = (runA + 31) >> 5;
+    a.chunksB[I] = (runB + 31) >> 5;
+  }
+}
+
+// ---- stage 4 -------------------------------------------------------------
+// Exclusive scan of chunks per i-tile, one block of 1024 threads.
+template <bool B_ONLY>
+__global__ void __launch_bounds__(1024) k_list_scan(const ListArgs a) {
+  __shared__ int s_a[1024], s_b[1024];
+  if (B_ONLY && !*a.flagB) return;
+  const int t = threadIdx.x, n = a.ntile;
+  const int per = (n + 1023) / 1024, lo = min(n, t * per), hi = min(n, lo + per);
+  int sa = 0, sb = 0;
+  for (int i = lo; i < hi; i++) {
+    if (!B_ONLY) sa += a.chunksA[i];
+    sb += a.chunksB[i];
+  }
+  s_a[t] = sa;
+  s_b[t] = sb;
+  __syncthreads();
+  for (int o = 1; o < 1024; o <<= 1) {  // inclusive Hillis-Steele scan
+    const int va = t >= o ? s_a[t - o] : 0, vb = t >= o ? s_b[t - o] : 0;
+    __syncthreads();
+    s_a[t] += va;
+    s_b[t] += vb;
+    __syncthreads();
+  }
+  int ra = s_a[t] - sa, rb = s_b[t] - sb;
+  for (int i = lo; i < hi; i++) {
+    if (!B_ONLY) {
+      a.chunk0A[i] = ra;
+      ra += a.chunksA[i];
+    }
+    a.chunk0B[i] = rb;
+    rb += a.chunksB[i];
+  }
+  if (t == 1023) {
+    if (!B_ONLY) *a.nchunkA = s_a[1023];
+    *a.nchunkB = s_b[1023];
+  }
+}
+
+// ---- stage 5 -------------------------------------------------------------
+template <bool B_ONLY>
+__global__ void k_list_fill(const ListArgs a) {
+  if (B_ONLY && !*a.flagB) return;
+  const int lane = threadIdx.x & 31;
+  const int ncand = *a.ncand, nwarps = (gridDim.x * blockDim.x) >> 5;
+  for (int c = (blockIdx.x * blockDim.x + threadIdx.x) >> 5; c < ncand; c += nwarps) {
+  const int2 p = a.cand[c];
+  const int2 off = a.cand_off[c];
+  const size_t e = static_cast<size_t>(c) * 32 + lane;
+  const unsigned lt = (1u << lane) - 1u;
+  if (!B_ONLY) {
+    const unsigned col = a.colA[e];
+    const unsigned bal = __ballot_sync(kFull, col != 0u);
+    if (col) {
+      const size_t pos = static_cast<size_t>(a.chunk0A[p.x]) * 32 + off.x + __popc(bal & lt);
+      a.entA_slot[pos] = p.y * 32 + lane;
+      a.entA_col[pos] = col;
+      a.entA_exc[pos] = a.colE[e];
+    }
+  }
+  const unsigned col = a.colB[e];
+  const unsigned bal = __ballot_sync(kFull, col != 0u);
+  if (col) {
+    const size_t pos = static_cast<size_t>(a.chunk0B[p.x]) * 32 + off.y + __popc(bal & lt);
+    a.entB_slot[pos] = p.y * 32 + lane;
+    a.entB_col[pos] = col;
+  }
+  }
+}
+
+// ---- stage 6 -------------------------------------------------------------
+// Padding entries after each i-tile's last entry, and the owner of every
+// chunk.  A padding entry points at the i-tile's own first slot with an
+// empty column, so the passes load harmless data for it.
+template <bool B_ONLY>
+__global__ void k_list_pad(const ListArgs a) {
+  if (B_ONLY && !*a.flagB) return;
+  const int lane = threadIdx.x & 31;
+  const int I = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+  if (I >= a.ntile) return;
+  const int c0 = a.cand_start[I], n = a.cand_count[I];
+  int totA = 0, totB = 0;
+  if (n > 0) {
+    const int2 lo = a.cand_off[c0 + n - 1], ln = a.cand_n[c0 + n - 1];
+    totA = lo.x + ln.x;
+    totB = lo.y + ln.y;
+  }
+  for (int list = B_ONLY ? 1 : 0; list < 2; list++) {
+    const int tot = list ? totB : totA;
+    const int ch0 = list ? a.chunk0B[I] : a.chunk0A[I];
+    const int nch = list ? a.chunksB[I] : a.chunksA[I];
+    int *slot = list ? a.entB_slot : a.entA_slot;
+    unsigned *col = list ? a.entB_col : a.entA_col;
+    int *owner = list ? a.chunkB_i : a.chunkA_i;
+    const int end = nch * 32;
+    for (int k = tot + lane; k < end; k += 32) {
+      const size_t pos = static_cast<size_t>(ch0) * 32 + k;
+      slot[pos] = I * 32;
+      col[pos] = 0u;
+      if (!list) a.entA_exc[pos] = 0u;
+    }
+    for (int k = lane; k < nch; k += 32) owner[ch0 + k] = I;
+  }
+  // list B now reflects the current positions
+  a.xb[I * 32 + lane] = a.pos_hi[I * 32 + lane];
+}
+
+// Clears the list-B flag after a (re)build; launched last.
+__global__ void k_list_done(int *flagB) { *flagB = 0; }
+
+}  // namespace sffg
