@@ -76,13 +76,14 @@ struct DeviceState {
   DBuf<int4> angle_atoms, dih_atoms, p14_atoms;
   DBuf<double4_32a> dih_par, p14_par;
   // pair lists (lists.cuh) and work counters: 0 candidates, 1 overflow,
-  // 2 chunks of list A, 3 chunks of list B, 4 list-B rebuild flag, 5..7
-  // pass queues
-  DBuf<int2> cand, cand_n, cand_off;
-  DBuf<unsigned> colA, colB, colE;
-  DBuf<int> cand_start, cand_count, chunksA, chunksB, chunk0A, chunk0B;
-  DBuf<int> chunkA_i, entA_slot, chunkB_i, entB_slot;
-  DBuf<unsigned> entA_col, entA_exc, entB_col;
+  // 2 chunks of list A, 3 chunks of list B, 4 rebuild flag of lists B and
+  // C, 5..7 queues of passes 1, 2 and 3, 10 chunks of list C
+  DBuf<int2> cand;
+  DBuf<int4> cand_n, cand_off;
+  DBuf<unsigned> colA, colB, colC, colE;
+  DBuf<int> cand_start, cand_count, chunksA, chunksB, chunksC, chunk0A, chunk0B, chunk0C;
+  DBuf<int> chunkA_i, entA_slot, chunkB_i, entB_slot, chunkC_i, entC_slot;
+  DBuf<unsigned> entA_col, entA_exc, entB_col, entC_col;
   DBuf<float4> xb;
   DBuf<int> counters;
   // model tables
@@ -118,10 +119,11 @@ struct DeviceState {
     rel(sys_atom_off); rel(lj); rel(energy); rel(etot); rel(x); rel(grad); rel(v); rel(accel);
     rel(minv); rel(sqrmass); rel(atom_slot); rel(atom_sys); rel(atom_frozen); rel(bond_atoms);
     rel(bond_par); rel(angle_par); rel(angle_atoms); rel(dih_atoms); rel(p14_atoms); rel(dih_par);
-    rel(p14_par); rel(cand); rel(cand_n); rel(cand_off); rel(colA); rel(colB); rel(colE);
-    rel(cand_start); rel(cand_count); rel(chunksA); rel(chunksB); rel(chunk0A); rel(chunk0B);
-    rel(chunkA_i); rel(entA_slot); rel(chunkB_i); rel(entB_slot); rel(entA_col); rel(entA_exc);
-    rel(entB_col); rel(xb); rel(counters); rel(neck_pos); rel(neck_val); rel(tscal);
+    rel(p14_par); rel(cand); rel(cand_n); rel(cand_off); rel(colA); rel(colB); rel(colC); rel(colE);
+    rel(cand_start); rel(cand_count); rel(chunksA); rel(chunksB); rel(chunksC); rel(chunk0A);
+    rel(chunk0B); rel(chunk0C); rel(chunkA_i); rel(entA_slot); rel(chunkB_i); rel(entB_slot);
+    rel(chunkC_i); rel(entC_slot); rel(entA_col); rel(entA_exc); rel(entB_col); rel(entC_col);
+    rel(xb); rel(counters); rel(neck_pos); rel(neck_val); rel(tscal);
     rel(noise); rel(rndf); rel(ekin); rel(cg_w); rel(cg_state);
   }
 };
@@ -458,8 +460,10 @@ int Batch::upload() {
   SFFG_CK(d.chunksB.alloc(ntile_));
   SFFG_CK(d.chunk0A.alloc(ntile_));
   SFFG_CK(d.chunk0B.alloc(ntile_));
+  SFFG_CK(d.chunksC.alloc(ntile_));
+  SFFG_CK(d.chunk0C.alloc(ntile_));
   SFFG_CK(d.xb.alloc(nslot_));
-  SFFG_CK(d.counters.alloc(8));
+  SFFG_CK(d.counters.alloc(16));
   SFFG_CK(cudaMemset(d.counters.p, 0, d.counters.bytes()));
   SFFG_CK(d.tscal.alloc(nsys));
   SFFG_CK(d.ekin.alloc(nsys));
@@ -488,9 +492,10 @@ size_t Batch::device_bytes() const {
   b += d.q64.bytes() + d.alpha.bytes() + d.beta.bytes() + d.gamma.bytes() + d.reff64.bytes();
   b += d.psi64.bytes() + d.chainfac.bytes() + d.acc_sumi.bytes() + d.acc_sd.bytes() + d.acc_fx.bytes();
   b += d.acc_fy.bytes() + d.acc_fz.bytes() + d.x.bytes();
-  b += d.cand.bytes() + d.cand_n.bytes() + d.cand_off.bytes() + d.colA.bytes() + d.colB.bytes() + d.colE.bytes();
+  b += d.cand.bytes() + d.cand_n.bytes() + d.cand_off.bytes() + d.colA.bytes() + d.colB.bytes() + d.colC.bytes() + d.colE.bytes();
   b += d.chunkA_i.bytes() + d.entA_slot.bytes() + d.entA_col.bytes() + d.entA_exc.bytes();
   b += d.chunkB_i.bytes() + d.entB_slot.bytes() + d.entB_col.bytes() + d.xb.bytes();
+  b += d.chunkC_i.bytes() + d.entC_slot.bytes() + d.entC_col.bytes();
   b += d.grad.bytes() + d.v.bytes() + d.accel.bytes() + d.minv.bytes() + d.sqrmass.bytes();
   b += d.excl_masks.bytes() + d.cg_w.bytes() + d.noise.bytes();
   b += d.bond_par.bytes() + d.angle_par.bytes() + d.dih_par.bytes() + d.p14_par.bytes();
@@ -626,6 +631,11 @@ DevTables make_tables(DeviceState &d, const ModelParams &mp, double fsmax, int q
   t.lb.col = d.entB_col.p;
   t.lb.exc = nullptr;
   t.lb.nchunk = d.counters.p + 3;
+  t.lc.chunk_i = d.chunkC_i.p;
+  t.lc.slot = d.entC_slot.p;
+  t.lc.col = d.entC_col.p;
+  t.lc.exc = nullptr;
+  t.lc.nchunk = d.counters.p + 10;
   t.counter = d.counters.p + queue;
   t.acc_sumi = d.acc_sumi.p;
   t.acc_sd = d.acc_sd.p;
@@ -692,15 +702,20 @@ ListArgs Batch::list_args(double fsmax) {
   a.cand_count = d.cand_count.p;
   a.colA = d.colA.p;
   a.colB = d.colB.p;
+  a.colC = d.colC.p;
   a.colE = d.colE.p;
+  a.gbpar = d.gbpar.p;
   a.cand_n = d.cand_n.p;
   a.cand_off = d.cand_off.p;
   a.chunksA = d.chunksA.p;
   a.chunksB = d.chunksB.p;
   a.chunk0A = d.chunk0A.p;
   a.chunk0B = d.chunk0B.p;
+  a.chunksC = d.chunksC.p;
+  a.chunk0C = d.chunk0C.p;
   a.nchunkA = d.counters.p + 2;
   a.nchunkB = d.counters.p + 3;
+  a.nchunkC = d.counters.p + 10;
   a.chunkA_i = d.chunkA_i.p;
   a.entA_slot = d.entA_slot.p;
   a.entA_col = d.entA_col.p;
@@ -708,6 +723,9 @@ ListArgs Batch::list_args(double fsmax) {
   a.chunkB_i = d.chunkB_i.p;
   a.entB_slot = d.entB_slot.p;
   a.entB_col = d.entB_col.p;
+  a.chunkC_i = d.chunkC_i.p;
+  a.entC_slot = d.entC_slot.p;
+  a.entC_col = d.entC_col.p;
   a.flagB = d.counters.p + 4;
   a.xb = d.xb.p;
   return a;
@@ -746,6 +764,7 @@ int Batch::build_lists(void *stream) {
   const size_t nc = std::max(1, ncand_);
   SFFG_CK(ensure(d.colA, nc * 32));
   SFFG_CK(ensure(d.colB, nc * 32));
+  SFFG_CK(ensure(d.colC, nc * 32));
   SFFG_CK(ensure(d.colE, nc * 32));
   SFFG_CK(ensure(d.cand_n, nc));
   SFFG_CK(ensure(d.cand_off, nc));
@@ -761,8 +780,8 @@ int Batch::build_lists(void *stream) {
   int nch = 0;
   SFFG_CK(cudaMemcpyAsync(&nch, d.counters.p + 2, sizeof(int), cudaMemcpyDeviceToHost, st));
   SFFG_CK(cudaStreamSynchronize(st));
-  // list B is a subset of list A: the same capacity serves both, also when
-  // list B is remade later
+  // lists B and C are subsets of list A: the same capacity serves all
+  // three, also when B and C are remade later
   const size_t ne = static_cast<size_t>(std::max(1, nch)) * 32;
   SFFG_CK(ensure(d.entA_slot, ne));
   SFFG_CK(ensure(d.entA_col, ne));
@@ -771,6 +790,9 @@ int Batch::build_lists(void *stream) {
   SFFG_CK(ensure(d.entB_col, ne));
   SFFG_CK(ensure(d.chunkA_i, ne / 32));
   SFFG_CK(ensure(d.chunkB_i, ne / 32));
+  SFFG_CK(ensure(d.entC_slot, ne));
+  SFFG_CK(ensure(d.entC_col, ne));
+  SFFG_CK(ensure(d.chunkC_i, ne / 32));
   {
     const ListArgs a = list_args(fsmax);
     k_list_fill<false><<<cand_blocks, 256, 0, st>>>(a);
@@ -813,7 +835,7 @@ int Batch::run_eval(bool rebuild, void *stream) {
   DeviceState &d = *d_;
   cudaStream_t st = pick(d, stream);
   const int nsys = num_systems();
-  SFFG_CK(cudaMemsetAsync(d.counters.p + 5, 0, 3 * sizeof(int), st));
+  SFFG_CK(cudaMemsetAsync(d.counters.p + 5, 0, 5 * sizeof(int), st));
   SFFG_CK(cudaMemsetAsync(d.energy.p, 0, d.energy.bytes(), st));
   k_pack<<<(nslot_ + 255) / 256, 256, 0, st>>>(d.x.p, d.slot_atom.p, d.q32.p, d.tile_valid.p, nslot_, d.pos_hi.p,
                                                d.pos_lo.p, d.box_lo.p, d.box_hi.p, d.acc_sumi.p, d.acc_fx.p,
@@ -911,7 +933,7 @@ int Batch::run_eval(bool rebuild, void *stream) {
                                                             d.grad.p, natom_total_);
   k_energy_total<<<(nsys + 127) / 128, 128, 0, st>>>(d.energy.p, d.etot.p, nsys);
   SFFG_CK(cudaGetLastError());
-  // pack, four bonded kinds (when present), three passes, Born finish,
+  // pack, four bonded kinds (when present), three pair kernels, Born finish,
   // chain prep, gather, energy total
   launches_ += 9 + (d.bond_atoms.n > 0) + (d.angle_atoms.n > 0) + (d.dih_atoms.n > 0) + (d.p14_atoms.n > 0);
   timers().nevals++;

@@ -47,9 +47,9 @@ struct DevTables {
   const int *sys_lj_off;
   const int *sys_ntypes;
   const float2 *lj;       // (A, B) per type pair, per system blocks
-  // lists: la (r < cut) for pass 2, lb (r < rgbmax + Fsmax + skin) for
-  // passes 1 and 3
-  ChunkList la, lb;
+  // lists: la (r < cut) for pass 2; lb and lc (r < rgbmax + Fsmax + skin,
+  // lc the pairs within near-field range) for passes 1 and 3
+  ChunkList la, lb, lc;
   int *counter;
   // accumulators
   long long *acc_sumi, *acc_sd, *acc_fx, *acc_fy, *acc_fz;
@@ -122,30 +122,26 @@ __device__ __forceinline__ int claim_chunk(int *counter, int lane) {
   return __shfl_sync(kFull, base, 0);
 }
 
-// Both directions of the descreening of one pair (value, or for DERIV the
-// derivative / dij): vi is atom i descreened by sphere j, vj the converse.
-// Only warp-uniform branches: the far-field Taylor form is evaluated for
-// every lane, the rgbmax-tail quadrature when any lane of the warp needs
-// it, and the near field (rare) out of line for the lanes that need it, so
-// a warp walks one short code path instead of a divergent ladder.
+// Both directions of the descreening of one pair of list B (value, or for
+// DERIV the derivative / dij): vi is atom i descreened by sphere j, vj the
+// converse.  List B holds no pair within near-field range, so only the far
+// field (evaluated for every lane), the rgbmax tail (evaluated when any
+// lane of the warp needs it) and the zero beyond rgbmax + s remain; the
+// branches are warp-uniform.
 template <bool DERIV>
-__device__ __forceinline__ void descreen_pair(const BornConst &c, bool in, float dij, float r2, float d1,
-                                              float rho_i, float s_i, float rho_j, float s_j, float &vi,
-                                              float &vj) {
+__device__ __forceinline__ void descreen_pair(const BornConst &c, bool in, float dij, float d1, float s_i,
+                                              float s_j, float &vi, float &vj) {
   vi = DERIV ? far_deriv(d1, s_j) : far_term(d1, s_j);
   vj = DERIV ? far_deriv(d1, s_i) : far_term(d1, s_i);
   const bool ti = dij > c.rgbmax - s_j, tj = dij > c.rgbmax - s_i;
   if (__any_sync(kFull, in && (ti || tj))) {
-    const float qi = tail_quad<DERIV>(c.rgbmax, r2, dij, d1, s_j);
-    const float qj = tail_quad<DERIV>(c.rgbmax, r2, dij, d1, s_i);
+    const float qi = tail_closed<DERIV>(c, dij, d1, s_j);
+    const float qj = tail_closed<DERIV>(c, dij, d1, s_i);
     vi = ti ? qi : vi;
     vj = tj ? qj : vj;
   }
-  const bool ni = in && !ti && dij <= 4.0f * s_j, nj = in && !tj && dij <= 4.0f * s_i;
-  if (__any_sync(kFull, ni || nj)) {
-    if (ni) vi = DERIV ? descreen_deriv_near(dij, r2, d1, rho_i, s_j) : descreen_near(dij, r2, d1, rho_i, s_j);
-    if (nj) vj = DERIV ? descreen_deriv_near(dij, r2, d1, rho_j, s_i) : descreen_near(dij, r2, d1, rho_j, s_i);
-  }
+  // beyond rgbmax + s the term is zero; with a negative s (GBneck2 screens
+  // sulfur with fs < 0) that range starts below rgbmax - s
   vi = dij > c.rgbmax + s_j ? 0.0f : vi;
   vj = dij > c.rgbmax + s_i ? 0.0f : vj;
 }
@@ -159,14 +155,90 @@ __device__ __forceinline__ int chunk_entry(const ChunkList &L, int k, int lane, 
   return L.slot[e];
 }
 
+// ------------------------------------------------------------ list C chunks
+// List C holds the pairs close enough for the near-field forms; its chunks
+// are sparse (~13% of the 32 x 32 bits set), so a warp walks the set bits
+// of a chunk 32 pairs at a time, one pair per lane, and evaluates the whole
+// ladder of the reference for both directions.  Lane t then collects, in
+// pair order, the terms of i-atom t and of j-entry t (a fixed order, so the
+// sums are deterministic).
+//
+// Passes 1 and 3 take the chunks of lists B and C from one work queue, the
+// list C chunks spread evenly among the others: near-field chunks are
+// latency-bound (long dependent chains, little work), far-field chunks
+// throughput-bound, and mixing them keeps every SM issuing.
+
+// Work item m of the merged queue: true and the list C chunk k, or false
+// and the list B chunk k.
+__device__ __forceinline__ bool merged_item(int m, int nB, int nC, int &k) {
+  const long long n = static_cast<long long>(nB) + nC;
+  const int c0 = static_cast<int>(static_cast<long long>(m) * nC / n);
+  const int c1 = static_cast<int>(static_cast<long long>(m + 1) * nC / n);
+  k = c1 > c0 ? c0 : m - c0;
+  return c1 > c0;
+}
+
+
+
+// Pair p of the chunk (0 <= p < total): its j-entry and i-lane, from the
+// exclusive prefix counts s_pre of set bits per entry.
+__device__ __forceinline__ void near_pair(const int *s_pre, const unsigned *s_col, int p, int &il, int &jl) {
+  int j = 0;
+#pragma unroll
+  for (int b = 16; b > 0; b >>= 1)
+    if (s_pre[j + b] <= p) j += b;
+  jl = j;
+  // position of set bit number r (from 0) of the entry's column
+  unsigned m = s_col[j];
+  int r = p - s_pre[j], pos = 0;
+#pragma unroll
+  for (int b = 16; b > 0; b >>= 1) {
+    const int c = __popc(m & ((1u << b) - 1u));
+    if (c <= r) {
+      r -= c;
+      m >>= b;
+      pos += b;
+    }
+  }
+  il = pos;
+}
+
+// Stages chunk k of list C: j-entries in shared memory, their bit counts'
+// exclusive prefix; returns the chunk's pair count.
+__device__ __forceinline__ int near_stage(const DevTables &t, int k, int lane, float4 *hj, float4 *lj,
+                                          float4 *gj, int *pj, unsigned *cj, int *pre, int &sj, unsigned &col,
+                                          bool sda) {
+  const size_t e = static_cast<size_t>(k) * 32 + lane;
+  col = t.lc.col[e];
+  sj = t.lc.slot[e];
+  float4 l = t.pos_lo[sj];
+  if (sda) l.w = t.sumda32[sj];
+  hj[lane] = t.pos_hi[sj];
+  lj[lane] = l;
+  gj[lane] = t.gbpar[sj];
+  pj[lane] = t.param[sj];
+  cj[lane] = col;
+  const int c = __popc(col);
+  int incl = c;
+#pragma unroll
+  for (int o = 1; o < 32; o <<= 1) {
+    const int v = __shfl_up_sync(kFull, incl, o);
+    if (lane >= o) incl += v;
+  }
+  pre[lane] = incl - c;
+  __syncwarp();
+  return __shfl_sync(kFull, incl, 31);
+}
+
 // ------------------------------------------------------------------ pass 1
 // Born-radius descreening sums (src/sff/eff.c:1566-1709): both directions
-// of every pair of list B within rgbmax + Fsmax.
+// of every pair within rgbmax + Fsmax, over lists B and C.
 template <bool NECK>
 __global__ void __launch_bounds__(256, 2) k_born(const DevTables t) {
-  __shared__ float4 sm_hi[8][32], sm_lo[8][32], sm_gb[8][32];
+  __shared__ float4 sm_hi[8][32], sm_lo[8][32], sm_gb[8][32];  // j entries of the chunk
+  __shared__ float4 si_hi[8][32], si_lo[8][32], si_gb[8][32];  // the i-tile
   __shared__ unsigned sm_col[8][32];
-  __shared__ int sm_par[8][NECK ? 32 : 1];
+  __shared__ int sm_par[8][32], si_par[8][32], s_pre[8][32];
   __shared__ float s_npos[NECK ? 441 : 1], s_nval[NECK ? 441 : 1];
   if (NECK) {
     for (int i = threadIdx.x; i < 441; i += blockDim.x) {
@@ -176,17 +248,120 @@ __global__ void __launch_bounds__(256, 2) k_born(const DevTables t) {
     __syncthreads();
   }
   const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
-  const int nchunk = *t.lb.nchunk;
+  const int nB = *t.lb.nchunk, nC = *t.lc.nchunk, nitem = nB + nC;
+  const float FB = 1099511627776.0f;
   int cur_I = -1;
-  float xi = 0, yi = 0, zi = 0, xli = 0, yli = 0, zli = 0, rhoi = 1, si = 0, rbi = 0, sci = 0;
+  float xi = 0, yi = 0, zi = 0, xli = 0, yli = 0, zli = 0, si = 0, rbi = 0, sci = 0;
   int nki = 0;
   long long sumi64 = 0;
+
+  // list B chunk k: lanes hold the i-tile, steps walk the 32 j-entries
+  auto far_chunk = [&](int k) {
+    unsigned mycol;
+    const int sj = chunk_entry(t.lb, k, lane, mycol);
+    sm_hi[w][lane] = t.pos_hi[sj];
+    sm_lo[w][lane] = t.pos_lo[sj];
+    sm_gb[w][lane] = t.gbpar[sj];
+    sm_col[w][lane] = mycol;
+    if (NECK) sm_par[w][lane] = t.param[sj];
+    const unsigned cols = __ballot_sync(kFull, mycol != 0u);
+    __syncwarp();
+    float acc_i = 0.0f, acc_j = 0.0f;
+#pragma unroll 1
+    for (int g = 0; g < 32 / kGroup; g++) {
+      float aj[kGroup];
+#pragma unroll
+      for (int s = 0; s < kGroup; s++) {
+        const int j = g * kGroup + s;
+        aj[s] = 0.0f;
+        if (!((cols >> j) & 1u)) continue;  // padding entry
+        const float4 h = sm_hi[w][j], l = sm_lo[w][j], gp = sm_gb[w][j];
+        const float dx = (xi - h.x) + (xli - l.x);
+        const float dy = (yi - h.y) + (yli - l.y);
+        const float dz = (zi - h.z) + (zli - l.z);
+        const float r2 = fmaf(dx, dx, fmaf(dy, dy, dz * dz));
+        const bool in = ((sm_col[w][j] >> lane) & 1u) && r2 <= t.born.cutoff2;
+        if (!__any_sync(kFull, in)) continue;  // every lane out of range
+        const float dij1i = rsqrt_nr(r2);
+        const float dij = r2 * dij1i;
+        float ti, tj;
+        descreen_pair<false>(t.born, in, dij, dij1i, si, gp.y, ti, tj);
+        ti = fmaf(ti, gp.w, ti);
+        tj = fmaf(tj, sci, tj);
+        if (NECK) {
+          const bool nk = in && dij < rbi + gp.z + 6.8f;
+          if (__any_sync(kFull, nk)) {
+            const int nkj = (sm_par[w][j] >> 16) & 0xff;
+            const float a = neck_term(dij, s_npos[nki * 21 + nkj], s_nval[nki * 21 + nkj], t.neck_scale);
+            const float b = neck_term(dij, s_npos[nkj * 21 + nki], s_nval[nkj * 21 + nki], t.neck_scale);
+            ti += nk ? a : 0.0f;
+            tj += nk ? b : 0.0f;
+          }
+        }
+        acc_i += in ? ti : 0.0f;
+        aj[s] = in ? tj : 0.0f;
+      }
+      acc_j += reduce_to_lane(aj, g, lane);
+    }
+    sumi64 += to_fixed(acc_i, FB);
+    if (mycol) atomic_add_ll(&t.acc_sumi[sj], to_fixed(acc_j, FB));
+    __syncwarp();
+  };
+
+  // list C chunk k: 32 compacted pairs per round, one per lane
+  auto near_chunk = [&](int k) {
+    int sj;
+    unsigned mycol;
+    const int total =
+        near_stage(t, k, lane, sm_hi[w], sm_lo[w], sm_gb[w], sm_par[w], sm_col[w], s_pre[w], sj, mycol, false);
+    float acc_i = 0.0f, acc_j = 0.0f;
+    for (int b0 = 0; b0 < total; b0 += 32) {
+      const int p = b0 + lane;
+      float ti = 0.0f, tj = 0.0f;
+      int il = 0, jl = 0;
+      if (p < total) {
+        near_pair(s_pre[w], sm_col[w], p, il, jl);
+        const float4 hi = si_hi[w][il], li = si_lo[w][il], gi = si_gb[w][il];
+        const float4 h = sm_hi[w][jl], l = sm_lo[w][jl], gp = sm_gb[w][jl];
+        const float dx = (hi.x - h.x) + (li.x - l.x);
+        const float dy = (hi.y - h.y) + (li.y - l.y);
+        const float dz = (hi.z - h.z) + (li.z - l.z);
+        const float r2 = fmaf(dx, dx, fmaf(dy, dy, dz * dz));
+        if (r2 <= t.born.cutoff2) {
+          const float d1 = rsqrt_nr(r2);
+          const float dij = r2 * d1;
+          ti = descreen(t.born, dij, r2, d1, gi.x, gp.y);
+          tj = descreen(t.born, dij, r2, d1, gp.x, gi.y);
+          ti = fmaf(ti, gp.w, ti);
+          tj = fmaf(tj, gi.w, tj);
+          if (NECK && dij < gi.z + gp.z + 6.8f) {
+            const int nkp = (si_par[w][il] >> 16) & 0xff, nkj = (sm_par[w][jl] >> 16) & 0xff;
+            ti += neck_term(dij, s_npos[nkp * 21 + nkj], s_nval[nkp * 21 + nkj], t.neck_scale);
+            tj += neck_term(dij, s_npos[nkj * 21 + nkp], s_nval[nkj * 21 + nkp], t.neck_scale);
+          }
+        }
+      }
+      const int n = min(32, total - b0);
+      for (int q = 0; q < n; q++) {
+        const float a = __shfl_sync(kFull, ti, q), c = __shfl_sync(kFull, tj, q);
+        const int iq = __shfl_sync(kFull, il, q), jq = __shfl_sync(kFull, jl, q);
+        acc_i += iq == lane ? a : 0.0f;
+        acc_j += jq == lane ? c : 0.0f;
+      }
+    }
+    sumi64 += to_fixed(acc_i, FB);
+    if (mycol) atomic_add_ll(&t.acc_sumi[sj], to_fixed(acc_j, FB));
+    __syncwarp();
+  };
+
   for (;;) {
     const int base = claim_chunk(t.counter, lane);
-    if (base >= nchunk) break;
-    const int end = min(base + kChunk, nchunk);
-    for (int k = base; k < end; k++) {
-      const int I = t.lb.chunk_i[k];
+    if (base >= nitem) break;
+    const int end = min(base + kChunk, nitem);
+    for (int m = base; m < end; m++) {
+      int k;
+      const bool nr = merged_item(m, nB, nC, k);
+      const int I = nr ? t.lc.chunk_i[k] : t.lb.chunk_i[k];
       if (!t.sys_active[t.tile_sys[I]]) continue;
       if (I != cur_I) {
         if (cur_I >= 0) atomic_add_ll(&t.acc_sumi[cur_I * 32 + lane], sumi64);
@@ -194,59 +369,17 @@ __global__ void __launch_bounds__(256, 2) k_born(const DevTables t) {
         sumi64 = 0;
         const int sl = I * 32 + lane;
         const float4 h = t.pos_hi[sl], l = t.pos_lo[sl], g = t.gbpar[sl];
+        const int pr = t.param[sl];
         xi = h.x; yi = h.y; zi = h.z; xli = l.x; yli = l.y; zli = l.z;
-        rhoi = g.x; si = g.y; rbi = g.z; sci = g.w;
-        nki = (t.param[sl] >> 16) & 0xff;
+        si = g.y; rbi = g.z; sci = g.w;
+        nki = (pr >> 16) & 0xff;
+        si_hi[w][lane] = h;
+        si_lo[w][lane] = l;
+        si_gb[w][lane] = g;
+        si_par[w][lane] = pr;
       }
-      unsigned mycol;
-      const int sj = chunk_entry(t.lb, k, lane, mycol);
-      sm_hi[w][lane] = t.pos_hi[sj];
-      sm_lo[w][lane] = t.pos_lo[sj];
-      sm_gb[w][lane] = t.gbpar[sj];
-      sm_col[w][lane] = mycol;
-      if (NECK) sm_par[w][lane] = t.param[sj];
-      const unsigned cols = __ballot_sync(kFull, mycol != 0u);
-      __syncwarp();
-      float acc_i = 0.0f, acc_j = 0.0f;
-#pragma unroll 1
-      for (int g = 0; g < 32 / kGroup; g++) {
-        float aj[kGroup];
-#pragma unroll
-        for (int s = 0; s < kGroup; s++) {
-          const int j = g * kGroup + s;
-          aj[s] = 0.0f;
-          if (!((cols >> j) & 1u)) continue;  // padding entry
-          const float4 h = sm_hi[w][j], l = sm_lo[w][j], gp = sm_gb[w][j];
-          const float dx = (xi - h.x) + (xli - l.x);
-          const float dy = (yi - h.y) + (yli - l.y);
-          const float dz = (zi - h.z) + (zli - l.z);
-          const float r2 = fmaf(dx, dx, fmaf(dy, dy, dz * dz));
-          const bool in = ((sm_col[w][j] >> lane) & 1u) && r2 <= t.born.cutoff2;
-          if (!__any_sync(kFull, in)) continue;  // every lane out of range
-          const float dij1i = rsqrt_nr(r2);
-          const float dij = r2 * dij1i;
-          float ti, tj;
-          descreen_pair<false>(t.born, in, dij, r2, dij1i, rhoi, si, gp.x, gp.y, ti, tj);
-          ti = fmaf(ti, gp.w, ti);
-          tj = fmaf(tj, sci, tj);
-          if (NECK) {
-            const bool nk = in && dij < rbi + gp.z + 6.8f;
-            if (__any_sync(kFull, nk)) {
-              const int nkj = (sm_par[w][j] >> 16) & 0xff;
-              const float a = neck_term(dij, s_npos[nki * 21 + nkj], s_nval[nki * 21 + nkj], t.neck_scale);
-              const float b = neck_term(dij, s_npos[nkj * 21 + nki], s_nval[nkj * 21 + nki], t.neck_scale);
-              ti += nk ? a : 0.0f;
-              tj += nk ? b : 0.0f;
-            }
-          }
-          acc_i += in ? ti : 0.0f;
-          aj[s] = in ? tj : 0.0f;
-        }
-        acc_j += reduce_to_lane(aj, g, lane);
-      }
-      sumi64 += to_fixed(acc_i, 1099511627776.0f);
-      if (mycol) atomic_add_ll(&t.acc_sumi[sj], to_fixed(acc_j, 1099511627776.0f));
-      __syncwarp();
+      if (nr) near_chunk(k);
+      else far_chunk(k);
     }
   }
   if (cur_I >= 0) atomic_add_ll(&t.acc_sumi[cur_I * 32 + lane], sumi64);
@@ -381,14 +514,15 @@ __global__ void __launch_bounds__(256, 2) k_gbpair(const DevTables t) {
 }
 
 // ------------------------------------------------------------------ pass 3
-// Chain rule through the Born radii (src/sff/eff.c:2241-2395) over list B:
-// for each pair within rgbmax + Fsmax, g = sumda_i d_ij + sumda_j d_ji,
-// f_i -= g r_ij, f_j += g r_ij.
+// Chain rule through the Born radii (src/sff/eff.c:2241-2395) over lists B
+// and C: for each pair within rgbmax + Fsmax, g = sumda_i d_ij +
+// sumda_j d_ji, f_i -= g r_ij, f_j += g r_ij.
 template <bool NECK>
 __global__ void __launch_bounds__(256, 2) k_chain(const DevTables t) {
-  __shared__ float4 sm_hi[8][32], sm_lo[8][32], sm_gb[8][32];
+  __shared__ float4 sm_hi[8][32], sm_lo[8][32], sm_gb[8][32];  // j entries (lo.w = sumda)
+  __shared__ float4 si_hi[8][32], si_lo[8][32], si_gb[8][32];  // the i-tile (lo.w = sumda)
   __shared__ unsigned sm_col[8][32];
-  __shared__ int sm_par[8][NECK ? 32 : 1];
+  __shared__ int sm_par[8][32], si_par[8][32], s_pre[8][32];
   __shared__ float s_npos[NECK ? 441 : 1], s_nval[NECK ? 441 : 1];
   if (NECK) {
     for (int i = threadIdx.x; i < 441; i += blockDim.x) {
@@ -398,10 +532,10 @@ __global__ void __launch_bounds__(256, 2) k_chain(const DevTables t) {
     __syncthreads();
   }
   const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
-  const int nchunk = *t.lb.nchunk;
+  const int nB = *t.lb.nchunk, nC = *t.lc.nchunk, nitem = nB + nC;
   const float FS = 4294967296.0f;
   int cur_I = -1;
-  float xi = 0, yi = 0, zi = 0, xli = 0, yli = 0, zli = 0, rhoi = 1, si = 0, rbi = 0, sci = 0, sdai = 0;
+  float xi = 0, yi = 0, zi = 0, xli = 0, yli = 0, zli = 0, si = 0, rbi = 0, sci = 0, sdai = 0;
   int nki = 0;
   long long fx64 = 0, fy64 = 0, fz64 = 0;
   auto flush_i = [&]() {
@@ -410,90 +544,163 @@ __global__ void __launch_bounds__(256, 2) k_chain(const DevTables t) {
     atomic_add_ll(&t.acc_fy[sl], fy64);
     atomic_add_ll(&t.acc_fz[sl], fz64);
   };
+  auto add_j = [&](int sj, float jx, float jy, float jz) {
+    atomic_add_ll(&t.acc_fx[sj], to_fixed(jx, FS));
+    atomic_add_ll(&t.acc_fy[sj], to_fixed(jy, FS));
+    atomic_add_ll(&t.acc_fz[sj], to_fixed(jz, FS));
+  };
+
+  auto far_chunk = [&](int k) {
+    unsigned mycol;
+    const int sj = chunk_entry(t.lb, k, lane, mycol);
+    {
+      float4 l = t.pos_lo[sj];
+      l.w = t.sumda32[sj];
+      sm_hi[w][lane] = t.pos_hi[sj];
+      sm_lo[w][lane] = l;
+      sm_gb[w][lane] = t.gbpar[sj];
+      sm_col[w][lane] = mycol;
+      if (NECK) sm_par[w][lane] = t.param[sj];
+    }
+    const unsigned cols = __ballot_sync(kFull, mycol != 0u);
+    __syncwarp();
+    float fix = 0, fiy = 0, fiz = 0, jx = 0, jy = 0, jz = 0;
+#pragma unroll 1
+    for (int g = 0; g < 32 / kGroup; g++) {
+      float ax[kGroup], ay[kGroup], az[kGroup];
+#pragma unroll
+      for (int s = 0; s < kGroup; s++) {
+        const int j = g * kGroup + s;
+        ax[s] = ay[s] = az[s] = 0.0f;
+        if (!((cols >> j) & 1u)) continue;
+        const float4 h = sm_hi[w][j], l = sm_lo[w][j], gp = sm_gb[w][j];
+        const float dx = (xi - h.x) + (xli - l.x);
+        const float dy = (yi - h.y) + (yli - l.y);
+        const float dz = (zi - h.z) + (zli - l.z);
+        const float r2 = fmaf(dx, dx, fmaf(dy, dy, dz * dz));
+        const bool in = ((sm_col[w][j] >> lane) & 1u) && r2 <= t.born.cutoff2;
+        if (!__any_sync(kFull, in)) continue;
+        const float dij1i = rsqrt_nr(r2);
+        const float dij = r2 * dij1i;
+        float di, dj;
+        descreen_pair<true>(t.born, in, dij, dij1i, si, gp.y, di, dj);
+        di = fmaf(di, gp.w, di);
+        dj = fmaf(dj, sci, dj);
+        if (NECK) {
+          const bool nk = in && dij < rbi + gp.z + 6.8f;
+          if (__any_sync(kFull, nk)) {
+            const int nkj = (sm_par[w][j] >> 16) & 0xff;
+            const float a = neck_deriv(dij, s_npos[nki * 21 + nkj], s_nval[nki * 21 + nkj], t.neck_scale);
+            const float b = neck_deriv(dij, s_npos[nkj * 21 + nki], s_nval[nkj * 21 + nki], t.neck_scale);
+            di += nk ? a : 0.0f;
+            dj += nk ? b : 0.0f;
+          }
+        }
+        const float gg = in ? fmaf(sdai, di, l.w * dj) : 0.0f;
+        fix = fmaf(-gg, dx, fix);
+        fiy = fmaf(-gg, dy, fiy);
+        fiz = fmaf(-gg, dz, fiz);
+        ax[s] = gg * dx;
+        ay[s] = gg * dy;
+        az[s] = gg * dz;
+      }
+      jx += reduce_to_lane(ax, g, lane);
+      jy += reduce_to_lane(ay, g, lane);
+      jz += reduce_to_lane(az, g, lane);
+    }
+    fx64 += to_fixed(fix, FS);
+    fy64 += to_fixed(fiy, FS);
+    fz64 += to_fixed(fiz, FS);
+    if (mycol) add_j(sj, jx, jy, jz);
+    __syncwarp();
+  };
+
+  auto near_chunk = [&](int k) {
+    int sj;
+    unsigned mycol;
+    const int total =
+        near_stage(t, k, lane, sm_hi[w], sm_lo[w], sm_gb[w], sm_par[w], sm_col[w], s_pre[w], sj, mycol, true);
+    float fix = 0, fiy = 0, fiz = 0, jx = 0, jy = 0, jz = 0;
+    for (int b0 = 0; b0 < total; b0 += 32) {
+      const int p = b0 + lane;
+      float gx = 0.0f, gy = 0.0f, gz = 0.0f;
+      int il = 0, jl = 0;
+      if (p < total) {
+        near_pair(s_pre[w], sm_col[w], p, il, jl);
+        const float4 hi = si_hi[w][il], li = si_lo[w][il], gi = si_gb[w][il];
+        const float4 h = sm_hi[w][jl], l = sm_lo[w][jl], gp = sm_gb[w][jl];
+        const float dx = (hi.x - h.x) + (li.x - l.x);
+        const float dy = (hi.y - h.y) + (li.y - l.y);
+        const float dz = (hi.z - h.z) + (li.z - l.z);
+        const float r2 = fmaf(dx, dx, fmaf(dy, dy, dz * dz));
+        if (r2 <= t.born.cutoff2) {
+          const float d1 = rsqrt_nr(r2);
+          const float dij = r2 * d1;
+          float di = descreen_deriv(t.born, dij, r2, d1, gi.x, gp.y);
+          float dj = descreen_deriv(t.born, dij, r2, d1, gp.x, gi.y);
+          di = fmaf(di, gp.w, di);
+          dj = fmaf(dj, gi.w, dj);
+          if (NECK && dij < gi.z + gp.z + 6.8f) {
+            const int nkp = (si_par[w][il] >> 16) & 0xff, nkj = (sm_par[w][jl] >> 16) & 0xff;
+            di += neck_deriv(dij, s_npos[nkp * 21 + nkj], s_nval[nkp * 21 + nkj], t.neck_scale);
+            dj += neck_deriv(dij, s_npos[nkj * 21 + nkp], s_nval[nkj * 21 + nkp], t.neck_scale);
+          }
+          const float gg = fmaf(li.w, di, l.w * dj);
+          gx = gg * dx;
+          gy = gg * dy;
+          gz = gg * dz;
+        }
+      }
+      const int n = min(32, total - b0);
+      for (int q = 0; q < n; q++) {
+        const float ax = __shfl_sync(kFull, gx, q), ay = __shfl_sync(kFull, gy, q),
+                    az = __shfl_sync(kFull, gz, q);
+        const int iq = __shfl_sync(kFull, il, q), jq = __shfl_sync(kFull, jl, q);
+        const bool mi = iq == lane, mj = jq == lane;
+        fix -= mi ? ax : 0.0f;
+        fiy -= mi ? ay : 0.0f;
+        fiz -= mi ? az : 0.0f;
+        jx += mj ? ax : 0.0f;
+        jy += mj ? ay : 0.0f;
+        jz += mj ? az : 0.0f;
+      }
+    }
+    fx64 += to_fixed(fix, FS);
+    fy64 += to_fixed(fiy, FS);
+    fz64 += to_fixed(fiz, FS);
+    if (mycol) add_j(sj, jx, jy, jz);
+    __syncwarp();
+  };
+
   for (;;) {
     const int base = claim_chunk(t.counter, lane);
-    if (base >= nchunk) break;
-    const int end = min(base + kChunk, nchunk);
-    for (int k = base; k < end; k++) {
-      const int I = t.lb.chunk_i[k];
+    if (base >= nitem) break;
+    const int end = min(base + kChunk, nitem);
+    for (int m = base; m < end; m++) {
+      int k;
+      const bool nr = merged_item(m, nB, nC, k);
+      const int I = nr ? t.lc.chunk_i[k] : t.lb.chunk_i[k];
       if (!t.sys_active[t.tile_sys[I]]) continue;
       if (I != cur_I) {
         if (cur_I >= 0) flush_i();
         cur_I = I;
         fx64 = fy64 = fz64 = 0;
         const int sl = I * 32 + lane;
-        const float4 h = t.pos_hi[sl], l = t.pos_lo[sl], g = t.gbpar[sl];
+        const float4 h = t.pos_hi[sl], g = t.gbpar[sl];
+        float4 l = t.pos_lo[sl];
+        const int pr = t.param[sl];
         xi = h.x; yi = h.y; zi = h.z; xli = l.x; yli = l.y; zli = l.z;
-        rhoi = g.x; si = g.y; rbi = g.z; sci = g.w;
+        si = g.y; rbi = g.z; sci = g.w;
         sdai = t.sumda32[sl];
-        nki = (t.param[sl] >> 16) & 0xff;
+        nki = (pr >> 16) & 0xff;
+        l.w = sdai;
+        si_hi[w][lane] = h;
+        si_lo[w][lane] = l;
+        si_gb[w][lane] = g;
+        si_par[w][lane] = pr;
       }
-      unsigned mycol;
-      const int sj = chunk_entry(t.lb, k, lane, mycol);
-      {
-        float4 l = t.pos_lo[sj];
-        l.w = t.sumda32[sj];
-        sm_hi[w][lane] = t.pos_hi[sj];
-        sm_lo[w][lane] = l;
-        sm_gb[w][lane] = t.gbpar[sj];
-        sm_col[w][lane] = mycol;
-        if (NECK) sm_par[w][lane] = t.param[sj];
-      }
-      const unsigned cols = __ballot_sync(kFull, mycol != 0u);
-      __syncwarp();
-      float fix = 0, fiy = 0, fiz = 0, jx = 0, jy = 0, jz = 0;
-#pragma unroll 1
-      for (int g = 0; g < 32 / kGroup; g++) {
-        float ax[kGroup], ay[kGroup], az[kGroup];
-#pragma unroll
-        for (int s = 0; s < kGroup; s++) {
-          const int j = g * kGroup + s;
-          ax[s] = ay[s] = az[s] = 0.0f;
-          if (!((cols >> j) & 1u)) continue;
-          const float4 h = sm_hi[w][j], l = sm_lo[w][j], gp = sm_gb[w][j];
-          const float dx = (xi - h.x) + (xli - l.x);
-          const float dy = (yi - h.y) + (yli - l.y);
-          const float dz = (zi - h.z) + (zli - l.z);
-          const float r2 = fmaf(dx, dx, fmaf(dy, dy, dz * dz));
-          const bool in = ((sm_col[w][j] >> lane) & 1u) && r2 <= t.born.cutoff2;
-          if (!__any_sync(kFull, in)) continue;
-          const float dij1i = rsqrt_nr(r2);
-          const float dij = r2 * dij1i;
-          float di, dj;
-          descreen_pair<true>(t.born, in, dij, r2, dij1i, rhoi, si, gp.x, gp.y, di, dj);
-          di = fmaf(di, gp.w, di);
-          dj = fmaf(dj, sci, dj);
-          if (NECK) {
-            const bool nk = in && dij < rbi + gp.z + 6.8f;
-            if (__any_sync(kFull, nk)) {
-              const int nkj = (sm_par[w][j] >> 16) & 0xff;
-              const float a = neck_deriv(dij, s_npos[nki * 21 + nkj], s_nval[nki * 21 + nkj], t.neck_scale);
-              const float b = neck_deriv(dij, s_npos[nkj * 21 + nki], s_nval[nkj * 21 + nki], t.neck_scale);
-              di += nk ? a : 0.0f;
-              dj += nk ? b : 0.0f;
-            }
-          }
-          const float gg = in ? fmaf(sdai, di, l.w * dj) : 0.0f;
-          fix = fmaf(-gg, dx, fix);
-          fiy = fmaf(-gg, dy, fiy);
-          fiz = fmaf(-gg, dz, fiz);
-          ax[s] = gg * dx;
-          ay[s] = gg * dy;
-          az[s] = gg * dz;
-        }
-        jx += reduce_to_lane(ax, g, lane);
-        jy += reduce_to_lane(ay, g, lane);
-        jz += reduce_to_lane(az, g, lane);
-      }
-      fx64 += to_fixed(fix, FS);
-      fy64 += to_fixed(fiy, FS);
-      fz64 += to_fixed(fiz, FS);
-      if (mycol) {
-        atomic_add_ll(&t.acc_fx[sj], to_fixed(jx, FS));
-        atomic_add_ll(&t.acc_fy[sj], to_fixed(jy, FS));
-        atomic_add_ll(&t.acc_fz[sj], to_fixed(jz, FS));
-      }
-      __syncwarp();
+      if (nr) near_chunk(k);
+      else far_chunk(k);
     }
   }
   if (cur_I >= 0) flush_i();

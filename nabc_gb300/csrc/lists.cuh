@@ -10,16 +10,20 @@
 // j-atoms instead of whole 32-atom tiles keeps ~50-60% of the lane-steps
 // busy at protein densities, against ~20-35% for tile pairs.
 //
-// Two lists share one build:
+// Three lists share one build:
 //   list A, pairs with r < cut: pass 2 (GB + Coulomb + LJ) -- exactly the
 //           reference's list, rebuilt every nsnb evaluations;
-//   list B, the pairs of list A with r < rgbmax + Fsmax + skin: passes 1
-//           and 3 (Born radii and chain rule), which the reference runs
-//           over list A skipping pairs beyond rgbmax + Fsmax at every
-//           evaluation.  List B is rebuilt from list A (on the device, with
-//           no host round trip) as soon as any atom has moved more than
-//           0.45 skin since list B was made, so every pair of list A that
-//           is within rgbmax + Fsmax now is on list B.
+//   lists B and C, the pairs of list A with r < rgbmax + Fsmax + skin:
+//           passes 1 and 3 (Born radii and chain rule), which the reference
+//           runs over list A skipping pairs beyond rgbmax + Fsmax at every
+//           evaluation.  List C holds the pairs close enough to need the
+//           near-field forms of the descreening integral (r < 4 max(s_i,
+//           s_j) + skin), list B all others, so the main kernels of passes 1
+//           and 3 carry no near-field code.  Lists B and C are remade from
+//           list A (on the device, with no host round trip) as soon as any
+//           atom has moved more than 0.45 skin since they were made, so
+//           every pair of list A within rgbmax + Fsmax now is on B or C,
+//           and no pair of list B has come within 4 max(s_i, s_j).
 //
 // Build stages (one launch each):
 //   1 candidates   warp per i-tile: tile pairs (I, J >= I) whose bounding
@@ -31,19 +35,21 @@
 //   4 scan         one block: first chunk of every i-tile, chunk totals
 //   5 fill         warp per candidate: the entries
 //   6 pad          warp per i-tile: padding entries and chunk owners
-// Stages 2-6 also run in "list B only" mode when the displacement check
-// fires; each of those launches returns at once unless the flag is set.
+// Stages 2-6 also run in "lists B and C only" mode when the displacement
+// check (in k_pack) fires; each of those launches returns at once unless
+// the flag is set.
 #pragma once
 
 #include "kernels.cuh"
 
 namespace sffg {
 
-constexpr float kListSkin = 0.6f;  // list B margin beyond rgbmax + Fsmax, in Angstrom
+constexpr float kListSkin = 0.6f;  // margin of lists B and C, in Angstrom
 
 struct ListArgs {
   const float4 *pos_hi, *pos_lo, *box_lo, *box_hi;
   const double *x;
+  const float4 *gbpar;  // per slot: .y = screened radius s
   const int *slot_atom, *param;
   const unsigned *tile_valid;
   const int *tile_sys, *sys_tile_end, *sys_active;
@@ -59,19 +65,21 @@ struct ListArgs {
   int cand_cap;
   int *ncand, *overflow;
   int *cand_start, *cand_count;  // per i-tile
-  unsigned *colA, *colB, *colE;  // per candidate x 32 lanes
-  int2 *cand_n;                  // entries of (A, B) per candidate
-  int2 *cand_off;                // their offsets within the i-tile
-  int *chunksA, *chunksB;        // per i-tile
-  int *chunk0A, *chunk0B;        // first chunk of each i-tile
-  int *nchunkA, *nchunkB;
+  unsigned *colA, *colB, *colC, *colE;  // per candidate x 32 lanes
+  int4 *cand_n;                  // entries of (A, B, C) per candidate
+  int4 *cand_off;                // their offsets within the i-tile
+  int *chunksA, *chunksB, *chunksC;  // per i-tile
+  int *chunk0A, *chunk0B, *chunk0C;  // first chunk of each i-tile
+  int *nchunkA, *nchunkB, *nchunkC;
   // the lists
   int *chunkA_i, *entA_slot;
   unsigned *entA_col, *entA_exc;
   int *chunkB_i, *entB_slot;
   unsigned *entB_col;
-  // list-B rebuild flag (set by the displacement check) and the positions
-  // list B was made from
+  int *chunkC_i, *entC_slot;
+  unsigned *entC_col;
+  // rebuild flag of lists B and C (set by the displacement check) and the
+  // positions they were made from
   int *flagB;
   float4 *xb;
 };
@@ -131,13 +139,16 @@ __global__ void k_list_candidates(const ListArgs a) {
 // list A: r^2 < cut^2, decided in FP64 from the double coordinates when
 // the FP32 distance is within 1e-5 of the cutoff, as the reference decides
 // (nblist.c:726-746); upper triangle within a tile; no pair of two frozen
-// atoms.  list B: list A pairs with r^2 < (rgbmax + Fsmax + skin)^2.
-// B_ONLY: list A stays as built; list B is remade from its columns.
-template <bool B_ONLY>
+// atoms.  Lists B and C: list A pairs with r^2 < (rgbmax + Fsmax + skin)^2,
+// on C when r < 4 max(s_i, s_j) + skin, else on B.
+// GB_ONLY: list A stays as built; lists B and C are remade from its
+// columns.
+template <bool GB_ONLY>
 __global__ void k_list_columns(const ListArgs a) {
   __shared__ float4 s_hi[8][32], s_lo[8][32];
+  __shared__ float s_s[8][32];
   __shared__ int s_atom[8][32];
-  if (B_ONLY && !*a.flagB) return;
+  if (GB_ONLY && !*a.flagB) return;
   const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
   const int ncand = *a.ncand, nwarps = (gridDim.x * blockDim.x) >> 5;
   for (int c = (blockIdx.x * blockDim.x + threadIdx.x) >> 5; c < ncand; c += nwarps) {
@@ -147,22 +158,24 @@ __global__ void k_list_columns(const ListArgs a) {
   s_hi[w][lane] = a.pos_hi[si];
   s_lo[w][lane] = a.pos_lo[si];
   s_atom[w][lane] = a.slot_atom[si];
+  s_s[w][lane] = a.gbpar[si].y;
   const unsigned vI = a.tile_valid[I];
   const unsigned frzI = __ballot_sync(kFull, (a.param[si] >> 24) & 1);
   const float4 hj = a.pos_hi[sj], lj = a.pos_lo[sj];
   const bool vj = (a.tile_valid[J] >> lane) & 1u;
   const bool frzj = (a.param[sj] >> 24) & 1;
   const int aj = a.slot_atom[sj];
+  const float sjs = a.gbpar[sj].y;
   int ex = -1;
-  if (!B_ONLY)
+  if (!GB_ONLY)
     for (int e = a.excl_tile_start[I]; e < a.excl_tile_start[I + 1]; e++)
       if (a.excl_tile_j[e] == J) {
         ex = a.excl_tile_idx[e];
         break;
       }
   __syncwarp();
-  const unsigned prevA = B_ONLY ? a.colA[static_cast<size_t>(c) * 32 + lane] : 0u;
-  unsigned colA = 0, colB = 0, colE = 0;
+  const unsigned prevA = GB_ONLY ? a.colA[static_cast<size_t>(c) * 32 + lane] : 0u;
+  unsigned colA = 0, colB = 0, colC = 0, colE = 0;
   const float gbb = a.gbb2f * 1.0001f + 1e-3f;
   for (int i = 0; i < 32; i++) {
     if (!((vI >> i) & 1u)) continue;  // warp-uniform
@@ -172,7 +185,7 @@ __global__ void k_list_columns(const ListArgs a) {
     const float dz = (hi.z - hj.z) + (li.z - lj.z);
     const float r2 = dx * dx + dy * dy + dz * dz;
     bool in;
-    if (B_ONLY) {
+    if (GB_ONLY) {
       in = (prevA >> i) & 1u;
     } else {
       if (!vj) {
@@ -190,106 +203,121 @@ __global__ void k_list_columns(const ListArgs a) {
       in = in && vj && !(I == J && i >= lane) && !(((frzI >> i) & 1u) && frzj);
       if (ex >= 0) colE |= ((a.excl_masks[static_cast<size_t>(ex) * 32 + i] >> lane) & 1u) << i;
     }
+    const float nr = 4.0f * fmaxf(s_s[w][i], sjs) + kListSkin;
+    const bool gb = in && r2 < gbb, near = r2 < nr * nr * 1.0001f;
     colA |= static_cast<unsigned>(in) << i;
-    colB |= static_cast<unsigned>(in && r2 < gbb) << i;
+    colB |= static_cast<unsigned>(gb && !near) << i;
+    colC |= static_cast<unsigned>(gb && near) << i;
   }
   const size_t e = static_cast<size_t>(c) * 32 + lane;
-  if (!B_ONLY) {
+  if (!GB_ONLY) {
     a.colA[e] = colA;
     a.colE[e] = colE;
   }
   a.colB[e] = colB;
+  a.colC[e] = colC;
   const int nA = __popc(__ballot_sync(kFull, colA != 0u)), nB = __popc(__ballot_sync(kFull, colB != 0u));
-  if (lane == 0) a.cand_n[c] = make_int2(nA, nB);
+  const int nC = __popc(__ballot_sync(kFull, colC != 0u));
+  if (lane == 0) a.cand_n[c] = make_int4(nA, nB, nC, 0);
   __syncwarp();  // the staged i-tile is rewritten by the next candidate
   }
 }
 
 // ---- stage 3 -------------------------------------------------------------
-template <bool B_ONLY>
+template <bool GB_ONLY>
 __global__ void k_list_offsets(const ListArgs a) {
-  if (B_ONLY && !*a.flagB) return;
+  if (GB_ONLY && !*a.flagB) return;
   const int lane = threadIdx.x & 31;
   const int I = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
   if (I >= a.ntile) return;
   const int c0 = a.cand_start[I], n = a.cand_count[I];
-  int runA = 0, runB = 0;
+  int runA = 0, runB = 0, runC = 0;
   for (int k0 = 0; k0 < n; k0 += 32) {
     const int k = k0 + lane;
-    int2 v = k < n ? a.cand_n[c0 + k] : make_int2(0, 0);
-    int sA = v.x, sB = v.y;  // inclusive warp scan
+    const int4 v = k < n ? a.cand_n[c0 + k] : make_int4(0, 0, 0, 0);
+    int sA = v.x, sB = v.y, sC = v.z;  // inclusive warp scans
 #pragma unroll
     for (int o = 1; o < 32; o <<= 1) {
-      const int tA = __shfl_up_sync(kFull, sA, o), tB = __shfl_up_sync(kFull, sB, o);
+      const int tA = __shfl_up_sync(kFull, sA, o), tB = __shfl_up_sync(kFull, sB, o),
+                tC = __shfl_up_sync(kFull, sC, o);
       if (lane >= o) {
         sA += tA;
         sB += tB;
+        sC += tC;
       }
     }
     if (k < n) {
-      int2 off = make_int2(runA + sA - v.x, runB + sB - v.y);
-      if (B_ONLY) off.x = a.cand_off[c0 + k].x;
+      int4 off = make_int4(runA + sA - v.x, runB + sB - v.y, runC + sC - v.z, 0);
+      if (GB_ONLY) off.x = a.cand_off[c0 + k].x;
       a.cand_off[c0 + k] = off;
     }
     runA += __shfl_sync(kFull, sA, 31);
     runB += __shfl_sync(kFull, sB, 31);
+    runC += __shfl_sync(kFull, sC, 31);
   }
   if (lane == 0) {
-    if (!B_ONLY) a.chunksA[I] = (runA + 31) >> 5;
+    if (!GB_ONLY) a.chunksA[I] = (runA + 31) >> 5;
     a.chunksB[I] = (runB + 31) >> 5;
+    a.chunksC[I] = (runC + 31) >> 5;
   }
 }
 
 // ---- stage 4 -------------------------------------------------------------
 // Exclusive scan of chunks per i-tile, one block of 1024 threads.
-template <bool B_ONLY>
+template <bool GB_ONLY>
 __global__ void __launch_bounds__(1024) k_list_scan(const ListArgs a) {
-  __shared__ int s_a[1024], s_b[1024];
-  if (B_ONLY && !*a.flagB) return;
+  __shared__ int s_a[1024], s_b[1024], s_c[1024];
+  if (GB_ONLY && !*a.flagB) return;
   const int t = threadIdx.x, n = a.ntile;
   const int per = (n + 1023) / 1024, lo = min(n, t * per), hi = min(n, lo + per);
-  int sa = 0, sb = 0;
+  int sa = 0, sb = 0, sc = 0;
   for (int i = lo; i < hi; i++) {
-    if (!B_ONLY) sa += a.chunksA[i];
+    if (!GB_ONLY) sa += a.chunksA[i];
     sb += a.chunksB[i];
+    sc += a.chunksC[i];
   }
   s_a[t] = sa;
   s_b[t] = sb;
+  s_c[t] = sc;
   __syncthreads();
   for (int o = 1; o < 1024; o <<= 1) {  // inclusive Hillis-Steele scan
-    const int va = t >= o ? s_a[t - o] : 0, vb = t >= o ? s_b[t - o] : 0;
+    const int va = t >= o ? s_a[t - o] : 0, vb = t >= o ? s_b[t - o] : 0, vc = t >= o ? s_c[t - o] : 0;
     __syncthreads();
     s_a[t] += va;
     s_b[t] += vb;
+    s_c[t] += vc;
     __syncthreads();
   }
-  int ra = s_a[t] - sa, rb = s_b[t] - sb;
+  int ra = s_a[t] - sa, rb = s_b[t] - sb, rc = s_c[t] - sc;
   for (int i = lo; i < hi; i++) {
-    if (!B_ONLY) {
+    if (!GB_ONLY) {
       a.chunk0A[i] = ra;
       ra += a.chunksA[i];
     }
     a.chunk0B[i] = rb;
     rb += a.chunksB[i];
+    a.chunk0C[i] = rc;
+    rc += a.chunksC[i];
   }
   if (t == 1023) {
-    if (!B_ONLY) *a.nchunkA = s_a[1023];
+    if (!GB_ONLY) *a.nchunkA = s_a[1023];
     *a.nchunkB = s_b[1023];
+    *a.nchunkC = s_c[1023];
   }
 }
 
 // ---- stage 5 -------------------------------------------------------------
-template <bool B_ONLY>
+template <bool GB_ONLY>
 __global__ void k_list_fill(const ListArgs a) {
-  if (B_ONLY && !*a.flagB) return;
+  if (GB_ONLY && !*a.flagB) return;
   const int lane = threadIdx.x & 31;
   const int ncand = *a.ncand, nwarps = (gridDim.x * blockDim.x) >> 5;
   for (int c = (blockIdx.x * blockDim.x + threadIdx.x) >> 5; c < ncand; c += nwarps) {
   const int2 p = a.cand[c];
-  const int2 off = a.cand_off[c];
+  const int4 off = a.cand_off[c];
   const size_t e = static_cast<size_t>(c) * 32 + lane;
   const unsigned lt = (1u << lane) - 1u;
-  if (!B_ONLY) {
+  if (!GB_ONLY) {
     const unsigned col = a.colA[e];
     const unsigned bal = __ballot_sync(kFull, col != 0u);
     if (col) {
@@ -299,12 +327,23 @@ __global__ void k_list_fill(const ListArgs a) {
       a.entA_exc[pos] = a.colE[e];
     }
   }
-  const unsigned col = a.colB[e];
-  const unsigned bal = __ballot_sync(kFull, col != 0u);
-  if (col) {
-    const size_t pos = static_cast<size_t>(a.chunk0B[p.x]) * 32 + off.y + __popc(bal & lt);
-    a.entB_slot[pos] = p.y * 32 + lane;
-    a.entB_col[pos] = col;
+  {
+    const unsigned col = a.colB[e];
+    const unsigned bal = __ballot_sync(kFull, col != 0u);
+    if (col) {
+      const size_t pos = static_cast<size_t>(a.chunk0B[p.x]) * 32 + off.y + __popc(bal & lt);
+      a.entB_slot[pos] = p.y * 32 + lane;
+      a.entB_col[pos] = col;
+    }
+  }
+  {
+    const unsigned col = a.colC[e];
+    const unsigned bal = __ballot_sync(kFull, col != 0u);
+    if (col) {
+      const size_t pos = static_cast<size_t>(a.chunk0C[p.x]) * 32 + off.z + __popc(bal & lt);
+      a.entC_slot[pos] = p.y * 32 + lane;
+      a.entC_col[pos] = col;
+    }
   }
   }
 }
@@ -313,36 +352,36 @@ __global__ void k_list_fill(const ListArgs a) {
 // Padding entries after each i-tile's last entry, and the owner of every
 // chunk.  A padding entry points at the i-tile's own first slot with an
 // empty column, so the passes load harmless data for it.
-template <bool B_ONLY>
+template <bool GB_ONLY>
 __global__ void k_list_pad(const ListArgs a) {
-  if (B_ONLY && !*a.flagB) return;
+  if (GB_ONLY && !*a.flagB) return;
   const int lane = threadIdx.x & 31;
   const int I = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
   if (I >= a.ntile) return;
   const int c0 = a.cand_start[I], n = a.cand_count[I];
-  int totA = 0, totB = 0;
+  int tot[3] = {0, 0, 0};
   if (n > 0) {
-    const int2 lo = a.cand_off[c0 + n - 1], ln = a.cand_n[c0 + n - 1];
-    totA = lo.x + ln.x;
-    totB = lo.y + ln.y;
+    const int4 lo = a.cand_off[c0 + n - 1], ln = a.cand_n[c0 + n - 1];
+    tot[0] = lo.x + ln.x;
+    tot[1] = lo.y + ln.y;
+    tot[2] = lo.z + ln.z;
   }
-  for (int list = B_ONLY ? 1 : 0; list < 2; list++) {
-    const int tot = list ? totB : totA;
-    const int ch0 = list ? a.chunk0B[I] : a.chunk0A[I];
-    const int nch = list ? a.chunksB[I] : a.chunksA[I];
-    int *slot = list ? a.entB_slot : a.entA_slot;
-    unsigned *col = list ? a.entB_col : a.entA_col;
-    int *owner = list ? a.chunkB_i : a.chunkA_i;
+  for (int list = GB_ONLY ? 1 : 0; list < 3; list++) {
+    const int ch0 = list == 0 ? a.chunk0A[I] : list == 1 ? a.chunk0B[I] : a.chunk0C[I];
+    const int nch = list == 0 ? a.chunksA[I] : list == 1 ? a.chunksB[I] : a.chunksC[I];
+    int *slot = list == 0 ? a.entA_slot : list == 1 ? a.entB_slot : a.entC_slot;
+    unsigned *col = list == 0 ? a.entA_col : list == 1 ? a.entB_col : a.entC_col;
+    int *owner = list == 0 ? a.chunkA_i : list == 1 ? a.chunkB_i : a.chunkC_i;
     const int end = nch * 32;
-    for (int k = tot + lane; k < end; k += 32) {
+    for (int k = tot[list] + lane; k < end; k += 32) {
       const size_t pos = static_cast<size_t>(ch0) * 32 + k;
       slot[pos] = I * 32;
       col[pos] = 0u;
-      if (!list) a.entA_exc[pos] = 0u;
+      if (list == 0) a.entA_exc[pos] = 0u;
     }
     for (int k = lane; k < nch; k += 32) owner[ch0 + k] = I;
   }
-  // list B now reflects the current positions
+  // lists B and C now reflect the current positions
   a.xb[I * 32 + lane] = a.pos_hi[I * 32 + lane];
 }
 
