@@ -875,7 +875,7 @@ int Batch::run_eval(bool rebuild, void *stream) {
   }
   {
     DevTables t = make_tables(d, mp_, fsmax, 5);
-    launch_born(neck, d.grid_pair, st, t);
+    launch_born(neck, d.nsm, st, t);
     SFFG_CK(cudaGetLastError());
   }
   if (profile_) SFFG_CK(cudaEventRecord(d.events[ring][0][1], st));
@@ -921,7 +921,7 @@ int Batch::run_eval(bool rebuild, void *stream) {
   if (profile_) SFFG_CK(cudaEventRecord(d.events[ring][2][0], st));
   {
     DevTables t = make_tables(d, mp_, fsmax, 7);
-    launch_chain(neck, d.grid_pair, st, t);
+    launch_chain(neck, d.nsm, st, t);
     SFFG_CK(cudaGetLastError());
   }
   if (profile_) {

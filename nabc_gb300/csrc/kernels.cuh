@@ -66,28 +66,36 @@ __device__ __forceinline__ long long to_fixed(float v, float scale) {
 }
 
 // Steps per group of the pair loops: j-side partial sums are kept in
-// registers for kGroup steps, then folded across the warp.  Fewer steps per
-// group keep the unrolled loop body (and the instruction-cache footprint)
-// small at the cost of more shuffles per step.
-#ifndef SFFG_GROUP
-#define SFFG_GROUP 4
+// registers for a group of steps, then folded across the warp.  Fewer steps
+// per group keep the unrolled loop body (and the instruction-cache
+// footprint) small at the cost of more shuffles per step; measured best:
+// 4 for passes 1 and 3, 8 for pass 2.
+#ifndef SFFG_GROUP_BORN
+#define SFFG_GROUP_BORN 4
 #endif
-constexpr int kGroup = SFFG_GROUP;
-constexpr int kGroupLog2 = kGroup == 8 ? 3 : kGroup == 4 ? 2 : 1;
-static_assert(kGroup == 2 || kGroup == 4 || kGroup == 8, "group of 2, 4 or 8 steps");
+#ifndef SFFG_GROUP_PAIR
+#define SFFG_GROUP_PAIR 8
+#endif
+constexpr int kGroup = SFFG_GROUP_BORN;
+constexpr int kGroupPair = SFFG_GROUP_PAIR;
+
+constexpr int ilog2(int k) { return k == 8 ? 3 : k == 4 ? 2 : k == 2 ? 1 : 0; }
 
 // Sum of v[e] over the 32 lanes for e = 0..K-1, delivered to lane K*g + e
 // (zero in the other lanes): log2(K) transposing shuffle stages (each lane
 // keeps half of its values and sends the other half across), then a plain
 // butterfly over the remaining lane bits.  After the transposing stages
 // lane L holds element L >> (5 - log2 K).
-__device__ __forceinline__ float reduce_to_lane(const float (&v)[kGroup], int g, int lane) {
-  float a[kGroup];
+template <int K>
+__device__ __forceinline__ float reduce_to_lane(const float (&v)[K], int g, int lane) {
+  static_assert(K == 2 || K == 4 || K == 8, "group of 2, 4 or 8 steps");
+  constexpr int kLog2 = ilog2(K);
+  float a[K];
 #pragma unroll
-  for (int k = 0; k < kGroup; k++) a[k] = v[k];
-  int m = kGroup, dist = 16;
+  for (int k = 0; k < K; k++) a[k] = v[k];
+  int m = K, dist = 16;
 #pragma unroll
-  for (int st = 0; st < kGroupLog2; st++) {
+  for (int st = 0; st < kLog2; st++) {
     const bool b = lane & dist;
     m >>= 1;
 #pragma unroll
@@ -100,9 +108,9 @@ __device__ __forceinline__ float reduce_to_lane(const float (&v)[kGroup], int g,
   }
   float c = a[0];
 #pragma unroll
-  for (int d = 16 >> kGroupLog2; d > 0; d >>= 1) c += __shfl_xor_sync(kFull, c, d);
-  const float r = __shfl_sync(kFull, c, (lane & (kGroup - 1)) << (5 - kGroupLog2));
-  return (lane >> kGroupLog2) == g ? r : 0.0f;
+  for (int d = 16 >> kLog2; d > 0; d >>= 1) c += __shfl_xor_sync(kFull, c, d);
+  const float r = __shfl_sync(kFull, c, (lane & (K - 1)) << (5 - kLog2));
+  return (lane >> kLog2) == g ? r : 0.0f;
 }
 
 __device__ __forceinline__ long long warp_sum_ll(long long v) {
@@ -234,7 +242,7 @@ __device__ __forceinline__ int near_stage(const DevTables &t, int k, int lane, f
 // Born-radius descreening sums (src/sff/eff.c:1566-1709): both directions
 // of every pair within rgbmax + Fsmax, over lists B and C.
 template <bool NECK>
-__global__ void __launch_bounds__(256, 2) k_born(const DevTables t) {
+__global__ void __launch_bounds__(256, 3) k_born(const DevTables t) {
   __shared__ float4 sm_hi[8][32], sm_lo[8][32], sm_gb[8][32];  // j entries of the chunk
   __shared__ float4 si_hi[8][32], si_lo[8][32], si_gb[8][32];  // the i-tile
   __shared__ unsigned sm_col[8][32];
@@ -458,11 +466,11 @@ __global__ void __launch_bounds__(256, 2) k_gbpair(const DevTables t) {
       float fix = 0, fiy = 0, fiz = 0, sdi = 0, ep = 0, ee = 0, ev = 0;
       float jx = 0, jy = 0, jz = 0, jsd = 0;
 #pragma unroll 1
-      for (int g = 0; g < 32 / kGroup; g++) {
-        float ax[kGroup], ay[kGroup], az[kGroup], as[kGroup];
+      for (int g = 0; g < 32 / kGroupPair; g++) {
+        float ax[kGroupPair], ay[kGroupPair], az[kGroupPair], as[kGroupPair];
 #pragma unroll
-        for (int s = 0; s < kGroup; s++) {
-          const int j = g * kGroup + s;
+        for (int s = 0; s < kGroupPair; s++) {
+          const int j = g * kGroupPair + s;
           ax[s] = ay[s] = az[s] = as[s] = 0.0f;
           if (!((cols >> j) & 1u)) continue;  // padding entry
           const float4 h = sm_hi[w][j], l = sm_lo[w][j];
@@ -518,7 +526,7 @@ __global__ void __launch_bounds__(256, 2) k_gbpair(const DevTables t) {
 // and C: for each pair within rgbmax + Fsmax, g = sumda_i d_ij +
 // sumda_j d_ji, f_i -= g r_ij, f_j += g r_ij.
 template <bool NECK>
-__global__ void __launch_bounds__(256, 2) k_chain(const DevTables t) {
+__global__ void __launch_bounds__(256, 3) k_chain(const DevTables t) {
   __shared__ float4 sm_hi[8][32], sm_lo[8][32], sm_gb[8][32];  // j entries (lo.w = sumda)
   __shared__ float4 si_hi[8][32], si_lo[8][32], si_gb[8][32];  // the i-tile (lo.w = sumda)
   __shared__ unsigned sm_col[8][32];

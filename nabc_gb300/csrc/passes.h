@@ -8,9 +8,11 @@
 
 namespace sffg {
 
-void launch_born(bool neck, int grid, cudaStream_t st, const DevTables &t);
+// Passes 1 and 3 size their persistent grids from the occupancy of the
+// kernel launched (nsm: multiprocessors of the device).
+void launch_born(bool neck, int nsm, cudaStream_t st, const DevTables &t);
 void launch_gbpair(bool kappa, int grid, cudaStream_t st, const DevTables &t);
-void launch_chain(bool neck, int grid, cudaStream_t st, const DevTables &t);
+void launch_chain(bool neck, int nsm, cudaStream_t st, const DevTables &t);
 // Resident 256-thread blocks per SM of the pair kernels.
 int pair_blocks_per_sm();
 
