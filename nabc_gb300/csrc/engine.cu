@@ -86,6 +86,12 @@ struct DeviceState {
   DBuf<unsigned> entA_col, entA_exc, entB_col, entC_col;
   DBuf<float4> xb;
   DBuf<int> counters;
+  DBuf<unsigned> step;  // md step number (the Philox counter of the noise)
+  // CUDA graphs of an evaluation and of an md step without a list rebuild,
+  // with the list-buffer pointers they were captured against
+  cudaGraphExec_t g_eval = nullptr, g_step = nullptr;
+  std::vector<const void *> sig_eval, sig_step;
+  long long launches_eval = 0, launches_step = 0;
   // model tables
   DBuf<float> neck_pos, neck_val;
   // dynamics
@@ -103,6 +109,8 @@ struct DeviceState {
   long long timed_evals = 0;
 
   ~DeviceState() {
+    if (g_eval) cudaGraphExecDestroy(g_eval);
+    if (g_step) cudaGraphExecDestroy(g_step);
     for (auto &ring : events)
       for (auto &pe : ring)
         for (auto &e : pe)
@@ -123,7 +131,7 @@ struct DeviceState {
     rel(cand_start); rel(cand_count); rel(chunksA); rel(chunksB); rel(chunksC); rel(chunk0A);
     rel(chunk0B); rel(chunk0C); rel(chunkA_i); rel(entA_slot); rel(chunkB_i); rel(entB_slot);
     rel(chunkC_i); rel(entC_slot); rel(entA_col); rel(entA_exc); rel(entB_col); rel(entC_col);
-    rel(xb); rel(counters); rel(neck_pos); rel(neck_val); rel(tscal);
+    rel(xb); rel(counters); rel(step); rel(neck_pos); rel(neck_val); rel(tscal);
     rel(noise); rel(rndf); rel(ekin); rel(cg_w); rel(cg_state);
   }
 };
@@ -464,6 +472,8 @@ int Batch::upload() {
   SFFG_CK(d.chunk0C.alloc(ntile_));
   SFFG_CK(d.xb.alloc(nslot_));
   SFFG_CK(d.counters.alloc(16));
+  SFFG_CK(d.step.alloc(1));
+  SFFG_CK(cudaMemset(d.step.p, 0, sizeof(unsigned)));
   SFFG_CK(cudaMemset(d.counters.p, 0, d.counters.bytes()));
   SFFG_CK(d.tscal.alloc(nsys));
   SFFG_CK(d.ekin.alloc(nsys));
@@ -810,9 +820,8 @@ int Batch::build_lists(void *stream) {
 void Batch::rebuild_list_b(void *stream) {
   DeviceState &d = *d_;
   cudaStream_t st = pick(d, stream);
-  const size_t nc = std::max(1, ncand_);
   const int tile_blocks = (ntile_ * 32 + 255) / 256;
-  const int cand_blocks = static_cast<int>(std::min<long long>((static_cast<long long>(nc) * 32 + 255) / 256, 16LL * d.nsm));
+  const int cand_blocks = 16 * d.nsm;  // grid-stride over the candidates (fixed, for graph capture)
   const ListArgs a = list_args(fsmax_all());
   k_list_columns<true><<<cand_blocks, 256, 0, st>>>(a);
   k_list_offsets<true><<<tile_blocks, 256, 0, st>>>(a);
@@ -831,7 +840,69 @@ int Batch::eval(bool rebuild, void *stream) {
   return run_eval(rebuild || !have_list_, stream);
 }
 
+// The list buffers a captured graph depends on (they move when a list
+// outgrows its store).
+std::vector<const void *> Batch::list_sig() const {
+  const DeviceState &d = *d_;
+  return {d.cand.p, d.cand_n.p, d.cand_off.p, d.colA.p, d.colB.p, d.colC.p, d.colE.p, d.chunkA_i.p, d.entA_slot.p,
+          d.entA_col.p, d.entA_exc.p, d.chunkB_i.p, d.entB_slot.p, d.entB_col.p, d.chunkC_i.p, d.entC_slot.p,
+          d.entC_col.p};
+}
+
+bool Batch::graphs_ok() const { return opts_.sffg_graph && !profile_ && have_list_; }
+
+// Captures body() (launches on the batch's private stream) into exec,
+// recording how many kernels one replay launches.
+int Batch::capture(cudaGraphExec_t &exec, std::vector<const void *> &sig, long long &nlaunch,
+                   const std::function<int(cudaStream_t)> &body) {
+  DeviceState &d = *d_;
+  if (exec && sig == list_sig()) return SFFG_OK;
+  if (exec) {
+    cudaGraphExecDestroy(exec);
+    exec = nullptr;
+  }
+  const long long l0 = launches_;
+  const long long e0 = timers().nevals;
+  cudaGraph_t g = nullptr;
+  SFFG_CK(cudaStreamBeginCapture(d.stream, cudaStreamCaptureModeThreadLocal));
+  const int rc = body(d.stream);
+  const cudaError_t ec = cudaStreamEndCapture(d.stream, &g);
+  nlaunch = launches_ - l0;
+  launches_ = l0;
+  timers().nevals = e0;
+  if (rc != SFFG_OK || ec != cudaSuccess) {
+    if (g) cudaGraphDestroy(g);
+    if (rc != SFFG_OK) return rc;
+    last_error = std::string("graph capture: ") + cudaGetErrorString(ec);
+    return SFFG_ECUDA;
+  }
+  const cudaError_t ei = cudaGraphInstantiate(&exec, g, 0);
+  cudaGraphDestroy(g);
+  if (ei != cudaSuccess) {
+    exec = nullptr;
+    last_error = std::string("graph instantiate: ") + cudaGetErrorString(ei);
+    return SFFG_ECUDA;
+  }
+  sig = list_sig();
+  return SFFG_OK;
+}
+
+// One evaluation; without a list rebuild it replays a captured graph (one
+// launch instead of ~20) unless graphs are off or pass timing is on.
 int Batch::run_eval(bool rebuild, void *stream) {
+  DeviceState &d = *d_;
+  cudaStream_t st = pick(d, stream);
+  if (rebuild || !graphs_ok()) return run_eval_direct(rebuild, st);
+  int rc = capture(d.g_eval, d.sig_eval, d.launches_eval,
+                   [&](cudaStream_t cs) { return run_eval_direct(false, cs); });
+  if (rc) return rc;
+  SFFG_CK(cudaGraphLaunch(d.g_eval, st));
+  launches_ += d.launches_eval;
+  timers().nevals++;
+  return SFFG_OK;
+}
+
+int Batch::run_eval_direct(bool rebuild, void *stream) {
   DeviceState &d = *d_;
   cudaStream_t st = pick(d, stream);
   const int nsys = num_systems();
@@ -1008,9 +1079,12 @@ int Batch::kernel_times(double ms[3], long long *nevals) {
 
 // ------------------------------------------------------------------ md
 
+// End of an md step: kinetic energy, the Berendsen factor of the next step
+// (apply) and the Philox step counter.
 __global__ void k_md_tscal(const long long *ekin, double *tscal, double *ekin_out, int nsys, double ekin0_per_dof,
-                           const double *rndf, double dttp, double c_ave_factor, int apply) {
+                           const double *rndf, double dttp, double c_ave_factor, int apply, unsigned *step) {
   const int s = blockIdx.x * blockDim.x + threadIdx.x;
+  if (s == 0) ++*step;
   if (s >= nsys) return;
   double ek = 0.5 * static_cast<double>(ekin[s]) * (1.0 / 4294967296.0) * c_ave_factor;
   if (ekin_out) ekin_out[s] = ek;
@@ -1044,7 +1118,7 @@ static void md_args(Batch &b, DeviceState &d, const Options &o, int natom_total,
   a.vlimit = o.vlimit;
   a.gammai = gammai;
   a.seed = o.sffg_seed;
-  a.step = 0;
+  a.step = d.step.p;
   c_ave = gammai > 0.0 ? 1.0 + gammai * dt5 : 1.0;
   (void)b;
 }
@@ -1088,6 +1162,7 @@ int Batch::md_begin(bool rebuild, NoiseFn noise, void *noise_ctx, void *stream) 
     a.noise = d.noise.p;
   }
   SFFG_CK(cudaMemsetAsync(d.ekin.p, 0, d.ekin.bytes(), st));
+  SFFG_CK(cudaMemsetAsync(d.step.p, 0, sizeof(unsigned), st));
   const int nb = (a.n3 + 255) / 256;
   k_md_kick<<<nb, 256, 0, st>>>(a, 1);
   SFFG_CK(cudaGetLastError());
@@ -1107,23 +1182,39 @@ int Batch::md_steps(int step0, int k, NoiseFn noise, void *noise_ctx, void *stre
   std::vector<double> h;
   const int nb = (a.n3 + 255) / 256;
   int rc = SFFG_OK;
-  for (int i = 1; i <= k; i++) {
-    const int nstep = step0 + i;
-    k_md_drift<<<nb, 256, 0, st>>>(a);
-    const bool rebuild = opts_.nsnb > 0 && nstep % opts_.nsnb == 0;
-    if ((rc = run_eval(rebuild, st))) break;
+  // the step counter holds the number of the next step
+  step_host_ = static_cast<unsigned>(step0 + 1);
+  SFFG_CK(cudaMemcpyAsync(d.step.p, &step_host_, sizeof(unsigned), cudaMemcpyHostToDevice, st));
+  // one step after the drift: evaluation, kick, kinetic energy, counter
+  auto step_body = [&](cudaStream_t s, bool rebuild, bool capturing) -> int {
+    k_md_drift<<<nb, 256, 0, s>>>(a);
+    int r = capturing ? run_eval_direct(false, s) : run_eval(rebuild, s);
+    if (r) return r;
     if (noise && a.gammai != 0.0) {
-      if ((rc = upload_noise(*this, d, noise, noise_ctx, st, h))) break;
+      if ((r = upload_noise(*this, d, noise, noise_ctx, s, h))) return r;
       a.noise = d.noise.p;
     }
-    a.step = static_cast<unsigned>(nstep);
-    SFFG_CK(cudaMemsetAsync(d.ekin.p, 0, d.ekin.bytes(), st));
-    k_md_kick<<<nb, 256, 0, st>>>(a, 0);
+    SFFG_CK(cudaMemsetAsync(d.ekin.p, 0, d.ekin.bytes(), s));
+    k_md_kick<<<nb, 256, 0, s>>>(a, 0);
+    k_md_tscal<<<(nsys + 127) / 128, 128, 0, s>>>(d.ekin.p, d.tscal.p, nullptr, nsys, boltz2 * opts_.temp0,
+                                                  d.rndf.p, opts_.dt / opts_.tautp, c_ave, a.gammai == 0.0,
+                                                  d.step.p);
     launches_ += 3;  // drift, kick, tscal
-    k_md_tscal<<<(nsys + 127) / 128, 128, 0, st>>>(d.ekin.p, d.tscal.p, nullptr, nsys,
-                                                   boltz2 * opts_.temp0, d.rndf.p, opts_.dt / opts_.tautp, c_ave,
-                                                   a.gammai == 0.0);
     SFFG_CK(cudaGetLastError());
+    return SFFG_OK;
+  };
+  for (int i = 1; i <= k; i++) {
+    const int nstep = step0 + i;
+    const bool rebuild = opts_.nsnb > 0 && nstep % opts_.nsnb == 0;
+    if (!rebuild && !noise && graphs_ok()) {
+      if ((rc = capture(d.g_step, d.sig_step, d.launches_step, [&](cudaStream_t cs) { return step_body(cs, false, true); })))
+        break;
+      SFFG_CK(cudaGraphLaunch(d.g_step, st));
+      launches_ += d.launches_step;
+      timers().nevals++;
+    } else if ((rc = step_body(st, rebuild, false))) {
+      break;
+    }
   }
   return rc;
 }

@@ -11,6 +11,8 @@
 // do not depend on the order in which tile pairs are processed.
 #pragma once
 
+#include <cuda_runtime_api.h>
+
 #include <functional>
 #include <memory>
 #include <string>
@@ -107,6 +109,11 @@ class Batch {
 
  private:
   int upload();
+  int run_eval_direct(bool rebuild, void *stream);
+  std::vector<const void *> list_sig() const;
+  bool graphs_ok() const;
+  int capture(cudaGraphExec_t &exec, std::vector<const void *> &sig, long long &nlaunch,
+              const std::function<int(cudaStream_t)> &body);
   int build_lists(void *stream);
   void rebuild_list_b(void *stream);
   ListArgs list_args(double fsmax);
@@ -119,6 +126,7 @@ class Batch {
   std::vector<HostSystem> host_;
   std::vector<std::vector<double>> x0_;
   int natom_total_ = 0, nslot_ = 0, ntile_ = 0;
+  unsigned step_host_ = 0;  // staging of the md step counter upload
   long long cand_max_ = 0;  // candidate tile pairs the batch could ever need
   int ncand_ = 0;           // candidates of the current pair list
   bool finalized_ = false, have_list_ = false, profile_ = false;

@@ -391,10 +391,12 @@ __device__ __forceinline__ uint4 philox4x32(uint4 c, uint2 k) {
   return c;
 }
 
+// Unit Gaussian from two uniform 32-bit words (Box-Muller, in FP32: the
+// Langevin noise needs no more, and FP64 transcendentals are slow here).
 __device__ __forceinline__ double normal_from(unsigned a, unsigned b) {
-  const double u1 = (static_cast<double>(a) + 1.0) * (1.0 / 4294967296.0);
-  const double u2 = static_cast<double>(b) * (1.0 / 4294967296.0);
-  return sqrt(-2.0 * log(u1)) * cospi(2.0 * u2);
+  const float u1 = (static_cast<float>(a >> 8) + 1.0f) * (1.0f / 16777216.0f);  // (0, 1]
+  const float u2 = static_cast<float>(b >> 8) * (1.0f / 16777216.0f);           // [0, 1)
+  return static_cast<double>(sqrtf(-2.0f * logf(u1)) * cospif(2.0f * u2));
 }
 
 struct MdArgs {
@@ -407,7 +409,7 @@ struct MdArgs {
   int n3;
   double dtx, dt5, c_explic, c_implic, sdfac, vlimit, gammai;
   unsigned long long seed;
-  unsigned step;
+  const unsigned *step;  // Philox counter: the step number (advanced by k_md_tscal)
 };
 
 // First half of a step (src/sff/sff.c:2243-2248): half-kick and drift.
@@ -447,7 +449,7 @@ __global__ void k_md_kick(const MdArgs a, int init) {
         if (a.noise) {
           z = a.noise[i];
         } else {
-          const uint4 r = philox4x32(make_uint4(static_cast<unsigned>(i), a.step, 0x51u, 0u),
+          const uint4 r = philox4x32(make_uint4(static_cast<unsigned>(i), *a.step, 0x51u, 0u),
                                      make_uint2(static_cast<unsigned>(a.seed), static_cast<unsigned>(a.seed >> 32)));
           z = normal_from(r.x, r.y);
         }
