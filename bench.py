@@ -97,6 +97,18 @@ class ClockSampler:
                 "reasons": reasons, "samples": len(self.rows)}
 
 
+def aggregate(total_ms, e2e_s, steps, e2e_steps, world, dist, device):
+    """Whole-job rates of independent replicas: each rank's timed region is
+    reduced with MAX over ranks (the job lasts as long as its slowest
+    replica) and the units of all ranks are counted."""
+    if dist is not None and world > 1:
+        import torch
+        t = torch.tensor([total_ms, e2e_s], dtype=torch.float64, device=device)
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        total_ms, e2e_s = float(t[0]), float(t[1])
+    return world * steps / (total_ms * 1e-3), world * e2e_steps / e2e_s, total_ms
+
+
 def count_pairs(x, cut, rcut_gb):
     """Unordered pairs within cut and within rgbmax + Fsmax (cell grid)."""
     from scipy.spatial import cKDTree
@@ -231,11 +243,6 @@ def main():
     torch.cuda.synchronize()
     pass_ms, nev = b.kernel_times()
     b.set_profiling(False)
-    if dist:
-        t = torch.tensor([total_ms], device="cuda")
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        total_ms = float(t.item())
-    value = world * args.steps / (total_ms * 1e-3)
 
     # e2e through the reference-facing C ABI with pinned host buffers
     L = sff.lib()
@@ -258,11 +265,7 @@ def main():
         t0 = time.perf_counter()
         L.mme(sff.dptr(xh), sff.dptr(fh), C.byref(it))
         e2e_s += time.perf_counter() - t0
-    e2e = e2e_steps / e2e_s
-    if dist:
-        t = torch.tensor([e2e_s], device="cuda", dtype=torch.float64)
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        e2e = world * e2e_steps / float(t.item())
+    value, e2e, total_ms = aggregate(total_ms, e2e_s, args.steps, e2e_steps, world, dist, "cuda")
 
     if rank != 0:
         dist.barrier() if dist else None
