@@ -109,6 +109,107 @@ def aggregate(total_ms, e2e_s, steps, e2e_steps, world, dist, device):
     return world * steps / (total_ms * 1e-3), world * e2e_steps / e2e_s, total_ms
 
 
+UNEVEN_OPTS = "gb=8, rgbmax=25.0, cut=30.0"   # GBneck2, the uneven-size batch
+CONFORMER_OPTS = "gb=5, cut=999.0"           # OBC II, all pairs, the conformer batch
+
+
+def make_molecules(sizes, seed0):
+    """Synthetic molecules of the given atom counts (seeds seed0 + k),
+    generated on all host cores."""
+    from concurrent.futures import ThreadPoolExecutor
+    from nabc_gb300 import sff
+    with ThreadPoolExecutor(os.cpu_count() or 1) as ex:
+        return list(ex.map(lambda k: sff.synth_molecule(int(sizes[k]), seed0 + k), range(len(sizes))))
+
+
+def timed(fn, reps, stream, flush):
+    """Device milliseconds of reps calls of fn, each bracketed by CUDA
+    events on stream, with L2 flushed between calls (outside the events)."""
+    import torch
+    ev = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(reps)]
+    for k in range(reps):
+        flush.zero_()
+        ev[k][0].record(stream)
+        fn()
+        ev[k][1].record(stream)
+    torch.cuda.synchronize()
+    return [a.elapsed_time(c) for a, c in ev]
+
+
+def bench_batched(args, stream, sp, flush):
+    """Batched versus plain evaluation on the GPU: many systems in one
+    flattened work queue (one Batch) against one Batch per system evaluated
+    one after another, same systems, same stream."""
+    import torch
+    from nabc_gb300 import sff
+    from nabc_gb300.batch import Batch
+    from oracle import oracle
+    out = {}
+
+    def compare(opts, systems, reps, label):
+        b = Batch(opts)
+        for prm, x in systems:
+            b.add(prm, x)
+        b.finalize()
+        b.eval(rebuild=True, stream=sp)
+        plain = []
+        for prm, x in systems:
+            p = Batch(opts)
+            p.add(prm, x)
+            p.finalize()
+            p.eval(rebuild=True, stream=sp)
+            plain.append(p)
+        torch.cuda.synchronize()
+        t_b = timed(lambda: b.eval(stream=sp), reps, stream, flush)
+        t_p = timed(lambda: [p.eval(stream=sp) for p in plain], reps, stream, flush)
+        n = len(systems)
+        ident = all(np.array_equal(b.energy(k), plain[k].energy(0)) for k in range(n))
+        res = {"systems": n, "atoms": int(sum(sff.natom(prm) for prm, _ in systems)), "options": opts,
+               "batched_evals_per_s": n * reps / (sum(t_b) * 1e-3),
+               "plain_evals_per_s": n * reps / (sum(t_p) * 1e-3),
+               "batched_ms_per_eval_of_all": float(np.median(t_b)), "plain_ms_per_loop_of_all": float(np.median(t_p)),
+               "same_bits_alone_and_batched": bool(ident)}
+        res["speedup"] = res["batched_evals_per_s"] / res["plain_evals_per_s"]
+        return b, plain, res
+
+    # uneven-size batch: log-uniform 200..20,000 atoms, each its own topology
+    rng = np.random.default_rng(4242)
+    sizes = np.floor(np.exp(rng.uniform(np.log(200), np.log(20000), args.uneven))).astype(int)
+    mols = make_molecules(sizes, 9000)
+    b, plain, res = compare(UNEVEN_OPTS, [(prm, x) for prm, x, _ in mols], 3, "uneven")
+    # accuracy of three of the smaller molecules against the FP64 oracle
+    errs = []
+    for k in np.argsort(sizes)[:: max(1, len(sizes) // 3)][:3]:
+        prm, x, _ = mols[k]
+        o = oracle.Oracle(prm, UNEVEN_OPTS)
+        e0, _, g0, _ = o.mme(x)
+        errs.append((abs(b.energy(int(k))[0] - e0) / abs(e0), float(np.sqrt(((b.grad(int(k)) - g0) ** 2).mean()))))
+    res["energy_rel_max"] = max(e for e, _ in errs)
+    res["force_rms_max"] = max(f for _, f in errs)
+    res["checked_vs_fp64"] = "3 molecules of the batch"
+    b.close()
+    for p in plain:
+        p.close()
+    out["uneven"] = res
+
+    # conformers: one 3,000-atom topology, base + N(0, 0.3^2) per coordinate
+    prm, x0, _ = sff.synth_molecule(3000, 777)
+    rng = np.random.default_rng(778)
+    confs = [(prm, x0 + rng.normal(0.0, 0.3, x0.shape)) for _ in range(args.conformers)]
+    b, plain, res = compare(CONFORMER_OPTS, confs, 3, "conformers")
+    for p in plain:
+        p.close()
+    t0 = time.perf_counter()
+    st, en = b.cg(args.cg_steps, 0.01, 1.0, stream=sp)
+    torch.cuda.synchronize()
+    res["cg_steps"] = args.cg_steps
+    res["cg_ms_per_step"] = (time.perf_counter() - t0) * 1e3 / args.cg_steps
+    res["cg_conformer_steps_per_s"] = args.conformers * args.cg_steps / (time.perf_counter() - t0)
+    b.close()
+    out["conformers"] = res
+    return out
+
+
 def count_pairs(x, cut, rcut_gb):
     """Unordered pairs within cut and within rgbmax + Fsmax (cell grid)."""
     from scipy.spatial import cKDTree
@@ -147,6 +248,10 @@ def main():
     ap.add_argument("--natom", type=int, default=25000)
     ap.add_argument("--seed", type=int, default=2025)
     ap.add_argument("--cpu-sample", type=int, default=6, help="evaluations in the CPU-baseline sample")
+    ap.add_argument("--uneven", type=int, default=512, help="molecules in the uneven-size batch (2048: full size)")
+    ap.add_argument("--conformers", type=int, default=512, help="conformers in the conformer batch")
+    ap.add_argument("--cg-steps", type=int, default=200, help="batched conjgrad steps on the conformers")
+    ap.add_argument("--no-batched", action="store_true", help="skip the batched-versus-plain measurements")
     args = ap.parse_args()
     rank, world, local = rank_info()
     cores = os.cpu_count() or 1
@@ -280,6 +385,8 @@ def main():
     fp32_peak = 152 * 128 * 2 * sm_mhz * 1e6 / 1e12
     achieved = flops[dom] / (pass_avg[dom] * 1e-3) / 1e12
 
+    batched = None if args.no_batched else bench_batched(args, stream, sp, flush)
+
     # CPU baseline: the oracle port on all host cores, bounded sample
     os.environ.setdefault("OMP_NUM_THREADS", str(cores))
     cpu_rate, cpu_dt, _ = run_cpu_reference(args, n, seed, args.cpu_sample, 1)
@@ -312,6 +419,7 @@ def main():
                 "path": "mme(x, f, &iter) of the C ABI, pinned host buffers"},
         "gpu_launches": launches,
         "clocks": clocks,
+        "batched": batched,
     }
     print(json.dumps(line))
     if dist:
