@@ -117,6 +117,46 @@ int sffg_batch_kernel_times(sffg_batch *b, double *ms3, long long *nevals);
 size_t sffg_batch_device_bytes(const sffg_batch *b);
 int sffg_batch_destroy(sffg_batch *b);
 
+/* ---- serving ------------------------------------------------------------ */
+
+/* A request loop with continuous batching (no counterpart in the
+ * reference).  Requests -- a minimisation (the reference's conjgrad() to
+ * rmsgrad or nsteps evaluations) or nsteps of Langevin md with the batch
+ * integrator -- wait in arrival order; every sffg_server_pump admits the
+ * waiting requests at the head of the queue that fit the device-memory
+ * budget as a new group (one batch on its own stream, resident until the
+ * group ends), advances every running group by `turns` evaluations or
+ * steps without waiting between groups, so their work overlaps on the GPU,
+ * and takes the result of every system that ended.  A result is the same
+ * whether the request ran alone or among others.  All requests of a server
+ * share its model options.  Not thread-safe: one thread drives a server. */
+#define SFFG_REQ_MINIMIZE 0
+#define SFFG_REQ_MD 1
+
+typedef struct sffg_server sffg_server;
+
+/* memory_budget_gb: device memory the running groups may hold (an estimate
+ * per request at admission, the measured size once admitted); max_groups:
+ * groups running at once. */
+int sffg_server_create(const char *opts, double memory_budget_gb, int max_groups, sffg_server **out);
+/* Copies the topology and coordinates (3*Natom) of one request; *id
+ * identifies it.  SFFG_ENOMEM when the request alone exceeds the budget. */
+int sffg_server_submit(sffg_server *s, PARMSTRUCT_T *prm, const double *x, int kind, int nsteps, double rmsgrad,
+                       long long *id);
+/* Admit, advance, collect; reports the groups running and the requests
+ * waiting. */
+int sffg_server_pump(sffg_server *s, int turns, int *nrunning, int *npending);
+/* The result of a finished request: the driver's return code (conjgrad's,
+ * or the steps run for md), final energy, coordinates (3*Natom, may be
+ * NULL) and the time from submission to the end, in ms.  SFFG_ESTATE while
+ * it runs or waits. */
+int sffg_server_result(sffg_server *s, long long id, int *status, double *energy, double *x, double *latency_ms);
+/* Device memory the running groups hold (bytes). */
+size_t sffg_server_device_bytes(const sffg_server *s);
+/* The most recent failure of this server. */
+const char *sffg_server_error(const sffg_server *s);
+int sffg_server_destroy(sffg_server *s);
+
 /* ---- Born radii without allocation ------------------------------------- */
 
 /* Largest molecule sffg_born_radii_static accepts: its scratch is one fixed

@@ -36,13 +36,6 @@ struct DBuf {
   size_t bytes() const { return n * sizeof(T); }
 };
 
-// State of one system's conjugate-gradient run (the locals of the
-// reference's conjgrad(), src/sff/conjgrad.c:40-55).
-struct CgState {
-  int done, ret, niter, nfbeg, iterc, nfopt, iterfm, iterrs, iretry, ier, maxiter;
-  double f, fmin, gmin, dfpr, gnew, step, finit, ginit, gsqrd, stmin, gamden, ddspln, stepch, sbound,
-      fch, sum, beta, gama, dgrad, dfpred;
-};
 
 }  // namespace
 
@@ -87,6 +80,8 @@ struct DeviceState {
   DBuf<float4> xb;
   DBuf<int> counters;
   DBuf<unsigned> step;  // md step number (the Philox counter of the noise)
+  DBuf<unsigned long long> sys_key;  // per system: noise key
+  DBuf<int> sys_flagB;               // per system: lists B and C to be remade
   // CUDA graphs of an evaluation and of an md step without a list rebuild,
   // with the list-buffer pointers they were captured against
   cudaGraphExec_t g_eval = nullptr, g_step = nullptr;
@@ -100,6 +95,7 @@ struct DeviceState {
   // minimisation
   DBuf<double> cg_w;
   DBuf<CgState> cg_state;
+  DBuf<int> cg_nactive;
   // per-pass timing: a ring of event pairs, read back lazily so that
   // timing never stalls the host between evaluations
   static constexpr int kRing = 64;
@@ -131,7 +127,7 @@ struct DeviceState {
     rel(cand_start); rel(cand_count); rel(chunksA); rel(chunksB); rel(chunksC); rel(chunk0A);
     rel(chunk0B); rel(chunk0C); rel(chunkA_i); rel(entA_slot); rel(chunkB_i); rel(entB_slot);
     rel(chunkC_i); rel(entC_slot); rel(entA_col); rel(entA_exc); rel(entB_col); rel(entC_col);
-    rel(xb); rel(counters); rel(step); rel(neck_pos); rel(neck_val); rel(tscal);
+    rel(xb); rel(counters); rel(step); rel(cg_nactive); rel(sys_key); rel(sys_flagB); rel(neck_pos); rel(neck_val); rel(tscal);
     rel(noise); rel(rndf); rel(ekin); rel(cg_w); rel(cg_state);
   }
 };
@@ -161,6 +157,14 @@ int Batch::add_system(PARMSTRUCT_T *prm, const int *frozen, const double *x, boo
   HostSystem hs;
   ModelParams mp;
   build_host_system(prm, frozen, opts_, mutate_prm, hs, mp);
+  return add_host_system(std::move(hs), x);
+}
+
+int Batch::add_host_system(HostSystem hs, const double *x) {
+  if (finalized_) {
+    last_error = "add_system after finalize";
+    return SFFG_ESTATE;
+  }
   SystemInfo si;
   si.natom = hs.natom;
   si.atom_off = natom_total_;
@@ -177,6 +181,7 @@ int Batch::add_system(PARMSTRUCT_T *prm, const int *frozen, const double *x, boo
       return SFFG_EINVAL;
     }
   }
+  si.noise_key = sys_.size();
   natom_total_ += hs.natom;
   x0_.emplace_back(x, x + 3 * hs.natom);
   host_.push_back(std::move(hs));
@@ -473,6 +478,13 @@ int Batch::upload() {
   SFFG_CK(d.xb.alloc(nslot_));
   SFFG_CK(d.counters.alloc(16));
   SFFG_CK(d.step.alloc(1));
+  SFFG_CK(d.sys_flagB.alloc(nsys));
+  SFFG_CK(cudaMemset(d.sys_flagB.p, 0, d.sys_flagB.bytes()));
+  {
+    std::vector<unsigned long long> keys(nsys);
+    for (int s = 0; s < nsys; s++) keys[s] = sys_[s].noise_key;
+    SFFG_CK(up(d.sys_key, keys));
+  }
   SFFG_CK(cudaMemset(d.step.p, 0, sizeof(unsigned)));
   SFFG_CK(cudaMemset(d.counters.p, 0, d.counters.bytes()));
   SFFG_CK(d.tscal.alloc(nsys));
@@ -737,6 +749,8 @@ ListArgs Batch::list_args(double fsmax) {
   a.entC_slot = d.entC_slot.p;
   a.entC_col = d.entC_col.p;
   a.flagB = d.counters.p + 4;
+  a.sys_flagB = d.sys_flagB.p;
+  a.nsys = num_systems();
   a.xb = d.xb.p;
   return a;
 }
@@ -807,7 +821,7 @@ int Batch::build_lists(void *stream) {
     const ListArgs a = list_args(fsmax);
     k_list_fill<false><<<cand_blocks, 256, 0, st>>>(a);
     k_list_pad<false><<<tile_blocks, 256, 0, st>>>(a);
-    k_list_done<<<1, 1, 0, st>>>(a.flagB);
+    k_list_done<<<(a.nsys + 255) / 256, 256, 0, st>>>(a.flagB, a.sys_flagB, a.nsys);
     SFFG_CK(cudaGetLastError());
     launches_ += 3;
   }
@@ -828,7 +842,7 @@ void Batch::rebuild_list_b(void *stream) {
   k_list_scan<true><<<1, 1024, 0, st>>>(a);
   k_list_fill<true><<<cand_blocks, 256, 0, st>>>(a);
   k_list_pad<true><<<tile_blocks, 256, 0, st>>>(a);
-  k_list_done<<<1, 1, 0, st>>>(a.flagB);
+  k_list_done<<<(a.nsys + 255) / 256, 256, 0, st>>>(a.flagB, a.sys_flagB, a.nsys);
   launches_ += 6;
 }
 
@@ -911,7 +925,7 @@ int Batch::run_eval_direct(bool rebuild, void *stream) {
   k_pack<<<(nslot_ + 255) / 256, 256, 0, st>>>(d.x.p, d.slot_atom.p, d.q32.p, d.tile_valid.p, nslot_, d.pos_hi.p,
                                                d.pos_lo.p, d.box_lo.p, d.box_hi.p, d.acc_sumi.p, d.acc_fx.p,
                                                d.acc_fy.p, d.acc_fz.p, d.nonfinite.p, d.tile_sys.p, d.xb.p,
-                                               0.2025f * kListSkin * kListSkin, d.counters.p + 4);
+                                               0.2025f * kListSkin * kListSkin, d.counters.p + 4, d.sys_flagB.p);
   SFFG_CK(cudaGetLastError());
   if (rebuild) {
     const int rc = build_lists(st);
@@ -1119,6 +1133,8 @@ static void md_args(Batch &b, DeviceState &d, const Options &o, int natom_total,
   a.gammai = gammai;
   a.seed = o.sffg_seed;
   a.step = d.step.p;
+  a.sys_atom_off = d.sys_atom_off.p;
+  a.sys_key = d.sys_key.p;
   c_ave = gammai > 0.0 ? 1.0 + gammai * dt5 : 1.0;
   (void)b;
 }
@@ -1486,30 +1502,52 @@ __global__ void __launch_bounds__(kCgThreads) k_cg_post(CgArgs a) {
 
 }  // namespace
 
-int Batch::cg(int maxiter, double rmsgrad, double dfpred, bool first_rebuild, std::vector<int> &status,
-              std::vector<double> &energy, void *stream, const std::function<int(int)> &after_eval) {
+// Batched conjgrad in pieces: cg_begin sets every system's state machine
+// at its start; cg_turns launches n turns (evaluation + state-machine step)
+// without waiting; cg_poll reads the states back; cg_end restores the
+// active flags.  cg() runs them to completion.
+int Batch::cg_begin(int maxiter, double rmsgrad, double dfpred, void *stream) {
+  return cg_begin(std::vector<int>(num_systems(), maxiter), std::vector<double>(num_systems(), rmsgrad), dfpred,
+                  stream);
+}
+
+int Batch::cg_begin(const std::vector<int> &maxiter, const std::vector<double> &rmsgrad, double dfpred,
+                    void *stream) {
   if (!finalized_) return SFFG_ESTATE;
+  if (static_cast<int>(maxiter.size()) != num_systems() || static_cast<int>(rmsgrad.size()) != num_systems()) {
+    last_error = "cg_begin: one maxiter and rmsgrad per system";
+    return SFFG_EINVAL;
+  }
   DeviceState &d = *d_;
   cudaStream_t st = pick(d, stream);
   const int nsys = num_systems();
   SFFG_CK(d.cg_w.alloc(6 * 3 * static_cast<size_t>(natom_total_)));
   SFFG_CK(d.cg_state.alloc(nsys));
+  SFFG_CK(d.cg_nactive.alloc(1));
   std::vector<CgState> init(nsys);
   for (int s = 0; s < nsys; s++) {
     CgState c;
     std::memset(&c, 0, sizeof(c));
     c.niter = 1;  // the reference's first ++niter at L10
-    c.maxiter = maxiter;
-    c.dgrad = rmsgrad * rmsgrad * 3.0 * sys_[s].natom;
+    c.maxiter = maxiter[s];
+    c.dgrad = rmsgrad[s] * rmsgrad[s] * 3.0 * sys_[s].natom;
     c.dfpred = dfpred;
     init[s] = c;
   }
-  SFFG_CK(cudaMemcpyAsync(d.cg_state.p, init.data(), nsys * sizeof(CgState), cudaMemcpyHostToDevice, st));
-  std::vector<int> ones(nsys, 1);
-  SFFG_CK(cudaMemcpyAsync(d.sys_active.p, ones.data(), nsys * sizeof(int), cudaMemcpyHostToDevice, st));
-  DBuf<int> nactive;
-  SFFG_CK(nactive.alloc(1));
-  SFFG_CK(cudaMemcpyAsync(nactive.p, &nsys, sizeof(int), cudaMemcpyHostToDevice, st));
+  cg_host_.assign(init.begin(), init.end());
+  SFFG_CK(cudaMemcpyAsync(d.cg_state.p, cg_host_.data(), nsys * sizeof(CgState), cudaMemcpyHostToDevice, st));
+  ones_.assign(nsys, 1);
+  SFFG_CK(cudaMemcpyAsync(d.sys_active.p, ones_.data(), nsys * sizeof(int), cudaMemcpyHostToDevice, st));
+  cg_nsys_ = nsys;
+  SFFG_CK(cudaMemcpyAsync(d.cg_nactive.p, &cg_nsys_, sizeof(int), cudaMemcpyHostToDevice, st));
+  cg_turn_ = 0;
+  cg_maxiter_ = *std::max_element(maxiter.begin(), maxiter.end());
+  return SFFG_OK;
+}
+
+int Batch::cg_turns(int n, bool first_rebuild, void *stream, const std::function<int(int)> &after_eval) {
+  DeviceState &d = *d_;
+  cudaStream_t st = pick(d, stream);
   CgArgs a;
   a.state = d.cg_state.p;
   a.x = d.x.p;
@@ -1519,35 +1557,82 @@ int Batch::cg(int maxiter, double rmsgrad, double dfpred, bool first_rebuild, st
   a.sys_natom = d.sys_natom.p;
   a.sys_atom_off = d.sys_atom_off.p;
   a.sys_active = d.sys_active.p;
-  a.nactive = nactive.p;
-  int rc = SFFG_OK;
-  for (int turn = 0; turn <= maxiter; turn++) {
+  a.nactive = d.cg_nactive.p;
+  for (int k = 0; k < n && cg_turn_ <= cg_maxiter_; k++, cg_turn_++) {
+    const int turn = cg_turn_;
     // every active system is at evaluation turn+1, so iter = turn for all
     const bool rebuild = (turn == 0 && first_rebuild) || (turn > 0 && opts_.nsnb > 0 && turn % opts_.nsnb == 0);
-    if ((rc = run_eval(rebuild || !have_list_, st))) break;
-    if (after_eval && (rc = after_eval(turn))) break;
-    k_cg_post<<<nsys, kCgThreads, 0, st>>>(a);
+    int rc = run_eval(rebuild || !have_list_, st);
+    if (rc) return rc;
+    if (after_eval && (rc = after_eval(turn))) return rc;
+    k_cg_post<<<num_systems(), kCgThreads, 0, st>>>(a);
     SFFG_CK(cudaGetLastError());
     launches_++;
-    if ((turn & 7) == 7 || turn == maxiter) {
-      int na = 0;
-      SFFG_CK(cudaMemcpyAsync(&na, nactive.p, sizeof(int), cudaMemcpyDeviceToHost, st));
-      SFFG_CK(cudaStreamSynchronize(st));
-      if (na <= 0) break;
-    }
   }
-  std::vector<CgState> fin(nsys);
-  SFFG_CK(cudaMemcpyAsync(fin.data(), d.cg_state.p, nsys * sizeof(CgState), cudaMemcpyDeviceToHost, st));
-  SFFG_CK(cudaMemcpyAsync(d.sys_active.p, ones.data(), nsys * sizeof(int), cudaMemcpyHostToDevice, st));
+  return SFFG_OK;
+}
+
+int Batch::cg_poll(int *nactive, std::vector<int> *status, std::vector<double> *energy, void *stream) {
+  DeviceState &d = *d_;
+  cudaStream_t st = pick(d, stream);
+  const int nsys = num_systems();
+  int na = 0;
+  SFFG_CK(cudaMemcpyAsync(&na, d.cg_nactive.p, sizeof(int), cudaMemcpyDeviceToHost, st));
+  if (status || energy)
+    SFFG_CK(cudaMemcpyAsync(cg_host_.data(), d.cg_state.p, nsys * sizeof(CgState), cudaMemcpyDeviceToHost, st));
   SFFG_CK(cudaStreamSynchronize(st));
-  nactive.release();
-  status.resize(nsys);
-  energy.resize(nsys);
-  for (int s = 0; s < nsys; s++) {
-    status[s] = fin[s].done ? fin[s].ret : -3;
-    energy[s] = fin[s].f;
+  if (cg_turn_ > cg_maxiter_) na = 0;  // every turn ran
+  if (nactive) *nactive = na;
+  if (status) {
+    status->resize(nsys);
+    for (int s = 0; s < nsys; s++) (*status)[s] = cg_host_[s].done ? cg_host_[s].ret : (na ? 0 : -3);
   }
-  return rc;
+  if (energy) {
+    energy->resize(nsys);
+    for (int s = 0; s < nsys; s++) (*energy)[s] = cg_host_[s].f;
+  }
+  return SFFG_OK;
+}
+
+int Batch::set_noise_key(int sys, unsigned long long key) {
+  if (finalized_ || sys < 0 || sys >= num_systems()) return SFFG_ESTATE;
+  sys_[sys].noise_key = key;
+  return SFFG_OK;
+}
+
+int Batch::set_active(int sys, bool on, void *stream) {
+  if (!finalized_ || sys < 0 || sys >= num_systems()) return SFFG_EINVAL;
+  DeviceState &d = *d_;
+  ones_.resize(num_systems());
+  ones_[sys] = on ? 1 : 0;
+  SFFG_CK(cudaMemcpyAsync(d.sys_active.p + sys, &ones_[sys], sizeof(int), cudaMemcpyHostToDevice, pick(d, stream)));
+  return SFFG_OK;
+}
+
+int Batch::cg_end(void *stream) {
+  DeviceState &d = *d_;
+  cudaStream_t st = pick(d, stream);
+  ones_.assign(num_systems(), 1);
+  SFFG_CK(cudaMemcpyAsync(d.sys_active.p, ones_.data(), ones_.size() * sizeof(int), cudaMemcpyHostToDevice, st));
+  SFFG_CK(cudaStreamSynchronize(st));
+  return SFFG_OK;
+}
+
+int Batch::cg(int maxiter, double rmsgrad, double dfpred, bool first_rebuild, std::vector<int> &status,
+              std::vector<double> &energy, void *stream, const std::function<int(int)> &after_eval) {
+  int rc = cg_begin(maxiter, rmsgrad, dfpred, stream);
+  if (rc) return rc;
+  bool first = first_rebuild;
+  while (true) {
+    if ((rc = cg_turns(8, first, stream, after_eval))) break;
+    first = false;
+    int na = 0;
+    if ((rc = cg_poll(&na, nullptr, nullptr, stream))) break;
+    if (na <= 0) break;
+  }
+  const int rc2 = cg_poll(nullptr, &status, &energy, stream);
+  const int rc3 = cg_end(stream);
+  return rc ? rc : (rc2 ? rc2 : rc3);
 }
 
 }  // namespace sffg

@@ -25,6 +25,14 @@ namespace sffg {
 struct DeviceState;  // defined in engine.cu
 struct ListArgs;     // defined in lists.cuh
 
+// State of one system's conjugate-gradient run (the locals of the
+// reference's conjgrad(), src/sff/conjgrad.c:40-55).
+struct CgState {
+  int done, ret, niter, nfbeg, iterc, nfopt, iterfm, iterrs, iretry, ier, maxiter;
+  double f, fmin, gmin, dfpr, gnew, step, finit, ginit, gsqrd, stmin, gamden, ddspln, stepch, sbound,
+      fch, sum, beta, gama, dgrad, dfpred;
+};
+
 struct SystemInfo {
   int natom = 0, atom_off = 0, slot_off = 0, tile_off = 0, ntile = 0;
   double fsmax = 0.0;
@@ -33,6 +41,7 @@ struct SystemInfo {
   std::vector<double> mass;
   int ntypes = 0;
   int lj_off = 0;
+  unsigned long long noise_key = 0;  // Philox key of the md noise (default: the system index)
 };
 
 class Batch {
@@ -44,6 +53,13 @@ class Batch {
 
   // Returns the system index, or a negative status.
   int add_system(PARMSTRUCT_T *prm, const int *frozen, const double *x, bool mutate_prm);
+  // The same for a topology already converted (build_host_system).
+  int add_host_system(HostSystem hs, const double *x);
+  // Key of a system's md noise (before finalize); systems with equal keys,
+  // topologies and coordinates draw equal noise in any batch.
+  int set_noise_key(int sys, unsigned long long key);
+  // Switches one system's work on or off (stream-ordered).
+  int set_active(int sys, bool on, void *stream);
   int finalize();
   bool finalized() const { return finalized_; }
   int num_systems() const { return static_cast<int>(sys_.size()); }
@@ -91,6 +107,17 @@ class Batch {
   // iteration count).
   int cg(int maxiter, double rmsgrad, double dfpred, bool first_rebuild, std::vector<int> &status,
          std::vector<double> &energy, void *stream, const std::function<int(int)> &after_eval);
+  // The same in pieces, for drivers that interleave several batches:
+  // cg_turns launches up to n turns without waiting (the first with a list
+  // rebuild when first_rebuild); cg_poll waits for the stream and reports
+  // the systems still running (0 once every system ended or maxiter turns
+  // ran) and, optionally, each system's return code (0: running) and
+  // energy; cg_end restores every system's active flag.
+  int cg_begin(int maxiter, double rmsgrad, double dfpred, void *stream);
+  int cg_begin(const std::vector<int> &maxiter, const std::vector<double> &rmsgrad, double dfpred, void *stream);
+  int cg_turns(int n, bool first_rebuild, void *stream, const std::function<int(int)> &after_eval = nullptr);
+  int cg_poll(int *nactive, std::vector<int> *status, std::vector<double> *energy, void *stream);
+  int cg_end(void *stream);
   // True once a pair list has been built.
   bool have_list() const { return have_list_; }
 
@@ -127,6 +154,10 @@ class Batch {
   std::vector<std::vector<double>> x0_;
   int natom_total_ = 0, nslot_ = 0, ntile_ = 0;
   unsigned step_host_ = 0;  // staging of the md step counter upload
+  // conjgrad driver state (host copies of the device state machines)
+  std::vector<CgState> cg_host_;
+  std::vector<int> ones_;
+  int cg_nsys_ = 0, cg_turn_ = 0, cg_maxiter_ = 0;
   long long cand_max_ = 0;  // candidate tile pairs the batch could ever need
   int ncand_ = 0;           // candidates of the current pair list
   bool finalized_ = false, have_list_ = false, profile_ = false;

@@ -19,7 +19,7 @@ __global__ void k_pack(const double *__restrict__ x, const int *__restrict__ slo
                        int nslot, float4 *pos_hi, float4 *pos_lo, float4 *box_lo, float4 *box_hi,
                        long long *acc_sumi, long long *acc_fx, long long *acc_fy, long long *acc_fz,
                        int *nonfinite_sys, const int *tile_sys, const float4 *xb, float xb_lim2,
-                       int *flagB) {
+                       int *flagB, int *sys_flagB) {
   const int slot = blockIdx.x * blockDim.x + threadIdx.x;
   const int lane = threadIdx.x & 31;
   if (slot - lane >= nslot) return;  // whole warp beyond the last tile
@@ -38,7 +38,10 @@ __global__ void k_pack(const double *__restrict__ x, const int *__restrict__ slo
     // since it was made (a NaN also asks for a rebuild)
     const float4 q = xb[slot];
     const float mx = hx - q.x, my = hy - q.y, mz = hz - q.z;
-    if (!(mx * mx + my * my + mz * mz <= xb_lim2)) *flagB = 1;
+    if (!(mx * mx + my * my + mz * mz <= xb_lim2)) {
+      *flagB = 1;
+      sys_flagB[tile_sys[tile]] = 1;
+    }
     if (!bad) {
       bx0 = bx1 = hx;
       by0 = by1 = hy;
@@ -410,6 +413,11 @@ struct MdArgs {
   double dtx, dt5, c_explic, c_implic, sdfac, vlimit, gammai;
   unsigned long long seed;
   const unsigned *step;  // Philox counter: the step number (advanced by k_md_tscal)
+  // per system: first atom and noise key; the noise of a coordinate depends
+  // on (system key, coordinate index within the system, step) only, so a
+  // system draws the same noise alone or in any batch
+  const int *sys_atom_off;
+  const unsigned long long *sys_key;
 };
 
 // First half of a step (src/sff/sff.c:2243-2248): half-kick and drift.
@@ -449,7 +457,9 @@ __global__ void k_md_kick(const MdArgs a, int init) {
         if (a.noise) {
           z = a.noise[i];
         } else {
-          const uint4 r = philox4x32(make_uint4(static_cast<unsigned>(i), *a.step, 0x51u, 0u),
+          const unsigned long long key = a.sys_key[sys];
+          const unsigned il = static_cast<unsigned>(i - 3 * a.sys_atom_off[sys]);
+          const uint4 r = philox4x32(make_uint4(il, *a.step, static_cast<unsigned>(key), static_cast<unsigned>(key >> 32)),
                                      make_uint2(static_cast<unsigned>(a.seed), static_cast<unsigned>(a.seed >> 32)));
           z = normal_from(r.x, r.y);
         }

@@ -36,8 +36,10 @@
 //   5 fill         warp per candidate: the entries
 //   6 pad          warp per i-tile: padding entries and chunk owners
 // Stages 2-6 also run in "lists B and C only" mode when the displacement
-// check (in k_pack) fires; each of those launches returns at once unless
-// the flag is set.
+// check (in k_pack) fires for some system; each of those launches returns
+// at once unless a flag is set, and only the flagged systems' lists are
+// remade (the others keep theirs), so a system's lists, and with them the
+// rounding of its sums, depend on its own history only.
 #pragma once
 
 #include "kernels.cuh"
@@ -80,7 +82,9 @@ struct ListArgs {
   unsigned *entC_col;
   // rebuild flag of lists B and C (set by the displacement check) and the
   // positions they were made from
-  int *flagB;
+  int *flagB;       // some system needs its lists B and C remade
+  int *sys_flagB;   // per system: this one does
+  int nsys;
   float4 *xb;
 };
 
@@ -154,6 +158,14 @@ __global__ void k_list_columns(const ListArgs a) {
   for (int c = (blockIdx.x * blockDim.x + threadIdx.x) >> 5; c < ncand; c += nwarps) {
   const int2 p = a.cand[c];
   const int I = p.x, J = p.y;
+  if (GB_ONLY && !a.sys_flagB[a.tile_sys[I]]) {
+    // this system keeps its lists: only the counts are needed again
+    const size_t e = static_cast<size_t>(c) * 32 + lane;
+    const int nA = __popc(__ballot_sync(kFull, a.colA[e] != 0u)), nB = __popc(__ballot_sync(kFull, a.colB[e] != 0u));
+    const int nC = __popc(__ballot_sync(kFull, a.colC[e] != 0u));
+    if (lane == 0) a.cand_n[c] = make_int4(nA, nB, nC, 0);
+    continue;
+  }
   const int si = I * 32 + lane, sj = J * 32 + lane;
   s_hi[w][lane] = a.pos_hi[si];
   s_lo[w][lane] = a.pos_lo[si];
@@ -381,11 +393,15 @@ __global__ void k_list_pad(const ListArgs a) {
     }
     for (int k = lane; k < nch; k += 32) owner[ch0 + k] = I;
   }
-  // lists B and C now reflect the current positions
-  a.xb[I * 32 + lane] = a.pos_hi[I * 32 + lane];
+  // lists B and C now reflect the current positions of the systems remade
+  if (!GB_ONLY || a.sys_flagB[a.tile_sys[I]]) a.xb[I * 32 + lane] = a.pos_hi[I * 32 + lane];
 }
 
 // Clears the list-B flag after a (re)build; launched last.
-__global__ void k_list_done(int *flagB) { *flagB = 0; }
+__global__ void k_list_done(int *flagB, int *sys_flagB, int nsys) {
+  const int s = blockIdx.x * blockDim.x + threadIdx.x;
+  if (s == 0) *flagB = 0;
+  if (s < nsys) sys_flagB[s] = 0;
+}
 
 }  // namespace sffg
