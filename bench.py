@@ -210,6 +210,58 @@ def bench_batched(args, stream, sp, flush):
     return out
 
 
+SERVE_OPTS = "gb=5, cut=999.0"
+
+
+def bench_serving(args):
+    """Poisson stream of minimisation requests (conjgrad to RMS gradient
+    0.01 or maxiter evaluations) served with continuous batching, against
+    the plain path: the same requests one at a time, each its own batch."""
+    from nabc_gb300.batch import Batch
+    from nabc_gb300.server import Server
+    rng = np.random.default_rng(5150)
+    n = args.serve_requests
+    sizes = np.floor(np.exp(rng.uniform(np.log(500), np.log(args.serve_max_atoms), n))).astype(int)
+    mols = make_molecules(sizes, 12000)
+    out = {"requests": n, "atoms_log_uniform": [500, args.serve_max_atoms], "options": SERVE_OPTS,
+           "rmsgrad": 0.01, "maxiter": args.serve_maxiter, "memory_budget_gb": 150.0}
+    # plain: one request at a time
+    t0 = time.perf_counter()
+    for prm, x, _ in mols:
+        b = Batch(SERVE_OPTS)
+        b.add(prm, x)
+        b.finalize()
+        b.cg(args.serve_maxiter, 0.01)
+        b.close()
+    plain_s = time.perf_counter() - t0
+    out["plain_requests_per_s"] = n / plain_s
+    rates = []
+    for rate in args.serve_rates:
+        arrive = np.cumsum(rng.exponential(1.0 / rate, n))
+        s = Server(SERVE_OPTS, memory_budget_gb=150.0, max_groups=16)
+        ids = [None] * n
+        t0 = time.perf_counter()
+        k = 0
+        while True:
+            now = time.perf_counter() - t0
+            while k < n and arrive[k] <= now:
+                prm, x, _ = mols[k]
+                ids[k] = s.submit(prm, x, "minimize", args.serve_maxiter, 0.01)
+                k += 1
+            nr, npend = s.pump(16)
+            if k == n and nr == 0 and npend == 0:
+                break
+            if nr == 0 and npend == 0 and k < n:
+                time.sleep(max(0.0, min(arrive[k] - (time.perf_counter() - t0), 0.01)))
+        span = time.perf_counter() - t0
+        lat = np.array([s.result(i)["latency_ms"] for i in ids])
+        s.close()
+        rates.append({"arrival_per_s": rate, "throughput_requests_per_s": n / span,
+                      "p50_ms": float(np.percentile(lat, 50)), "p99_ms": float(np.percentile(lat, 99))})
+    out["served"] = rates
+    return out
+
+
 def count_pairs(x, cut, rcut_gb):
     """Unordered pairs within cut and within rgbmax + Fsmax (cell grid)."""
     from scipy.spatial import cKDTree
@@ -252,6 +304,10 @@ def main():
     ap.add_argument("--conformers", type=int, default=512, help="conformers in the conformer batch")
     ap.add_argument("--cg-steps", type=int, default=200, help="batched conjgrad steps on the conformers")
     ap.add_argument("--no-batched", action="store_true", help="skip the batched-versus-plain measurements")
+    ap.add_argument("--serve-requests", type=int, default=48)
+    ap.add_argument("--serve-max-atoms", type=int, default=5000, help="50000: the full request size range")
+    ap.add_argument("--serve-maxiter", type=int, default=300, help="2000: the full conjgrad limit")
+    ap.add_argument("--serve-rates", type=float, nargs="*", default=[50.0, 500.0])
     args = ap.parse_args()
     rank, world, local = rank_info()
     cores = os.cpu_count() or 1
@@ -386,6 +442,7 @@ def main():
     achieved = flops[dom] / (pass_avg[dom] * 1e-3) / 1e12
 
     batched = None if args.no_batched else bench_batched(args, stream, sp, flush)
+    serving = None if args.no_batched else bench_serving(args)
 
     # CPU baseline: the oracle port on all host cores, bounded sample
     os.environ.setdefault("OMP_NUM_THREADS", str(cores))
@@ -420,6 +477,7 @@ def main():
         "gpu_launches": launches,
         "clocks": clocks,
         "batched": batched,
+        "serving": serving,
     }
     print(json.dumps(line))
     if dist:
