@@ -113,6 +113,13 @@ long long sffg_batch_launch_count(const sffg_batch *b);
 int sffg_batch_set_profiling(sffg_batch *b, int on);
 int sffg_batch_kernel_times(sffg_batch *b, double *ms3, long long *nevals);
 
+/* The work split of pair pass `pass` (0: Born radii, 1: GB + Coulomb + LJ,
+ * 2: chain rule): work items a warp claims per grab of the queue and
+ * persistent blocks.  With the option sffg_tune=1 (default) batches of
+ * 20,000 atoms or more choose it by timing candidates at their first
+ * evaluation without a list rebuild; results do not depend on it. */
+int sffg_batch_tuned_split(const sffg_batch *b, int pass, int *claim, int *blocks);
+
 /* Device memory the batch holds, in bytes. */
 size_t sffg_batch_device_bytes(const sffg_batch *b);
 int sffg_batch_destroy(sffg_batch *b);

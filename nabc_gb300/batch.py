@@ -109,6 +109,15 @@ class Batch:
     def device_bytes(self):
         return sff.lib().sffg_batch_device_bytes(self.h)
 
+    def tuned_split(self):
+        """(claim, blocks) of the three pair passes."""
+        out = []
+        for p in range(3):
+            c, b = C.c_int(0), C.c_int(0)
+            _check(sff.lib().sffg_batch_tuned_split(self.h, p, C.byref(c), C.byref(b)), "tuned_split")
+            out.append((c.value, b.value))
+        return out
+
     def close(self):
         if self.h:
             sff.lib().sffg_batch_destroy(self.h)

@@ -136,3 +136,8 @@ extern "C" int sffg_batch_destroy(sffg_batch *b) {
   delete b;
   return SFFG_OK;
 }
+
+extern "C" int sffg_batch_tuned_split(const sffg_batch *b, int pass, int *claim, int *blocks) {
+  if (!b || !claim || !blocks) return fail(SFFG_EINVAL, "null argument");
+  return b->impl->tuned_split(pass, claim, blocks);
+}

@@ -41,7 +41,8 @@ struct DBuf {
 
 struct DeviceState {
   cudaStream_t stream = nullptr;
-  int nsm = 0, grid_pair = 0;
+  int nsm = 0;
+  cudaEvent_t tune_ev[3][2] = {};  // pass timing while the work split is tuned
   // per slot
   DBuf<float4> pos_hi, pos_lo, gbpar;
   DBuf<int> param, slot_atom;
@@ -105,6 +106,9 @@ struct DeviceState {
   long long timed_evals = 0;
 
   ~DeviceState() {
+    for (auto &pe : tune_ev)
+      for (auto &e : pe)
+        if (e) cudaEventDestroy(e);
     if (g_eval) cudaGraphExecDestroy(g_eval);
     if (g_step) cudaGraphExecDestroy(g_step);
     for (auto &ring : events)
@@ -501,7 +505,16 @@ int Batch::upload() {
   }
   std::vector<double> onesd(nsys, 1.0);
   SFFG_CK(cudaMemcpy(d.tscal.p, onesd.data(), nsys * sizeof(double), cudaMemcpyHostToDevice));
-  d.grid_pair = d.nsm * pair_blocks_per_sm();
+  {
+    const bool neck = mp_.gb == 7 || mp_.gb == 8;
+    occ_[0] = born_blocks_per_sm(neck);
+    occ_[1] = gbpair_blocks_per_sm(mp_.kappa != 0.0);
+    occ_[2] = chain_blocks_per_sm(neck);
+    for (int p = 0; p < 3; p++) {
+      cfg_[p].claim = 4;
+      cfg_[p].blocks = occ_[p] * d.nsm;
+    }
+  }
   return SFFG_OK;
 }
 
@@ -901,11 +914,74 @@ int Batch::capture(cudaGraphExec_t &exec, std::vector<const void *> &sig, long l
   return SFFG_OK;
 }
 
+// The autotuner of the work split: for each pair pass, how many work
+// items a warp claims per grab of the queue and how many blocks run per SM.
+// Every candidate runs whole evaluations (twice; best of the two counts)
+// with the passes timed by events; each pass keeps its fastest candidate.
+// Results do not depend on the split (fixed-point sums), so tuning changes
+// speed only.  Batches under kTuneMinAtoms atoms keep the defaults.
+int Batch::ensure_tuned(cudaStream_t st) {
+  constexpr int kTuneMinAtoms = 20000;
+  if (tuned_ || !have_list_ || profile_ || !opts_.sffg_tune || natom_total_ < kTuneMinAtoms) return SFFG_OK;
+  DeviceState &d = *d_;
+  tuned_ = true;
+  for (auto &pe : d.tune_ev)
+    for (auto &e : pe)
+      if (!e) SFFG_CK(cudaEventCreate(&e));
+  struct Cand {
+    int claim, level;
+  };
+  std::vector<Cand> cands;
+  for (int claim : {1, 2, 4, 8})
+    for (int level = 0; level < 2; level++) cands.push_back({claim, level});
+  double best[3] = {1e30, 1e30, 1e30};
+  PassCfg pick_cfg[3] = {cfg_[0], cfg_[1], cfg_[2]};
+  tuning_ = true;
+  const long long l0 = launches_, e0 = timers().nevals;
+  int rc = SFFG_OK;
+  for (int round = 0; round < 2 && rc == SFFG_OK; round++)
+    for (const Cand &c : cands) {
+      for (int p = 0; p < 3; p++) {
+        cfg_[p].claim = c.claim;
+        cfg_[p].blocks = std::max(1, occ_[p] - c.level) * d.nsm;
+      }
+      if ((rc = run_eval_direct(false, st))) break;
+      if (cudaStreamSynchronize(st) != cudaSuccess) {
+        rc = SFFG_ECUDA;
+        break;
+      }
+      for (int p = 0; p < 3; p++) {
+        float ms = 0.f;
+        cudaEventElapsedTime(&ms, d.tune_ev[p][0], d.tune_ev[p][1]);
+        if (ms < best[p]) {
+          best[p] = ms;
+          pick_cfg[p] = cfg_[p];
+        }
+      }
+    }
+  tuning_ = false;
+  launches_ = l0;
+  timers().nevals = e0;
+  for (int p = 0; p < 3; p++) cfg_[p] = pick_cfg[p];
+  return rc;
+}
+
+int Batch::tuned_split(int pass, int *claim, int *blocks) const {
+  if (pass < 0 || pass > 2) return SFFG_EINVAL;
+  *claim = cfg_[pass].claim;
+  *blocks = cfg_[pass].blocks;
+  return SFFG_OK;
+}
+
 // One evaluation; without a list rebuild it replays a captured graph (one
 // launch instead of ~20) unless graphs are off or pass timing is on.
 int Batch::run_eval(bool rebuild, void *stream) {
   DeviceState &d = *d_;
   cudaStream_t st = pick(d, stream);
+  if (!rebuild) {
+    const int rc = ensure_tuned(st);
+    if (rc) return rc;
+  }
   if (rebuild || !graphs_ok()) return run_eval_direct(rebuild, st);
   int rc = capture(d.g_eval, d.sig_eval, d.launches_eval,
                    [&](cudaStream_t cs) { return run_eval_direct(false, cs); });
@@ -960,7 +1036,10 @@ int Batch::run_eval_direct(bool rebuild, void *stream) {
   }
   {
     DevTables t = make_tables(d, mp_, fsmax, 5);
-    launch_born(neck, d.nsm, st, t);
+    t.claim = cfg_[0].claim;
+    if (tuning_) SFFG_CK(cudaEventRecord(d.tune_ev[0][0], st));
+    launch_born(neck, cfg_[0].blocks, st, t);
+    if (tuning_) SFFG_CK(cudaEventRecord(d.tune_ev[0][1], st));
     SFFG_CK(cudaGetLastError());
   }
   if (profile_) SFFG_CK(cudaEventRecord(d.events[ring][0][1], st));
@@ -996,7 +1075,10 @@ int Batch::run_eval_direct(bool rebuild, void *stream) {
   if (profile_) SFFG_CK(cudaEventRecord(d.events[ring][1][0], st));
   {
     DevTables t = make_tables(d, mp_, fsmax, 6);
-    launch_gbpair(mp_.kappa != 0.0, d.grid_pair, st, t);
+    t.claim = cfg_[1].claim;
+    if (tuning_) SFFG_CK(cudaEventRecord(d.tune_ev[1][0], st));
+    launch_gbpair(mp_.kappa != 0.0, cfg_[1].blocks, st, t);
+    if (tuning_) SFFG_CK(cudaEventRecord(d.tune_ev[1][1], st));
     SFFG_CK(cudaGetLastError());
   }
   if (profile_) SFFG_CK(cudaEventRecord(d.events[ring][1][1], st));
@@ -1006,7 +1088,10 @@ int Batch::run_eval_direct(bool rebuild, void *stream) {
   if (profile_) SFFG_CK(cudaEventRecord(d.events[ring][2][0], st));
   {
     DevTables t = make_tables(d, mp_, fsmax, 7);
-    launch_chain(neck, d.nsm, st, t);
+    t.claim = cfg_[2].claim;
+    if (tuning_) SFFG_CK(cudaEventRecord(d.tune_ev[2][0], st));
+    launch_chain(neck, cfg_[2].blocks, st, t);
+    if (tuning_) SFFG_CK(cudaEventRecord(d.tune_ev[2][1], st));
     SFFG_CK(cudaGetLastError());
   }
   if (profile_) {
@@ -1223,6 +1308,7 @@ int Batch::md_steps(int step0, int k, NoiseFn noise, void *noise_ctx, void *stre
     const int nstep = step0 + i;
     const bool rebuild = opts_.nsnb > 0 && nstep % opts_.nsnb == 0;
     if (!rebuild && !noise && graphs_ok()) {
+      if ((rc = ensure_tuned(st))) break;
       if ((rc = capture(d.g_step, d.sig_step, d.launches_step, [&](cudaStream_t cs) { return step_body(cs, false, true); })))
         break;
       SFFG_CK(cudaGraphLaunch(d.g_step, st));

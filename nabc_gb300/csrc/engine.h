@@ -124,6 +124,10 @@ class Batch {
   size_t device_bytes() const;
   std::string last_error;
 
+  // The work split the autotuner chose for pass 0, 1 or 2 (pair passes 1-3):
+  // work items claimed per grab and persistent blocks.
+  int tuned_split(int pass, int *claim, int *blocks) const;
+
   // Launch counting and per-pass CUDA-event timing.
   long long launches() const { return launches_; }
   int set_profiling(bool on);
@@ -137,6 +141,7 @@ class Batch {
  private:
   int upload();
   int run_eval_direct(bool rebuild, void *stream);
+  int ensure_tuned(cudaStream_t st);
   std::vector<const void *> list_sig() const;
   bool graphs_ok() const;
   int capture(cudaGraphExec_t &exec, std::vector<const void *> &sig, long long &nlaunch,
@@ -154,6 +159,13 @@ class Batch {
   std::vector<std::vector<double>> x0_;
   int natom_total_ = 0, nslot_ = 0, ntile_ = 0;
   unsigned step_host_ = 0;  // staging of the md step counter upload
+  // work split of the three pair passes (autotuned, see ensure_tuned)
+  struct PassCfg {
+    int claim = 4, blocks = 1;
+  };
+  PassCfg cfg_[3];
+  int occ_[3] = {1, 1, 1};
+  bool tuned_ = false, tuning_ = false;
   // conjgrad driver state (host copies of the device state machines)
   std::vector<CgState> cg_host_;
   std::vector<int> ones_;

@@ -20,7 +20,6 @@
 namespace sffg {
 
 constexpr unsigned kFull = 0xffffffffu;
-constexpr int kChunk = 4;  // list chunks a warp claims per work-queue grab
 
 // One compacted pair list (built by lists.cuh).
 struct ChunkList {
@@ -51,6 +50,7 @@ struct DevTables {
   // lc the pairs within near-field range) for passes 1 and 3
   ChunkList la, lb, lc;
   int *counter;
+  int claim;  // work items a warp takes per grab of the queue (tuned)
   // accumulators
   long long *acc_sumi, *acc_sd, *acc_fx, *acc_fy, *acc_fz;
   long long *energy;       // nsys * E_NSLOTS
@@ -123,10 +123,10 @@ __device__ __forceinline__ void atomic_add_ll(long long *p, long long v) {
   if (v != 0) atomicAdd(reinterpret_cast<unsigned long long *>(p), static_cast<unsigned long long>(v));
 }
 
-// Claims the next chunk of the work queue for this warp.
-__device__ __forceinline__ int claim_chunk(int *counter, int lane) {
+// Claims the next `claim` work items of the queue for this warp.
+__device__ __forceinline__ int claim_chunk(int *counter, int lane, int claim) {
   int base = 0;
-  if (lane == 0) base = atomicAdd(counter, kChunk);
+  if (lane == 0) base = atomicAdd(counter, claim);
   return __shfl_sync(kFull, base, 0);
 }
 
@@ -363,9 +363,9 @@ __global__ void __launch_bounds__(256, 3) k_born(const DevTables t) {
   };
 
   for (;;) {
-    const int base = claim_chunk(t.counter, lane);
+    const int base = claim_chunk(t.counter, lane, t.claim);
     if (base >= nitem) break;
-    const int end = min(base + kChunk, nitem);
+    const int end = min(base + t.claim, nitem);
     for (int m = base; m < end; m++) {
       int k;
       const bool nr = merged_item(m, nB, nC, k);
@@ -426,9 +426,9 @@ __global__ void __launch_bounds__(256, 2) k_gbpair(const DevTables t) {
     ep64 = ee64 = ev64 = 0;
   };
   for (;;) {
-    const int base = claim_chunk(t.counter, lane);
+    const int base = claim_chunk(t.counter, lane, t.claim);
     if (base >= nchunk) break;
-    const int end = min(base + kChunk, nchunk);
+    const int end = min(base + t.claim, nchunk);
     for (int k = base; k < end; k++) {
       const int I = t.la.chunk_i[k];
       const int sys = t.tile_sys[I];
@@ -681,9 +681,9 @@ __global__ void __launch_bounds__(256, 3) k_chain(const DevTables t) {
   };
 
   for (;;) {
-    const int base = claim_chunk(t.counter, lane);
+    const int base = claim_chunk(t.counter, lane, t.claim);
     if (base >= nitem) break;
-    const int end = min(base + kChunk, nitem);
+    const int end = min(base + t.claim, nitem);
     for (int m = base; m < end; m++) {
       int k;
       const bool nr = merged_item(m, nB, nC, k);

@@ -3,18 +3,16 @@
 
 namespace sffg {
 
-// Persistent grid: as many 256-thread blocks as fit on the GPU at once.
-template <class K>
-int full_grid(K kernel, int nsm) {
-  int occ = 0;
-  cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, kernel, 256, 0);
-  return nsm * (occ > 0 ? occ : 1);
+void launch_born(bool neck, int grid, cudaStream_t st, const DevTables &t) {
+  if (neck) k_born<true><<<grid, 256, 0, st>>>(t);
+  else k_born<false><<<grid, 256, 0, st>>>(t);
 }
 
-void launch_born(bool neck, int nsm, cudaStream_t st, const DevTables &t) {
-  static const int g1 = full_grid(k_born<true>, nsm), g0 = full_grid(k_born<false>, nsm);
-  if (neck) k_born<true><<<g1, 256, 0, st>>>(t);
-  else k_born<false><<<g0, 256, 0, st>>>(t);
+int born_blocks_per_sm(bool neck) {
+  int occ = 0;
+  if (neck) cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, k_born<true>, 256, 0);
+  else cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, k_born<false>, 256, 0);
+  return occ > 0 ? occ : 1;
 }
 
 }  // namespace sffg

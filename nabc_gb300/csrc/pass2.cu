@@ -8,12 +8,11 @@ void launch_gbpair(bool kappa, int grid, cudaStream_t st, const DevTables &t) {
   else k_gbpair<false><<<grid, 256, 0, st>>>(t);
 }
 
-int pair_blocks_per_sm() {
-  int a = 0, b = 0, c = 0;
-  cudaOccupancyMaxActiveBlocksPerMultiprocessor(&a, k_gbpair<false>, 256, 0);
-  cudaOccupancyMaxActiveBlocksPerMultiprocessor(&b, k_gbpair<true>, 256, 0);
-  c = a < b ? a : b;
-  return c > 0 ? c : 1;
+int gbpair_blocks_per_sm(bool kappa) {
+  int occ = 0;
+  if (kappa) cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, k_gbpair<true>, 256, 0);
+  else cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, k_gbpair<false>, 256, 0);
+  return occ > 0 ? occ : 1;
 }
 
 }  // namespace sffg

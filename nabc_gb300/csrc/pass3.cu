@@ -4,18 +4,16 @@
 
 namespace sffg {
 
-// Persistent grid: as many 256-thread blocks as fit on the GPU at once.
-template <class K>
-int full_grid(K kernel, int nsm) {
-  int occ = 0;
-  cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, kernel, 256, 0);
-  return nsm * (occ > 0 ? occ : 1);
+void launch_chain(bool neck, int grid, cudaStream_t st, const DevTables &t) {
+  if (neck) k_chain<true><<<grid, 256, 0, st>>>(t);
+  else k_chain<false><<<grid, 256, 0, st>>>(t);
 }
 
-void launch_chain(bool neck, int nsm, cudaStream_t st, const DevTables &t) {
-  static const int g1 = full_grid(k_chain<true>, nsm), g0 = full_grid(k_chain<false>, nsm);
-  if (neck) k_chain<true><<<g1, 256, 0, st>>>(t);
-  else k_chain<false><<<g0, 256, 0, st>>>(t);
+int chain_blocks_per_sm(bool neck) {
+  int occ = 0;
+  if (neck) cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, k_chain<true>, 256, 0);
+  else cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, k_chain<false>, 256, 0);
+  return occ > 0 ? occ : 1;
 }
 
 }  // namespace sffg

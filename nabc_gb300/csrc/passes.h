@@ -8,12 +8,13 @@
 
 namespace sffg {
 
-// Passes 1 and 3 size their persistent grids from the occupancy of the
-// kernel launched (nsm: multiprocessors of the device).
-void launch_born(bool neck, int nsm, cudaStream_t st, const DevTables &t);
+// grid: 256-thread blocks of the persistent kernel.
+void launch_born(bool neck, int grid, cudaStream_t st, const DevTables &t);
 void launch_gbpair(bool kappa, int grid, cudaStream_t st, const DevTables &t);
-void launch_chain(bool neck, int nsm, cudaStream_t st, const DevTables &t);
-// Resident 256-thread blocks per SM of the pair kernels.
-int pair_blocks_per_sm();
+void launch_chain(bool neck, int grid, cudaStream_t st, const DevTables &t);
+// Resident 256-thread blocks per SM of each pair kernel.
+int born_blocks_per_sm(bool neck);
+int gbpair_blocks_per_sm(bool kappa);
+int chain_blocks_per_sm(bool neck);
 
 }  // namespace sffg

@@ -114,6 +114,7 @@ def lib():
         L.sffg_batch_launch_count.restype = C.c_longlong
         L.sffg_batch_set_profiling.argtypes = [vp, C.c_int]
         L.sffg_batch_kernel_times.argtypes = [vp, C.POINTER(C.c_double), C.POINTER(C.c_longlong)]
+        L.sffg_batch_tuned_split.argtypes = [vp, C.c_int, INT_P, INT_P]
         L.sffg_batch_device_bytes.argtypes = [vp]
         L.sffg_batch_device_bytes.restype = C.c_size_t
         L.sffg_batch_destroy.argtypes = [vp]

@@ -129,3 +129,24 @@ def test_graph_replay_bit_identical(lib):
     for u, v in zip(out[0], out[1]):
         assert np.array_equal(u, v)
     sff.free_prm(prm)
+
+
+def test_autotuned_split_bit_identical(lib):
+    """The autotuner picks the work split of each pass by timing; the
+    results are the same bits with or without it."""
+    from nabc_gb300 import sff
+    from nabc_gb300.batch import Batch
+    prm, x, _ = sff.synth_molecule(22000, 31)
+    res = []
+    for tune in (0, 1):
+        b = Batch(f"gb=5, cut=20.0, rgbmax=15.0, sffg_tune={tune}")
+        b.add(prm, x)
+        b.finalize()
+        b.eval(rebuild=True)
+        b.eval()
+        res.append((b.energy(0), b.grad(0), b.tuned_split()))
+        b.close()
+    assert np.array_equal(res[0][0], res[1][0]) and np.array_equal(res[0][1], res[1][1])
+    for claim, blocks in res[1][2]:
+        assert claim in (1, 2, 4, 8) and blocks > 0
+    sff.free_prm(prm)
