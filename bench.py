@@ -44,6 +44,11 @@ OPTS = "gb=5, rgbmax=15.0, cut=25.0, nsnb=10, dt=0.002, gamma_ln=5.0, temp0=300.
 # = 1, FFMA = 2) for the three passes, from the reference formulas at
 # kappa = 0 with the far-field Born branch.
 FLOPS_PASS = (36.0, 60.0, 62.0)
+# DRAM bytes (read + write) per launch of each pass on this workload, from
+# one ncu capture (dram__bytes_read.sum + dram__bytes_write.sum): the inputs
+# (~1.6 MB of per-atom data, the lists) stay in L2, so traffic is far below
+# what the FP32 work would allow.
+TRAFFIC_PASS = (6.77e6, 17.87e6, 7.28e6)
 
 
 def rank_info():
@@ -306,6 +311,9 @@ def main():
     ap.add_argument("--conformers", type=int, default=512, help="conformers in the conformer batch")
     ap.add_argument("--cg-steps", type=int, default=200, help="batched conjgrad steps on the conformers")
     ap.add_argument("--no-batched", action="store_true", help="skip the batched-versus-plain measurements")
+    ap.add_argument("--no-tune", action="store_true",
+                    help="default work split instead of the autotuned one (for profiler runs, whose timing the "
+                         "tuner would otherwise follow)")
     ap.add_argument("--serve-requests", type=int, default=48)
     ap.add_argument("--serve-max-atoms", type=int, default=5000, help="50000: the full request size range")
     ap.add_argument("--serve-maxiter", type=int, default=300, help="2000: the full conjgrad limit")
@@ -348,7 +356,8 @@ def main():
     cut, rgbmax = 25.0, 15.0
     npairs, npairs_gb = count_pairs(x, cut, rgbmax + prm.contents.Fsmax)
 
-    b = Batch(OPTS)
+    opts = OPTS + (", sffg_tune=0" if args.no_tune else "")
+    b = Batch(opts)
     b.add(prm, x)
     b.finalize()
     # one explicit stream carries the flush, the timing events and every
@@ -469,7 +478,7 @@ def main():
                    "accuracy_vs_fp64": err,
                    "tuned_split_claim_blocks": split},
         "roofline": {"bound": "fp32", "kernel": names[dom], "achieved": achieved, "peak": fp32_peak,
-                     "unit": "TFLOP/s", "frac": achieved / fp32_peak, "traffic": None,
+                     "unit": "TFLOP/s", "frac": achieved / fp32_peak, "traffic": TRAFFIC_PASS[dom],
                      "peak_source": f"nominal FP32 FMA rate (152 SMs x 128 lanes x 2) at the sampled median SM clock "
                                     f"{sm_mhz:.0f} MHz; no tensor cores or HBM bound apply to this pass",
                      "algorithmic_flops_per_launch": flops[dom], "avg_launch_ms": pass_avg[dom],

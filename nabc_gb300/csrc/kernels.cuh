@@ -69,12 +69,13 @@ __device__ __forceinline__ long long to_fixed(float v, float scale) {
 // registers for a group of steps, then folded across the warp.  Fewer steps
 // per group keep the unrolled loop body (and the instruction-cache
 // footprint) small at the cost of more shuffles per step; measured best:
-// 4 for passes 1 and 3, 8 for pass 2.
+// 4 for all three passes (with pass 2 at 3 blocks per SM; at 2 blocks per
+// SM, 8 was better for it).
 #ifndef SFFG_GROUP_BORN
 #define SFFG_GROUP_BORN 4
 #endif
 #ifndef SFFG_GROUP_PAIR
-#define SFFG_GROUP_PAIR 8
+#define SFFG_GROUP_PAIR 4
 #endif
 constexpr int kGroup = SFFG_GROUP_BORN;
 constexpr int kGroupPair = SFFG_GROUP_PAIR;
@@ -397,7 +398,7 @@ __global__ void __launch_bounds__(256, 3) k_born(const DevTables t) {
 // GB + Coulomb + Lennard-Jones pair energies, dE/dr and sumdeijda
 // (src/sff/eff.c:1902-2063) over list A.
 template <bool KAPPA>
-__global__ void __launch_bounds__(256, 2) k_gbpair(const DevTables t) {
+__global__ void __launch_bounds__(256, 3) k_gbpair(const DevTables t) {
   __shared__ float4 sm_hi[8][32], sm_lo[8][32];
   __shared__ float2 sm_aux[8][32];
   __shared__ unsigned sm_col[8][32], sm_exc[8][32];
