@@ -82,7 +82,7 @@ struct DeviceState {
   DBuf<int> counters;
   DBuf<unsigned> step;  // md step number (the Philox counter of the noise)
   DBuf<unsigned long long> sys_key;  // per system: noise key
-  DBuf<int> sys_flagB;               // per system: lists B and C to be remade
+  DBuf<int> tile_flagB;              // per tile: entries of lists B and C to be remade
   // CUDA graphs of an evaluation and of an md step without a list rebuild,
   // with the list-buffer pointers they were captured against
   cudaGraphExec_t g_eval = nullptr, g_step = nullptr;
@@ -131,7 +131,7 @@ struct DeviceState {
     rel(cand_start); rel(cand_count); rel(chunksA); rel(chunksB); rel(chunksC); rel(chunk0A);
     rel(chunk0B); rel(chunk0C); rel(chunkA_i); rel(entA_slot); rel(chunkB_i); rel(entB_slot);
     rel(chunkC_i); rel(entC_slot); rel(entA_col); rel(entA_exc); rel(entB_col); rel(entC_col);
-    rel(xb); rel(counters); rel(step); rel(cg_nactive); rel(sys_key); rel(sys_flagB); rel(neck_pos); rel(neck_val); rel(tscal);
+    rel(xb); rel(counters); rel(step); rel(cg_nactive); rel(sys_key); rel(tile_flagB); rel(neck_pos); rel(neck_val); rel(tscal);
     rel(noise); rel(rndf); rel(ekin); rel(cg_w); rel(cg_state);
   }
 };
@@ -482,8 +482,8 @@ int Batch::upload() {
   SFFG_CK(d.xb.alloc(nslot_));
   SFFG_CK(d.counters.alloc(16));
   SFFG_CK(d.step.alloc(1));
-  SFFG_CK(d.sys_flagB.alloc(nsys));
-  SFFG_CK(cudaMemset(d.sys_flagB.p, 0, d.sys_flagB.bytes()));
+  SFFG_CK(d.tile_flagB.alloc(ntile_));
+  SFFG_CK(cudaMemset(d.tile_flagB.p, 0, d.tile_flagB.bytes()));
   {
     std::vector<unsigned long long> keys(nsys);
     for (int s = 0; s < nsys; s++) keys[s] = sys_[s].noise_key;
@@ -762,8 +762,7 @@ ListArgs Batch::list_args(double fsmax) {
   a.entC_slot = d.entC_slot.p;
   a.entC_col = d.entC_col.p;
   a.flagB = d.counters.p + 4;
-  a.sys_flagB = d.sys_flagB.p;
-  a.nsys = num_systems();
+  a.tile_flagB = d.tile_flagB.p;
   a.xb = d.xb.p;
   return a;
 }
@@ -834,7 +833,7 @@ int Batch::build_lists(void *stream) {
     const ListArgs a = list_args(fsmax);
     k_list_fill<false><<<cand_blocks, 256, 0, st>>>(a);
     k_list_pad<false><<<tile_blocks, 256, 0, st>>>(a);
-    k_list_done<<<(a.nsys + 255) / 256, 256, 0, st>>>(a.flagB, a.sys_flagB, a.nsys);
+    k_list_done<<<(a.ntile + 255) / 256, 256, 0, st>>>(a.flagB, a.tile_flagB, a.ntile);
     SFFG_CK(cudaGetLastError());
     launches_ += 3;
   }
@@ -855,7 +854,7 @@ void Batch::rebuild_list_b(void *stream) {
   k_list_scan<true><<<1, 1024, 0, st>>>(a);
   k_list_fill<true><<<cand_blocks, 256, 0, st>>>(a);
   k_list_pad<true><<<tile_blocks, 256, 0, st>>>(a);
-  k_list_done<<<(a.nsys + 255) / 256, 256, 0, st>>>(a.flagB, a.sys_flagB, a.nsys);
+  k_list_done<<<(a.ntile + 255) / 256, 256, 0, st>>>(a.flagB, a.tile_flagB, a.ntile);
   launches_ += 6;
 }
 
@@ -1001,7 +1000,7 @@ int Batch::run_eval_direct(bool rebuild, void *stream) {
   k_pack<<<(nslot_ + 255) / 256, 256, 0, st>>>(d.x.p, d.slot_atom.p, d.q32.p, d.tile_valid.p, nslot_, d.pos_hi.p,
                                                d.pos_lo.p, d.box_lo.p, d.box_hi.p, d.acc_sumi.p, d.acc_fx.p,
                                                d.acc_fy.p, d.acc_fz.p, d.nonfinite.p, d.tile_sys.p, d.xb.p,
-                                               0.2025f * kListSkin * kListSkin, d.counters.p + 4, d.sys_flagB.p);
+                                               kListMove * kListMove, d.counters.p + 4, d.tile_flagB.p);
   SFFG_CK(cudaGetLastError());
   if (rebuild) {
     const int rc = build_lists(st);

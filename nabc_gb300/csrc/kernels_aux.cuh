@@ -19,7 +19,7 @@ __global__ void k_pack(const double *__restrict__ x, const int *__restrict__ slo
                        int nslot, float4 *pos_hi, float4 *pos_lo, float4 *box_lo, float4 *box_hi,
                        long long *acc_sumi, long long *acc_fx, long long *acc_fy, long long *acc_fz,
                        int *nonfinite_sys, const int *tile_sys, const float4 *xb, float xb_lim2,
-                       int *flagB, int *sys_flagB) {
+                       int *flagB, int *tile_flagB) {
   const int slot = blockIdx.x * blockDim.x + threadIdx.x;
   const int lane = threadIdx.x & 31;
   if (slot - lane >= nslot) return;  // whole warp beyond the last tile
@@ -34,13 +34,14 @@ __global__ void k_pack(const double *__restrict__ x, const int *__restrict__ slo
     const float hx = static_cast<float>(X), hy = static_cast<float>(Y), hz = static_cast<float>(Z);
     hi = make_float4(hx, hy, hz, q32[slot]);
     lo = make_float4(static_cast<float>(X - hx), static_cast<float>(Y - hy), static_cast<float>(Z - hz), 0.f);
-    // list B stays valid while no atom has moved more than sqrt(xb_lim2)
-    // since it was made (a NaN also asks for a rebuild)
+    // a tile's entries of lists B and C stay valid while none of its atoms
+    // has moved more than sqrt(xb_lim2) since they were made (a NaN also
+    // asks for a remake)
     const float4 q = xb[slot];
     const float mx = hx - q.x, my = hy - q.y, mz = hz - q.z;
     if (!(mx * mx + my * my + mz * mz <= xb_lim2)) {
       *flagB = 1;
-      sys_flagB[tile_sys[tile]] = 1;
+      tile_flagB[tile] = 1;
     }
     if (!bad) {
       bx0 = bx1 = hx;

@@ -19,11 +19,12 @@
 //           evaluation.  List C holds the pairs close enough to need the
 //           near-field forms of the descreening integral (r < 4 max(s_i,
 //           s_j) + skin), list B all others, so the main kernels of passes 1
-//           and 3 carry no near-field code.  Lists B and C are remade from
-//           list A (on the device, with no host round trip) as soon as any
-//           atom has moved more than 0.45 skin since they were made, so
-//           every pair of list A within rgbmax + Fsmax now is on B or C,
-//           and no pair of list B has come within 4 max(s_i, s_j).
+//           and 3 carry no near-field code.  The entries of a tile are
+//           remade from list A (on the device, with no host round trip) as
+//           soon as one of its atoms has moved more than skin / 3 since its
+//           last remake, so every pair of list A within rgbmax + Fsmax now
+//           is on B or C, and no pair of list B has come within
+//           4 max(s_i, s_j).
 //
 // Build stages (one launch each):
 //   1 candidates   warp per i-tile: tile pairs (I, J >= I) whose bounding
@@ -36,17 +37,24 @@
 //   5 fill         warp per candidate: the entries
 //   6 pad          warp per i-tile: padding entries and chunk owners
 // Stages 2-6 also run in "lists B and C only" mode when the displacement
-// check (in k_pack) fires for some system; each of those launches returns
-// at once unless a flag is set, and only the flagged systems' lists are
-// remade (the others keep theirs), so a system's lists, and with them the
-// rounding of its sums, depend on its own history only.
+// check (in k_pack) fires for some tile; each of those launches returns at
+// once unless a flag is set, and only the tile pairs with a flagged tile
+// get new columns (the others keep theirs), and only flagged tiles take new
+// reference positions.  Since a tile pair's columns were made, each of its
+// atoms has moved at most 2 x skin/3 from there (skin/3 from its reference
+// position, which was at most skin/3 away then) and the flagged tile's
+// atoms at most skin/3, so the pair distance has changed by less than the
+// skin: no pair within rgbmax + Fsmax is ever missing, none of list B is
+// in near-field range; and a system's lists, with the rounding of its
+// sums, depend on its own atoms only.
 #pragma once
 
 #include "kernels.cuh"
 
 namespace sffg {
 
-constexpr float kListSkin = 0.6f;  // margin of lists B and C, in Angstrom
+constexpr float kListSkin = 0.8f;  // margin of lists B and C, in Angstrom
+constexpr float kListMove = kListSkin / 3.0f;  // displacement that remakes a tile's entries
 
 struct ListArgs {
   const float4 *pos_hi, *pos_lo, *box_lo, *box_hi;
@@ -82,9 +90,8 @@ struct ListArgs {
   unsigned *entC_col;
   // rebuild flag of lists B and C (set by the displacement check) and the
   // positions they were made from
-  int *flagB;       // some system needs its lists B and C remade
-  int *sys_flagB;   // per system: this one does
-  int nsys;
+  int *flagB;        // some tile needs its entries of lists B and C remade
+  int *tile_flagB;   // per tile: an atom of it moved more than kListMove
   float4 *xb;
 };
 
@@ -152,14 +159,16 @@ __global__ void k_list_columns(const ListArgs a) {
   __shared__ float4 s_hi[8][32], s_lo[8][32];
   __shared__ float s_s[8][32];
   __shared__ int s_atom[8][32];
+  __shared__ unsigned s_ex[8][32];
   if (GB_ONLY && !*a.flagB) return;
   const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
   const int ncand = *a.ncand, nwarps = (gridDim.x * blockDim.x) >> 5;
   for (int c = (blockIdx.x * blockDim.x + threadIdx.x) >> 5; c < ncand; c += nwarps) {
   const int2 p = a.cand[c];
   const int I = p.x, J = p.y;
-  if (GB_ONLY && !a.sys_flagB[a.tile_sys[I]]) {
-    // this system keeps its lists: only the counts are needed again
+  if (GB_ONLY && !a.tile_flagB[I] && !a.tile_flagB[J]) {
+    // both tiles stayed within kListMove of their reference positions: the
+    // pairs keep their lists, only the counts are needed again
     const size_t e = static_cast<size_t>(c) * 32 + lane;
     const int nA = __popc(__ballot_sync(kFull, a.colA[e] != 0u)), nB = __popc(__ballot_sync(kFull, a.colB[e] != 0u));
     const int nC = __popc(__ballot_sync(kFull, a.colC[e] != 0u));
@@ -178,13 +187,24 @@ __global__ void k_list_columns(const ListArgs a) {
   const bool frzj = (a.param[sj] >> 24) & 1;
   const int aj = a.slot_atom[sj];
   const float sjs = a.gbpar[sj].y;
-  int ex = -1;
-  if (!GB_ONLY)
-    for (int e = a.excl_tile_start[I]; e < a.excl_tile_start[I + 1]; e++)
-      if (a.excl_tile_j[e] == J) {
-        ex = a.excl_tile_idx[e];
+  // exclusion rows of this tile pair, if it has any: the lanes search the
+  // i-tile's list of excluded tile partners together, then stage the rows
+  unsigned exrow = 0u;
+  if (!GB_ONLY) {
+    const int e0 = a.excl_tile_start[I], e1 = a.excl_tile_start[I + 1];
+    int ex = -1;
+    for (int e = e0; e < e1; e += 32) {
+      const bool hit = e + lane < e1 && a.excl_tile_j[e + lane] == J;
+      const unsigned bal = __ballot_sync(kFull, hit);
+      if (bal) {
+        ex = a.excl_tile_idx[e + __ffs(bal) - 1];
         break;
       }
+    }
+    if (ex >= 0) exrow = a.excl_masks[static_cast<size_t>(ex) * 32 + lane];
+  }
+  s_ex[w][lane] = exrow;
+  const bool has_ex = __any_sync(kFull, exrow != 0u);
   __syncwarp();
   const unsigned prevA = GB_ONLY ? a.colA[static_cast<size_t>(c) * 32 + lane] : 0u;
   unsigned colA = 0, colB = 0, colC = 0, colE = 0;
@@ -213,7 +233,7 @@ __global__ void k_list_columns(const ListArgs a) {
         in = ddx * ddx + ddy * ddy + ddz * ddz < a.cut2;
       }
       in = in && vj && !(I == J && i >= lane) && !(((frzI >> i) & 1u) && frzj);
-      if (ex >= 0) colE |= ((a.excl_masks[static_cast<size_t>(ex) * 32 + i] >> lane) & 1u) << i;
+      if (has_ex) colE |= ((s_ex[w][i] >> lane) & 1u) << i;
     }
     const float nr = 4.0f * fmaxf(s_s[w][i], sjs) + kListSkin;
     const bool gb = in && r2 < gbb, near = r2 < nr * nr * 1.0001f;
@@ -393,15 +413,15 @@ __global__ void k_list_pad(const ListArgs a) {
     }
     for (int k = lane; k < nch; k += 32) owner[ch0 + k] = I;
   }
-  // lists B and C now reflect the current positions of the systems remade
-  if (!GB_ONLY || a.sys_flagB[a.tile_sys[I]]) a.xb[I * 32 + lane] = a.pos_hi[I * 32 + lane];
+  // lists B and C now reflect the current positions of the tiles remade
+  if (!GB_ONLY || a.tile_flagB[I]) a.xb[I * 32 + lane] = a.pos_hi[I * 32 + lane];
 }
 
 // Clears the list-B flag after a (re)build; launched last.
-__global__ void k_list_done(int *flagB, int *sys_flagB, int nsys) {
+__global__ void k_list_done(int *flagB, int *tile_flagB, int ntile) {
   const int s = blockIdx.x * blockDim.x + threadIdx.x;
   if (s == 0) *flagB = 0;
-  if (s < nsys) sys_flagB[s] = 0;
+  if (s < ntile) tile_flagB[s] = 0;
 }
 
 }  // namespace sffg
