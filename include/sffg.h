@@ -64,6 +64,11 @@ int sffg_batch_create(const char *opts, sffg_batch **out);
  * 3*Natom doubles; frozen may be NULL).  Returns the system index. */
 int sffg_batch_add_system(sffg_batch *b, PARMSTRUCT_T *prm, const int *frozen, const double *x,
                           int *sys_index);
+/* Harmonic positional restraints of one system (the reference's
+ * constrained/x0 arguments of mme_init_sff with the option wcons,
+ * src/sff/eff.c:17-80): atoms with constrained[i] != 0 are held to x0
+ * (3*Natom).  Before finalize; the arrays are copied. */
+int sffg_batch_set_restraints(sffg_batch *b, int sys, const int *constrained, const double *x0);
 /* Uploads topologies and allocates device state; no systems may be added
  * afterwards. */
 int sffg_batch_finalize(sffg_batch *b);

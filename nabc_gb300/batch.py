@@ -25,12 +25,18 @@ class Batch:
         _check(L.sffg_batch_create(opts.encode(), C.byref(self.h)), "sffg_batch_create")
         self.natoms = []
 
-    def add(self, prm, x, frozen=None):
+    def add(self, prm, x, frozen=None, constrained=None, x0=None):
+        """Adds a system; constrained/x0 hold atoms to reference positions
+        with the option wcons."""
         L = sff.lib()
         idx = C.c_int(-1)
         fz = None if frozen is None else sff.iptr(np.ascontiguousarray(frozen, np.int32))
         x = np.ascontiguousarray(x, np.float64)
         _check(L.sffg_batch_add_system(self.h, prm, fz, sff.dptr(x), C.byref(idx)), "add_system")
+        if constrained is not None:
+            c = np.ascontiguousarray(constrained, np.int32)
+            r = np.ascontiguousarray(x0, np.float64)
+            _check(L.sffg_batch_set_restraints(self.h, idx.value, sff.iptr(c), sff.dptr(r)), "set_restraints")
         self.natoms.append(prm.contents.Natom)
         return idx.value
 

@@ -46,6 +46,13 @@ extern "C" int sffg_batch_add_system(sffg_batch *b, PARMSTRUCT_T *prm, const int
   return SFFG_OK;
 }
 
+extern "C" int sffg_batch_set_restraints(sffg_batch *b, int sys, const int *constrained, const double *x0) {
+  if (!b) return fail(SFFG_EINVAL, "null batch");
+  const int rc = b->impl->set_restraints(sys, constrained, x0);
+  if (rc) return fail(rc, "set_restraints: bad system or arrays, or batch already finalized");
+  return SFFG_OK;
+}
+
 extern "C" int sffg_batch_finalize(sffg_batch *b) {
   if (!b) return fail(SFFG_EINVAL, "null batch");
   return pass(b->impl, b->impl->finalize());

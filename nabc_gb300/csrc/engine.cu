@@ -83,6 +83,7 @@ struct DeviceState {
   DBuf<unsigned> step;  // md step number (the Philox counter of the noise)
   DBuf<unsigned long long> sys_key;  // per system: noise key
   DBuf<int> tile_flagB;              // per tile: entries of lists B and C to be remade
+  DBuf<double> cons_w, cons_x0;      // per atom: restraint weight (0: none), reference position
   // CUDA graphs of an evaluation and of an md step without a list rebuild,
   // with the list-buffer pointers they were captured against
   cudaGraphExec_t g_eval = nullptr, g_step = nullptr;
@@ -131,7 +132,7 @@ struct DeviceState {
     rel(cand_start); rel(cand_count); rel(chunksA); rel(chunksB); rel(chunksC); rel(chunk0A);
     rel(chunk0B); rel(chunk0C); rel(chunkA_i); rel(entA_slot); rel(chunkB_i); rel(entB_slot);
     rel(chunkC_i); rel(entC_slot); rel(entA_col); rel(entA_exc); rel(entB_col); rel(entC_col);
-    rel(xb); rel(counters); rel(step); rel(cg_nactive); rel(sys_key); rel(tile_flagB); rel(neck_pos); rel(neck_val); rel(tscal);
+    rel(xb); rel(counters); rel(step); rel(cg_nactive); rel(sys_key); rel(tile_flagB); rel(cons_w); rel(cons_x0); rel(neck_pos); rel(neck_val); rel(tscal);
     rel(noise); rel(rndf); rel(ekin); rel(cg_w); rel(cg_state);
   }
 };
@@ -462,7 +463,8 @@ int Batch::upload() {
   SFFG_CK(d.acc_fz.alloc(nslot_));
   SFFG_CK(d.box_lo.alloc(ntile_));
   SFFG_CK(d.box_hi.alloc(ntile_));
-  SFFG_CK(d.energy.alloc(static_cast<size_t>(nsys) * 8));
+  static_assert(E_NSLOTS == kEnergySlots, "energy slots");
+  SFFG_CK(d.energy.alloc(static_cast<size_t>(nsys) * kEnergySlots));
   SFFG_CK(d.etot.alloc(nsys));
   SFFG_CK(d.grad.alloc(3 * static_cast<size_t>(natom_total_)));
   SFFG_CK(d.v.alloc(3 * static_cast<size_t>(natom_total_)));
@@ -482,6 +484,25 @@ int Batch::upload() {
   SFFG_CK(d.xb.alloc(nslot_));
   SFFG_CK(d.counters.alloc(16));
   SFFG_CK(d.step.alloc(1));
+  {
+    // positional restraints, per atom
+    bool any = false;
+    std::vector<double> w(natom_total_, 0.0), xr(3 * static_cast<size_t>(natom_total_), 0.0);
+    for (int s = 0; s < nsys; s++) {
+      const SystemInfo &si = sys_[s];
+      if (si.constrained.empty()) continue;
+      for (int i = 0; i < si.natom; i++)
+        if (si.constrained[i]) {
+          w[si.atom_off + i] = opts_.wcons;
+          any = any || opts_.wcons != 0.0;
+        }
+      std::copy(si.x0.begin(), si.x0.end(), xr.begin() + 3 * static_cast<size_t>(si.atom_off));
+    }
+    if (any) {
+      SFFG_CK(up(d.cons_w, w));
+      SFFG_CK(up(d.cons_x0, xr));
+    }
+  }
   SFFG_CK(d.tile_flagB.alloc(ntile_));
   SFFG_CK(cudaMemset(d.tile_flagB.p, 0, d.tile_flagB.bytes()));
   {
@@ -616,15 +637,16 @@ static void ene_from_fixed(const long long *e, double *ene) {
   ene[5] = e[E_DIHED] * k;
   ene[7] = e[E_ENB14] * k;
   ene[8] = e[E_EEL14] * k;
+  ene[9] = e[E_CONS] * k;
   ene[10] = e[E_EGB] * k;
   for (int i = 1; i <= 12; i++) ene[0] += ene[i];
 }
 
 int Batch::get_energy(int s, double *ene, void *stream) {
   if (!finalized_ || s < 0 || s >= num_systems()) return SFFG_EINVAL;
-  long long e[8];
+  long long e[kEnergySlots];
   cudaStream_t st = pick(*d_, stream);
-  SFFG_CK(cudaMemcpyAsync(e, d_->energy.p + 8 * s, sizeof(e), cudaMemcpyDeviceToHost, st));
+  SFFG_CK(cudaMemcpyAsync(e, d_->energy.p + kEnergySlots * s, sizeof(e), cudaMemcpyDeviceToHost, st));
   SFFG_CK(cudaStreamSynchronize(st));
   ene_from_fixed(e, ene);
   return SFFG_OK;
@@ -633,12 +655,12 @@ int Batch::get_energy(int s, double *ene, void *stream) {
 int Batch::get_all_energies(std::vector<double> &out, void *stream) {
   if (!finalized_) return SFFG_ESTATE;
   const int nsys = num_systems();
-  std::vector<long long> e(8 * static_cast<size_t>(nsys));
+  std::vector<long long> e(kEnergySlots * static_cast<size_t>(nsys));
   cudaStream_t st = pick(*d_, stream);
   SFFG_CK(cudaMemcpyAsync(e.data(), d_->energy.p, e.size() * sizeof(long long), cudaMemcpyDeviceToHost, st));
   SFFG_CK(cudaStreamSynchronize(st));
   out.resize(13 * static_cast<size_t>(nsys));
-  for (int s = 0; s < nsys; s++) ene_from_fixed(&e[8 * s], &out[13 * s]);
+  for (int s = 0; s < nsys; s++) ene_from_fixed(&e[kEnergySlots * s], &out[13 * s]);
   return SFFG_OK;
 }
 
@@ -1025,6 +1047,10 @@ int Batch::run_eval_direct(bool rebuild, void *stream) {
   if (d.angle_atoms.n) k_angles<<<blocks(d.angle_atoms.n), 128, 0, st>>>(ba, d.angle_atoms.p, d.angle_par.p, static_cast<int>(d.angle_atoms.n));
   if (d.dih_atoms.n) k_dihedrals<<<blocks(d.dih_atoms.n), 128, 0, st>>>(ba, d.dih_atoms.p, d.dih_par.p, static_cast<int>(d.dih_atoms.n));
   if (d.p14_atoms.n) k_pairs14<<<blocks(d.p14_atoms.n), 128, 0, st>>>(ba, d.p14_atoms.p, d.p14_par.p, static_cast<int>(d.p14_atoms.n));
+  if (d.cons_w.n) {
+    k_restraints<<<blocks(d.cons_w.n), 128, 0, st>>>(ba, d.cons_w.p, d.cons_x0.p, static_cast<int>(d.cons_w.n));
+    launches_++;
+  }
   SFFG_CK(cudaGetLastError());
   // pass 1
   const bool neck = mp_.gb == 7 || mp_.gb == 8;
@@ -1306,7 +1332,9 @@ int Batch::md_steps(int step0, int k, NoiseFn noise, void *noise_ctx, void *stre
   for (int i = 1; i <= k; i++) {
     const int nstep = step0 + i;
     const bool rebuild = opts_.nsnb > 0 && nstep % opts_.nsnb == 0;
-    if (!rebuild && !noise && graphs_ok()) {
+    // centre-of-mass motion removal every nscm steps (sff.c:2346-2351)
+    const bool com = opts_.nscm > 0 && nstep % opts_.nscm == 0;
+    if (!rebuild && !noise && !com && graphs_ok()) {
       if ((rc = ensure_tuned(st))) break;
       if ((rc = capture(d.g_step, d.sig_step, d.launches_step, [&](cudaStream_t cs) { return step_body(cs, false, true); })))
         break;
@@ -1315,6 +1343,12 @@ int Batch::md_steps(int step0, int k, NoiseFn noise, void *noise_ctx, void *stre
       timers().nevals++;
     } else if ((rc = step_body(st, rebuild, false))) {
       break;
+    }
+    if (com) {
+      k_com_remove<<<nsys, kComThreads, 0, st>>>(d.x.p, d.v.p, d.minv.p, d.sys_atom_off.p, d.sys_natom.p,
+                                                 d.sys_active.p, a.gammai == 0.0 || opts_.hcp != 0);
+      SFFG_CK(cudaGetLastError());
+      launches_++;
     }
   }
   return rc;
@@ -1676,6 +1710,14 @@ int Batch::cg_poll(int *nactive, std::vector<int> *status, std::vector<double> *
     energy->resize(nsys);
     for (int s = 0; s < nsys; s++) (*energy)[s] = cg_host_[s].f;
   }
+  return SFFG_OK;
+}
+
+int Batch::set_restraints(int sys, const int *constrained, const double *x0) {
+  if (finalized_ || sys < 0 || sys >= num_systems() || !constrained || !x0) return SFFG_EINVAL;
+  SystemInfo &si = sys_[sys];
+  si.constrained.assign(constrained, constrained + si.natom);
+  si.x0.assign(x0, x0 + 3 * static_cast<size_t>(si.natom));
   return SFFG_OK;
 }
 

@@ -42,6 +42,8 @@ struct SystemInfo {
   int ntypes = 0;
   int lj_off = 0;
   unsigned long long noise_key = 0;  // Philox key of the md noise (default: the system index)
+  std::vector<int> constrained;      // positional restraints (econs): flags ...
+  std::vector<double> x0;            // ... and reference positions, 3 per atom
 };
 
 class Batch {
@@ -55,6 +57,9 @@ class Batch {
   int add_system(PARMSTRUCT_T *prm, const int *frozen, const double *x, bool mutate_prm);
   // The same for a topology already converted (build_host_system).
   int add_host_system(HostSystem hs, const double *x);
+  // Harmonic positional restraints of a system (before finalize): atoms with
+  // constrained[i] != 0 are held to x0 with the option wcons.
+  int set_restraints(int sys, const int *constrained, const double *x0);
   // Key of a system's md noise (before finalize); systems with equal keys,
   // topologies and coordinates draw equal noise in any batch.
   int set_noise_key(int sys, unsigned long long key);

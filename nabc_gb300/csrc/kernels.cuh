@@ -20,6 +20,7 @@
 namespace sffg {
 
 constexpr unsigned kFull = 0xffffffffu;
+constexpr int kEnergySlots = 9;  // fixed-point energy terms per system (EnergySlot)
 
 // One compacted pair list (built by lists.cuh).
 struct ChunkList {
@@ -53,7 +54,7 @@ struct DevTables {
   int claim;  // work items a warp takes per grab of the queue (tuned)
   // accumulators
   long long *acc_sumi, *acc_sd, *acc_fx, *acc_fy, *acc_fz;
-  long long *energy;       // nsys * E_NSLOTS
+  long long *energy;       // nsys * kEnergySlots
   // model
   BornConst born;
   PairConst pair;
@@ -420,9 +421,9 @@ __global__ void __launch_bounds__(256, 3) k_gbpair(const DevTables t) {
   auto flush_e = [&]() {
     long long a = warp_sum_ll(ep64), b = warp_sum_ll(ee64), c = warp_sum_ll(ev64);
     if (lane == 0) {
-      atomic_add_ll(&t.energy[cur_sys * 8 + 0], -a);
-      atomic_add_ll(&t.energy[cur_sys * 8 + 1], b);
-      atomic_add_ll(&t.energy[cur_sys * 8 + 2], c);
+      atomic_add_ll(&t.energy[cur_sys * kEnergySlots + 0], -a);
+      atomic_add_ll(&t.energy[cur_sys * kEnergySlots + 1], b);
+      atomic_add_ll(&t.energy[cur_sys * kEnergySlots + 2], c);
     }
     ep64 = ee64 = ev64 = 0;
   };

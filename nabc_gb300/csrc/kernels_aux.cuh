@@ -136,7 +136,7 @@ __global__ void k_born_finish(const FinishArgs a) {
   }
   // a tile never straddles systems, so the warp shares sys
   const long long e = warp_sum_ll(__double2ll_rn(ediag * 4294967296.0));
-  if (lane == 0 && slot < a.nslot) atomic_add_ll(&a.energy[sys * 8 + 0], e);
+  if (lane == 0 && slot < a.nslot) atomic_add_ll(&a.energy[sys * kEnergySlots + 0], e);
 }
 
 // Chain-rule weight of each atom for pass 3 (src/sff/eff.c:2211-2231).
@@ -176,9 +176,9 @@ __device__ __forceinline__ void add_energy(const BondedArgs &a, int sys, int slo
   const int s0 = __shfl_sync(kFull, sys, 0);
   if (__all_sync(kFull, sys == s0 || sys < 0)) {
     const long long t = warp_sum_ll(sys >= 0 ? v : 0);
-    if ((threadIdx.x & 31) == 0 && s0 >= 0) atomic_add_ll(&a.energy[s0 * 8 + slot], t);
+    if ((threadIdx.x & 31) == 0 && s0 >= 0) atomic_add_ll(&a.energy[s0 * kEnergySlots + slot], t);
   } else if (sys >= 0) {
-    atomic_add_ll(&a.energy[sys * 8 + slot], v);
+    atomic_add_ll(&a.energy[sys * kEnergySlots + slot], v);
   }
 }
 
@@ -346,6 +346,121 @@ __global__ void k_pairs14(const BondedArgs a, const int4 *atoms, const double4_3
 
 // Fixed-point forces -> FP64 gradient in the caller's atom order; frozen
 // atoms get zero (src/sff/eff.c:2826-2834).
+// Harmonic positional restraints (src/sff/eff.c:17-80, econs):
+// wcons |x - x0|^2 for every constrained atom; w[atom] = wcons or 0.
+__global__ void k_restraints(const BondedArgs a, const double *w, const double *x0, int natom) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  int sys = -1;
+  double e = 0.0;
+  if (i < natom && w[i] != 0.0) {
+    sys = a.atom_sys[i];
+    if (!a.sys_active[sys]) {
+      sys = -1;
+    } else {
+      const double rx = a.x[3 * i] - x0[3 * i], ry = a.x[3 * i + 1] - x0[3 * i + 1],
+                   rz = a.x[3 * i + 2] - x0[3 * i + 2];
+      e = w[i] * (rx * rx + ry * ry + rz * rz);
+      add_force(a, i, 2. * w[i] * rx, 2. * w[i] * ry, 2. * w[i] * rz);
+    }
+  }
+  add_energy(a, sys, E_CONS, e);
+}
+
+// Centre-of-mass motion removal of md (src/sff/com.c:10-47 and 53-147,
+// called every nscm steps at sff.c:2347-2351): one block per system moves
+// the centre of mass to the origin and, with also_v, removes the
+// centre-of-mass velocity and the rigid rotation (angular momentum over the
+// inertia tensor, both scaled by 1e-3 as the reference does).
+constexpr int kComThreads = 256;
+
+__device__ double block_sum(double v, double *sh) {
+  const int t = threadIdx.x;
+  sh[t] = v;
+  __syncthreads();
+  for (int o = blockDim.x / 2; o > 0; o >>= 1) {
+    if (t < o) sh[t] += sh[t + o];
+    __syncthreads();
+  }
+  const double r = sh[0];
+  __syncthreads();
+  return r;
+}
+
+__global__ void __launch_bounds__(kComThreads) k_com_remove(double *x, double *v, const double *minv,
+                                                             const int *sys_atom_off, const int *sys_natom,
+                                                             const int *sys_active, int also_v) {
+  __shared__ double sh[kComThreads];
+  const int s = blockIdx.x;
+  if (!sys_active[s]) return;
+  const int a0 = sys_atom_off[s], n = sys_natom[s];
+  double m = 0, mx = 0, my = 0, mz = 0;
+  for (int k = threadIdx.x; k < n; k += blockDim.x) {
+    const int i = 3 * (a0 + k);
+    const double mi = 1. / minv[i];
+    m += mi;
+    mx += x[i] * mi;
+    my += x[i + 1] * mi;
+    mz += x[i + 2] * mi;
+  }
+  const double mt = block_sum(m, sh);
+  const double xs = block_sum(mx, sh) / mt, ys = block_sum(my, sh) / mt, zs = block_sum(mz, sh) / mt;
+  for (int k = threadIdx.x; k < n; k += blockDim.x) {
+    const int i = 3 * (a0 + k);
+    x[i] -= xs;
+    x[i + 1] -= ys;
+    x[i + 2] -= zs;
+  }
+  if (!also_v) return;
+  __syncthreads();
+  double px = 0, py = 0, pz = 0;
+  for (int k = threadIdx.x; k < n; k += blockDim.x) {
+    const int i = 3 * (a0 + k);
+    const double mi = 1. / minv[i];
+    px += v[i] * mi;
+    py += v[i + 1] * mi;
+    pz += v[i + 2] * mi;
+  }
+  const double vx = block_sum(px, sh) / mt, vy = block_sum(py, sh) / mt, vz = block_sum(pz, sh) / mt;
+  constexpr double kScale = 1.e-3;
+  double l[3] = {0, 0, 0}, in[6] = {0, 0, 0, 0, 0, 0};  // xx xy xz yy yz zz
+  for (int k = threadIdx.x; k < n; k += blockDim.x) {
+    const int i = 3 * (a0 + k);
+    v[i] -= vx;
+    v[i + 1] -= vy;
+    v[i + 2] -= vz;
+    const double mi = 1. / minv[i], X = x[i], Y = x[i + 1], Z = x[i + 2];
+    l[0] += kScale * (Y * v[i + 2] - Z * v[i + 1]) * mi;
+    l[1] += kScale * (Z * v[i] - X * v[i + 2]) * mi;
+    l[2] += kScale * (X * v[i + 1] - Y * v[i]) * mi;
+    in[0] += X * X * mi;
+    in[1] += X * Y * mi;
+    in[2] += X * Z * mi;
+    in[3] += Y * Y * mi;
+    in[4] += Y * Z * mi;
+    in[5] += Z * Z * mi;
+  }
+  double L[3], M[6];
+  for (int c = 0; c < 3; c++) L[c] = block_sum(l[c], sh);
+  for (int c = 0; c < 6; c++) M[c] = block_sum(in[c], sh);
+  // inertia tensor and its inverse by cofactors (com.c:107-118, 150-175)
+  const double I0 = (M[3] + M[5]) * kScale, I1 = -M[1] * kScale, I2 = -M[2] * kScale;
+  const double I4 = (M[0] + M[5]) * kScale, I5 = -M[4] * kScale, I8 = (M[0] + M[3]) * kScale;
+  const double c0 = I4 * I8 - I5 * I5, c1 = I1 * I8 - I5 * I2, c2 = I1 * I5 - I4 * I2;
+  const double c4 = I0 * I8 - I2 * I2, c5 = I0 * I5 - I1 * I2, c8 = I0 * I4 - I1 * I1;
+  const double det = I0 * c0 - I1 * c1 + I2 * c2;
+  // the symmetric inverse: [c0 -c1 c2; -c1 c4 -c5; c2 -c5 c8] / det
+  const double ox = (c0 * L[0] - c1 * L[1] + c2 * L[2]) / det;
+  const double oy = (-c1 * L[0] + c4 * L[1] - c5 * L[2]) / det;
+  const double oz = (c2 * L[0] - c5 * L[1] + c8 * L[2]) / det;
+  for (int k = threadIdx.x; k < n; k += blockDim.x) {
+    const int i = 3 * (a0 + k);
+    const double X = x[i], Y = x[i + 1], Z = x[i + 2];
+    v[i] = v[i] - oy * Z + oz * Y;
+    v[i + 1] = v[i + 1] - oz * X + ox * Z;
+    v[i + 2] = v[i + 2] - ox * Y + oy * X;
+  }
+}
+
 __global__ void k_gather_grad(const long long *acc_fx, const long long *acc_fy, const long long *acc_fz,
                               const int *atom_slot, const int *atom_frozen, const int *atom_sys,
                               const int *sys_active, double *grad, int natom) {
@@ -365,7 +480,7 @@ __global__ void k_energy_total(const long long *energy, double *etot, int nsys) 
   const int s = blockIdx.x * blockDim.x + threadIdx.x;
   if (s >= nsys) return;
   const double k = 1.0 / 4294967296.0;
-  const long long *e = energy + s * 8;
+  const long long *e = energy + s * kEnergySlots;
   double ene[13] = {0};
   ene[1] = e[E_EVDW] * k;
   ene[2] = e[E_EEL] * k;
@@ -374,6 +489,7 @@ __global__ void k_energy_total(const long long *energy, double *etot, int nsys) 
   ene[5] = e[E_DIHED] * k;
   ene[7] = e[E_ENB14] * k;
   ene[8] = e[E_EEL14] * k;
+  ene[9] = e[E_CONS] * k;
   ene[10] = e[E_EGB] * k;
   double t = 0.0;
   for (int i = 1; i <= 12; i++) t += ene[i];

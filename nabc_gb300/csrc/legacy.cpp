@@ -23,6 +23,8 @@ namespace {
 struct Session {
   PARMSTRUCT_T *prm = nullptr;
   int *frozen = nullptr;
+  int *constrained = nullptr;  // borrowed with x0, as the reference does (sff.c:886)
+  double *x0 = nullptr;
   std::unique_ptr<Batch> batch;
   int natom = 0;
   bool list_built = false;
@@ -182,8 +184,6 @@ extern "C" REAL_T mme(REAL_T *x, REAL_T *f, INT_T *iter);
 using namespace sffg;
 
 extern "C" INT_T mme_init_sff(PARMSTRUCT_T *prm, INT_T *frozen, INT_T *constrained, REAL_T *x0, STRING_T *ncname) {
-  (void)constrained;
-  (void)x0;
   (void)ncname;
   const double t0 = wall_seconds();
   Session &s = session();
@@ -198,9 +198,18 @@ extern "C" INT_T mme_init_sff(PARMSTRUCT_T *prm, INT_T *frozen, INT_T *constrain
     std::fprintf(legacy_out(), "Error in egb: rgbmax = %f is greater than cutoff = %f\n", o.rgbmax, o.cut);
     std::exit(1);
   }
+  // positional restraints (src/sff/sff.c:1169-1178): counted and reported
+  // here, applied from the first mme() on
+  s.constrained = nullptr;
+  s.x0 = x0;
   if (constrained) {
-    for (int i = 0; i < prm->Natom; i++)
-      if (constrained[i]) fatal("positional constraints are not supported on the device path");
+    int nc = 0;
+    for (int i = 0; i < prm->Natom; i++) nc += constrained[i] != 0;
+    if (nc) {
+      std::fprintf(legacy_out(), "constrained %d atoms from input array\n", nc);
+      if (!x0) fatal("constrained atoms need the reference positions x0");
+      s.constrained = constrained;
+    }
   }
   // Validate and apply the reference's in-place changes to prm (charges
   // scaled by 1/sqrt(dielc), gb=7/8 screening factors); the device copy is
@@ -224,6 +233,7 @@ void ensure_finalized(const double *x) {
   Batch &b = require_batch();
   if (!b.finalized()) {
     if (b.add_system(s.prm, s.frozen, x, false) < 0) fatal("mme: " + b.last_error);
+    if (s.constrained) b.set_restraints(0, s.constrained, s.x0);
     const int rc = b.finalize();
     if (rc) fatal("mme: device setup failed: " + b.last_error);
   }
@@ -250,8 +260,74 @@ extern "C" REAL_T mme(REAL_T *x, REAL_T *f, INT_T *iter) {
 
 namespace {
 
+// Centre-of-mass motion removal (src/sff/com.c:10-147): translation to the
+// origin and, with also_v, the centre-of-mass velocity and rigid rotation.
+void com_remove_host(int n, double *x, double *v, const double *minv, bool also_v) {
+  double mt = 0, xs = 0, ys = 0, zs = 0;
+  for (int i = 0; i < n / 3; i++) mt += 1. / minv[3 * i];
+  for (int i = 0; i < n / 3; i++) {
+    xs += x[3 * i] / minv[3 * i];
+    ys += x[3 * i + 1] / minv[3 * i + 1];
+    zs += x[3 * i + 2] / minv[3 * i + 2];
+  }
+  xs /= mt;
+  ys /= mt;
+  zs /= mt;
+  for (int i = 0; i < n / 3; i++) {
+    x[3 * i] -= xs;
+    x[3 * i + 1] -= ys;
+    x[3 * i + 2] -= zs;
+  }
+  if (!also_v) return;
+  double vx = 0, vy = 0, vz = 0;
+  for (int i = 0; i < n / 3; i++) {
+    vx += v[3 * i] / minv[3 * i];
+    vy += v[3 * i + 1] / minv[3 * i + 1];
+    vz += v[3 * i + 2] / minv[3 * i + 2];
+  }
+  vx /= mt;
+  vy /= mt;
+  vz /= mt;
+  for (int i = 0; i < n / 3; i++) {
+    v[3 * i] -= vx;
+    v[3 * i + 1] -= vy;
+    v[3 * i + 2] -= vz;
+  }
+  const double sc = 1.e-3;
+  double L[3] = {0, 0, 0}, M[6] = {0, 0, 0, 0, 0, 0};
+  for (int i = 0; i < n / 3; i++) {
+    const double m = 1. / minv[3 * i], X = x[3 * i], Y = x[3 * i + 1], Z = x[3 * i + 2];
+    L[0] += sc * (Y * v[3 * i + 2] - Z * v[3 * i + 1]) * m;
+    L[1] += sc * (Z * v[3 * i] - X * v[3 * i + 2]) * m;
+    L[2] += sc * (X * v[3 * i + 1] - Y * v[3 * i]) * m;
+  }
+  for (int i = 0; i < n / 3; i++) {
+    const double m = 1. / minv[3 * i], X = x[3 * i], Y = x[3 * i + 1], Z = x[3 * i + 2];
+    M[0] += X * X * m;
+    M[1] += X * Y * m;
+    M[2] += X * Z * m;
+    M[3] += Y * Y * m;
+    M[4] += Y * Z * m;
+    M[5] += Z * Z * m;
+  }
+  const double I0 = (M[3] + M[5]) * sc, I1 = -M[1] * sc, I2 = -M[2] * sc;
+  const double I4 = (M[0] + M[5]) * sc, I5 = -M[4] * sc, I8 = (M[0] + M[3]) * sc;
+  const double c0 = I4 * I8 - I5 * I5, c1 = I1 * I8 - I5 * I2, c2 = I1 * I5 - I4 * I2;
+  const double c4 = I0 * I8 - I2 * I2, c5 = I0 * I5 - I1 * I2, c8 = I0 * I4 - I1 * I1;
+  const double det = I0 * c0 - I1 * c1 + I2 * c2;
+  const double ox = (c0 * L[0] - c1 * L[1] + c2 * L[2]) / det;
+  const double oy = (-c1 * L[0] + c4 * L[1] - c5 * L[2]) / det;
+  const double oz = (c2 * L[0] - c5 * L[1] + c8 * L[2]) / det;
+  for (int i = 0; i < n / 3; i++) {
+    const double X = x[3 * i], Y = x[3 * i + 1], Z = x[3 * i + 2];
+    v[3 * i] = v[3 * i] - oy * Z + oz * Y;
+    v[3 * i + 1] = v[3 * i + 1] - oz * X + ox * Z;
+    v[3 * i + 2] = v[3 * i + 2] - ox * Y + oy * X;
+  }
+}
+
 // The reference's md() loop on the host around an arbitrary energy
-// function (src/sff/sff.c:2071-2366, without RATTLE and COM removal).
+// function (src/sff/sff.c:2071-2366, without RATTLE).
 int md_host(int n, int maxstep, double *x, double *f, double *v, REAL_T (*func)(REAL_T *, REAL_T *, INT_T *)) {
   Session &s = session();
   const Options &o = options();
@@ -323,6 +399,7 @@ int md_host(int n, int maxstep, double *x, double *f, double *v, REAL_T (*func)(
                    ekin + epot, ekin / (boltz2 * rndf));
       std::fflush(legacy_out());
     }
+    if (o.nscm > 0 && nstep % o.nscm == 0) com_remove_host(n, x, v, minv.data(), gammai == 0.0 || o.hcp);
   }
   options().t = t;
   nstep = -3;

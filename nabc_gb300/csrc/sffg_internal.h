@@ -101,7 +101,7 @@ constexpr double kBornScale = 1099511627776.0;    // 2^40 per 1/A
 constexpr double kSumdScale = 4294967296.0;       // 2^32
 
 // Per-system energy slots kept in fixed point on the device.
-enum EnergySlot { E_EGB = 0, E_EEL, E_EVDW, E_BOND, E_ANGLE, E_DIHED, E_EEL14, E_ENB14, E_NSLOTS };
+enum EnergySlot { E_EGB = 0, E_EEL, E_EVDW, E_BOND, E_ANGLE, E_DIHED, E_EEL14, E_ENB14, E_CONS, E_NSLOTS };
 
 // ---------------------------------------------------------------- timing
 struct Timers {

@@ -97,6 +97,7 @@ def lib():
         L.sffg_batch_create.argtypes = [C.c_char_p, C.POINTER(vp)]
         L.sffg_batch_add_system.argtypes = [vp, PRM_P, INT_P, REAL_P, INT_P]
         L.sffg_batch_finalize.argtypes = [vp]
+        L.sffg_batch_set_restraints.argtypes = [vp, C.c_int, INT_P, REAL_P]
         L.sffg_batch_num_systems.argtypes = [vp]
         L.sffg_batch_num_atoms.argtypes = [vp, C.c_int]
         for name in ("set_coords", "get_coords", "get_grad", "get_reff", "set_velocities",

@@ -18,7 +18,8 @@ class Opts(C.Structure):
     _fields_ = [(n, C.c_double) for n in ("cut", "rgbmax", "kappa", "epsext", "dielc")] + \
                [(n, C.c_int) for n in ("gb", "nsnb", "ntpr")] + \
                [(n, C.c_double) for n in ("dt", "temp0", "tempi", "gamma_ln", "tautp", "vlimit")] + \
-               [(n, C.c_int) for n in ("zerov", "ntpr_md")]
+               [(n, C.c_int) for n in ("zerov", "ntpr_md")] + \
+               [("wcons", C.c_double), ("nscm", C.c_int)]
 
 
 _lib = None
@@ -46,6 +47,7 @@ def lib():
         L.sffo_conjgrad.argtypes = [C.c_void_p, REAL_P, REAL_P, C.c_double, C.c_double, C.c_int,
                                     REAL_P, INT_P]
         L.sffo_gauss_stream.argtypes = [INT_P, C.c_int, C.c_double, REAL_P, REAL_P]
+        L.sffo_set_restraints.argtypes = [C.c_void_p, INT_P, REAL_P]
         _lib = L
     return _lib
 
@@ -70,7 +72,7 @@ def parse_opts(text):
             i += 2
         if key == "diel":
             continue
-        if key in ("gb", "nsnb", "ntpr", "zerov", "ntpr_md"):
+        if key in ("gb", "nsnb", "ntpr", "zerov", "ntpr_md", "nscm"):
             setattr(o, key, int(val))
         elif key in dict(Opts._fields_):
             setattr(o, key, float(val))
@@ -106,6 +108,11 @@ class Oracle:
 
     def npairs(self):
         return lib().sffo_npairs(self.h)
+
+    def set_restraints(self, constrained, x0):
+        c = np.ascontiguousarray(constrained, np.int32)
+        x0 = np.ascontiguousarray(x0, np.float64)
+        lib().sffo_set_restraints(self.h, c.ctypes.data_as(INT_P), _p(x0))
 
     def conjgrad(self, x, rmsgrad, dfpred, maxiter):
         x = np.array(x, np.float64)

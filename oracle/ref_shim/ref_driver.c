@@ -9,6 +9,10 @@
  *   cg  <maxiter> <dfpred> <rmsgrad> [out.bin]   conjgrad() driven by mme
  *   md  <nsteps> [out.bin]            md() driven by mme
  *   time <nevals>                     repeated quiet mme() evaluations
+ *   spc <every> <out.bin>             single point with atoms 0, every, 2 every,
+ *                                     ... restrained (option wcons) to the
+ *                                     input positions shifted by
+ *                                     0.05 ((3 i + k) mod 5 - 2) A per coordinate
  *
  * Coordinates come from a PDB (columns 31-54 of ATOM/HETATM records, the
  * order the prmtop uses) or an Amber ASCII restart read with getxv().
@@ -94,9 +98,21 @@ int main(int argc, char **argv)
   mm_options(argv[4]);
   frozen = calloc((size_t)natom, sizeof(int));
   constrained = calloc((size_t)natom, sizeof(int));
+  mode = argv[3];
+  if (strcmp(mode, "spc") == 0) {
+    int every = atoi(argv[5]), i;
+    double *x0 = calloc((size_t)n3, sizeof(double));
+    for (i = 0; i < n3; i++) x0[i] = x[i] + 0.05 * (double)(i % 5 - 2);
+    for (i = 0; i < natom; i += every) constrained[i] = 1;
+    mme_init_sff(prm, frozen, constrained, x0, NULL);
+    iter = -1;
+    e = mme(x, g, &iter);
+    printf("oracle_total: %.17g\n", e);
+    dump(argc > 6 ? argv[6] : NULL, natom, e, x, g);
+    return 0;
+  }
   mme_init_sff(prm, frozen, constrained, NULL, NULL);
 
-  mode = argv[3];
   if (strcmp(mode, "sp") == 0) {
     iter = -1;
     e = mme(x, g, &iter);

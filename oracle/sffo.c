@@ -47,6 +47,9 @@ struct sffo_session {
   int have_list;
   /* scratch */
   double *reff, *psi, *sumdeijda;
+  /* positional restraints (src/sff/sff.c:100, 1169-1178) */
+  int *constrained;
+  double *x0;
   /* gauss2 state (src/sff/rand2.c:22-25) */
   int rng_seed2, rng_iy, rng_iv[32], rng_seed3;
 };
@@ -70,6 +73,8 @@ void sffo_default_opts(sffo_opts *o)
   o->vlimit = 10.0;
   o->zerov = 0;
   o->ntpr_md = 10;
+  o->wcons = 0.0;
+  o->nscm = 0;
 }
 
 static void *xcalloc(size_t n, size_t sz)
@@ -202,7 +207,92 @@ void sffo_destroy(sffo_session *s)
   free(s->neck); free(s->frozen); free(s->ex_start); free(s->ex_atoms); free(s->n14_start);
   free(s->n14_atoms); free(s->n14_scee); free(s->n14_scnb); free(s->pl_start); free(s->pl_low);
   free(s->pl_up); free(s->pl_atoms); free(s->reff); free(s->psi); free(s->sumdeijda);
+  free(s->constrained); free(s->x0);
   free(s);
+}
+
+void sffo_set_restraints(sffo_session *s, const int *constrained, const double *x0)
+{
+  free(s->constrained);
+  free(s->x0);
+  s->constrained = xcalloc(s->n, sizeof(int));
+  s->x0 = xcalloc(3 * (size_t)s->n, sizeof(double));
+  memcpy(s->constrained, constrained, s->n * sizeof(int));
+  memcpy(s->x0, x0, 3 * (size_t)s->n * sizeof(double));
+}
+
+/* Harmonic positional restraints: src/sff/eff.c:17-80 (econs). */
+static double econs(const sffo_session *s, const double *x, double *g)
+{
+  double e = 0.0;
+  int i;
+  if (!s->constrained) return 0.0;
+  for (i = 0; i < s->n; i++) {
+    if (!s->constrained[i]) continue;
+    const double rx = x[3 * i] - s->x0[3 * i], ry = x[3 * i + 1] - s->x0[3 * i + 1],
+                 rz = x[3 * i + 2] - s->x0[3 * i + 2];
+    e += s->o.wcons * (rx * rx + ry * ry + rz * rz);
+    g[3 * i] += 2. * s->o.wcons * rx;
+    g[3 * i + 1] += 2. * s->o.wcons * ry;
+    g[3 * i + 2] += 2. * s->o.wcons * rz;
+  }
+  return e;
+}
+
+/* Centre-of-mass motion removal: src/sff/com.c:10-47 (com2zero) and, with
+ * also_v, 53-147 (com_vw2zero, with the cofactor inverse of com_psinv). */
+static void com_remove(int n, double *x, double *v, const double *minv, int also_v)
+{
+  double mt = 0, xs = 0, ys = 0, zs = 0, vx = 0, vy = 0, vz = 0, L[3] = {0, 0, 0}, M[6] = {0, 0, 0, 0, 0, 0};
+  const double sc = 1.e-3;
+  int i;
+  for (i = 0; i < n; i++) mt += 1. / minv[3 * i];
+  for (i = 0; i < n; i++) {
+    xs += x[3 * i] / minv[3 * i];
+    ys += x[3 * i + 1] / minv[3 * i + 1];
+    zs += x[3 * i + 2] / minv[3 * i + 2];
+  }
+  xs /= mt; ys /= mt; zs /= mt;
+  for (i = 0; i < n; i++) {
+    x[3 * i] -= xs; x[3 * i + 1] -= ys; x[3 * i + 2] -= zs;
+  }
+  if (!also_v) return;
+  for (i = 0; i < n; i++) {
+    vx += v[3 * i] / minv[3 * i];
+    vy += v[3 * i + 1] / minv[3 * i + 1];
+    vz += v[3 * i + 2] / minv[3 * i + 2];
+  }
+  vx /= mt; vy /= mt; vz /= mt;
+  for (i = 0; i < n; i++) {
+    v[3 * i] -= vx; v[3 * i + 1] -= vy; v[3 * i + 2] -= vz;
+  }
+  for (i = 0; i < n; i++) {
+    const double m = 1. / minv[3 * i], X = x[3 * i], Y = x[3 * i + 1], Z = x[3 * i + 2];
+    L[0] += sc * (Y * v[3 * i + 2] - Z * v[3 * i + 1]) * m;
+    L[1] += sc * (Z * v[3 * i] - X * v[3 * i + 2]) * m;
+    L[2] += sc * (X * v[3 * i + 1] - Y * v[3 * i]) * m;
+  }
+  for (i = 0; i < n; i++) {
+    const double m = 1. / minv[3 * i], X = x[3 * i], Y = x[3 * i + 1], Z = x[3 * i + 2];
+    M[0] += X * X * m; M[1] += X * Y * m; M[2] += X * Z * m;
+    M[3] += Y * Y * m; M[4] += Y * Z * m; M[5] += Z * Z * m;
+  }
+  {
+    const double I0 = (M[3] + M[5]) * sc, I1 = -M[1] * sc, I2 = -M[2] * sc;
+    const double I4 = (M[0] + M[5]) * sc, I5 = -M[4] * sc, I8 = (M[0] + M[3]) * sc;
+    const double c0 = I4 * I8 - I5 * I5, c1 = I1 * I8 - I5 * I2, c2 = I1 * I5 - I4 * I2;
+    const double c4 = I0 * I8 - I2 * I2, c5 = I0 * I5 - I1 * I2, c8 = I0 * I4 - I1 * I1;
+    const double det = I0 * c0 - I1 * c1 + I2 * c2;
+    const double ox = (c0 * L[0] - c1 * L[1] + c2 * L[2]) / det;
+    const double oy = (-c1 * L[0] + c4 * L[1] - c5 * L[2]) / det;
+    const double oz = (c2 * L[0] - c5 * L[1] + c8 * L[2]) / det;
+    for (i = 0; i < n; i++) {
+      const double X = x[3 * i], Y = x[3 * i + 1], Z = x[3 * i + 2];
+      v[3 * i] = v[3 * i] - oy * Z + oz * Y;
+      v[3 * i + 1] = v[3 * i + 1] - oz * X + ox * Z;
+      v[3 * i + 2] = v[3 * i + 2] - ox * Y + oy * X;
+    }
+  }
 }
 
 long sffo_npairs(const sffo_session *s) { return s->npairs; }
@@ -705,6 +795,7 @@ double sffo_mme(sffo_session *s, const double *x, double *g, double *ene, double
   nb14(s, x, g, &enb14, &eel14);
   e[7] = enb14;
   e[8] = eel14;
+  e[9] = econs(s, x, g); /* eff.c:2663-2680 */
   egbv = egb(s, x, g, &enb, &eel);
   e[1] = enb;
   e[2] = eel;
@@ -876,6 +967,8 @@ int sffo_md(sffo_session *s, int maxstep, double *x, double *f, double *v, int *
       trace[2 * (nstep - 1)] = ekin;
       trace[2 * (nstep - 1) + 1] = epot;
     }
+    /* sff.c:2346-2351 */
+    if (s->o.nscm > 0 && nstep % s->o.nscm == 0) com_remove(s->n, x, v, minv, gammai == 0.0);
   }
   *seed = s->rng_seed3;
   free(minv);

@@ -23,6 +23,8 @@ typedef struct sffo_opts {
   int gb, nsnb, ntpr;
   double dt, temp0, tempi, gamma_ln, tautp, vlimit;
   int zerov, ntpr_md;
+  double wcons;   /* restraint weight (econs, src/sff/eff.c:17) */
+  int nscm;       /* md: centre-of-mass motion removal period (sff.c:2347) */
 } sffo_opts;
 
 typedef struct sffo_session sffo_session;
@@ -41,6 +43,11 @@ void sffo_destroy(sffo_session *s);
  * receives the effective Born radii. */
 double sffo_mme(sffo_session *s, const double *x, double *g, double *ene, double *reff,
                 int rebuild);
+
+/* Harmonic positional restraints: atoms with constrained[i] != 0 are held
+ * to x0 (3 per atom) with weight opts.wcons (src/sff/eff.c:17-80).  Both
+ * arrays are copied. */
+void sffo_set_restraints(sffo_session *s, const int *constrained, const double *x0);
 
 /* Number of unordered pairs on the current pair list. */
 long sffo_npairs(const sffo_session *s);

@@ -179,6 +179,26 @@ def main():
                          "nsteps": 20, "md": md_lines}
     arrays["s300_md_x"] = x
     arrays["s300_md_v"] = v
+    # md with centre-of-mass removal: Langevin (translation only) and
+    # Berendsen from tempi velocities (translation, velocity and rotation)
+    for name, opts in (("s300_md_nscm", "gb=5, cut=999.0, rgbmax=15.0, ntpr=10, gamma_ln=5.0, temp0=300.0, "
+                                        "dt=0.001, ntpr_md=1, zerov=1, nscm=4"),
+                       ("s300_md_nscm_vw", "gb=5, cut=999.0, rgbmax=15.0, ntpr=10, gamma_ln=0.0, temp0=300.0, "
+                                           "tempi=300.0, tautp=0.2, dt=0.001, ntpr_md=1, nscm=3")):
+        out = run([SFFREF, base + ".parm7", base + ".rst7", "md", opts, "20", tmp])
+        n, e, x, v = read_dump(tmp)
+        md_lines = [[float(t) for t in line.split()[1:]] for line in out.splitlines() if line.startswith("md:")]
+        checks[name] = {"prmtop": "n300_s11.parm7", "coords": "n300_s11.rst7", "options": opts,
+                        "nsteps": 20, "md": md_lines}
+        arrays[f"{name}_x"] = x
+        arrays[f"{name}_v"] = v
+    # positional restraints (econs): every 7th atom held to shifted positions
+    opts = "gb=5, cut=999.0, rgbmax=15.0, ntpr=1, wcons=2.5"
+    out = run([SFFREF, base + ".parm7", base + ".rst7", "spc", opts, "7", tmp])
+    n, e, x, g = read_dump(tmp)
+    checks["s300_cons"] = {"prmtop": "n300_s11.parm7", "coords": "n300_s11.rst7", "options": opts,
+                           "every": 7, "shift": 0.05, "sp": parse_breakdown(out), "energy": e}
+    arrays["s300_cons_g"] = g
     os.remove(tmp)
     with open(os.path.join(HERE, "checks.json"), "w") as f:
         json.dump(checks, f, indent=1)

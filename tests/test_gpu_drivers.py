@@ -150,3 +150,54 @@ def test_autotuned_split_bit_identical(lib):
     for claim, blocks in res[1][2]:
         assert claim in (1, 2, 4, 8) and blocks > 0
     sff.free_prm(prm)
+
+
+def test_positional_restraints(lib, oracle_mod, checks, refrun):
+    """econs on the device, through the batch API and through mme_init_sff's
+    constrained/x0 arguments, against the reference's run."""
+    from nabc_gb300 import sff
+    from nabc_gb300.batch import Batch
+    from test_oracle_golden import restraint_inputs
+    c = checks["s300_cons"]
+    prm, x = load_case(c)
+    cons, x0 = restraint_inputs(c, x)
+    b = Batch(c["options"])
+    b.add(prm, x, constrained=cons, x0=x0)
+    b.finalize()
+    b.eval(rebuild=True)
+    ene, g = b.energy(0), b.grad(0)
+    b.close()
+    assert ene[9] == pytest.approx(c["sp"]["econs"], abs=1e-8)
+    assert abs(ene[0] - c["energy"]) <= 1e-6 * abs(c["energy"])
+    assert np.sqrt(((g - refrun["s300_cons_g"]) ** 2).mean()) <= 1e-5
+    L = sff.lib()
+    L.sffg_options_reset()
+    L.mm_options(c["options"].encode())
+    frozen = np.zeros(len(cons), np.int32)
+    L.mme_init_sff(prm, sff.iptr(frozen), sff.iptr(cons), sff.dptr(x0), None)
+    gl = np.zeros_like(x)
+    it = C.c_int(-1)
+    e = L.mme(sff.dptr(x), sff.dptr(gl), C.byref(it))
+    assert abs(e - c["energy"]) <= 1e-6 * abs(c["energy"])
+    assert np.sqrt(((gl - refrun["s300_cons_g"]) ** 2).mean()) <= 1e-5
+
+
+@pytest.mark.parametrize("name", ["s300_md_nscm", "s300_md_nscm_vw"])
+def test_legacy_md_centre_of_mass_removal(lib, checks, refrun, name):
+    """md(..., mme) with nscm on the device tracks the reference trajectory
+    (translation removal under Langevin; translation, velocity and rotation
+    under Berendsen from tempi velocities)."""
+    from nabc_gb300 import sff
+    c = checks[name]
+    prm, x = load_case(c)
+    session = sff.Session(prm, c["options"])
+    L = sff.lib()
+    seed = C.c_int(-1)
+    L.setseed(C.byref(seed))
+    n = 3 * prm.contents.Natom
+    v = np.zeros(n)
+    f = np.zeros(n)
+    L.md(n, c["nsteps"], sff.dptr(x), sff.dptr(f), sff.dptr(v), C.cast(L.mme, C.c_void_p))
+    assert np.abs(x - refrun[f"{name}_x"]).max() < 1e-5
+    assert np.abs(v - refrun[f"{name}_v"]).max() < 1e-4
+    del session

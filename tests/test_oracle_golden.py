@@ -83,3 +83,37 @@ def test_planted_error_is_detected(lib, oracle_mod, checks, refrun):
     o = oracle_mod.Oracle(prm, c["options"].replace("rgbmax=15.0", "rgbmax=15.15"))
     e, ene, g, reff = o.mme(x)
     assert abs(ene[10] - c["sp"]["egb"]) / abs(c["sp"]["egb"]) > 1e-6
+
+
+@pytest.mark.parametrize("name", ["s300_md_nscm", "s300_md_nscm_vw"])
+def test_md_centre_of_mass_removal(lib, oracle_mod, checks, refrun, name):
+    """md with nscm: the reference removes the centre-of-mass translation
+    (Langevin) and also its velocity and rotation (Berendsen, tempi start)."""
+    c = checks[name]
+    prm, x = load_case(c)
+    o = oracle_mod.Oracle(prm, c["options"])
+    xo, vo, trace = o.md(x, np.zeros_like(x), c["nsteps"], seed=-1)
+    assert np.abs(xo - refrun[f"{name}_x"]).max() < 1e-9
+    assert np.abs(vo - refrun[f"{name}_v"]).max() < 1e-9
+    md = np.array(c["md"])
+    assert trace[:, 0] == pytest.approx(md[:, 2], abs=0.006)
+
+
+def restraint_inputs(c, x):
+    n = len(x) // 3
+    constrained = np.zeros(n, np.int32)
+    constrained[::c["every"]] = 1
+    x0 = x + c["shift"] * (np.arange(3 * n) % 5 - 2)
+    return constrained, x0
+
+
+def test_positional_restraints(lib, oracle_mod, checks, refrun):
+    """econs: the restraint energy and gradient of the reference (eff.c:17)."""
+    c = checks["s300_cons"]
+    prm, x = load_case(c)
+    o = oracle_mod.Oracle(prm, c["options"])
+    o.set_restraints(*restraint_inputs(c, x))
+    e, ene, g, _ = o.mme(x)
+    assert ene[9] == pytest.approx(c["sp"]["econs"], abs=1e-9)
+    assert e == pytest.approx(c["energy"], rel=1e-12)
+    assert np.abs(g - refrun["s300_cons_g"]).max() < 1e-8
