@@ -107,6 +107,13 @@ INT_T conjgrad(REAL_T *x, INT_T *n, REAL_T *f,
 /* Print the timing summary (src/sff/sff.h:149, src/sff/timer.c:71). */
 INT_T mme_timer(void);
 
+/* mme() of a structure whose bond lengths RATTLE first restores (rattle=1:
+ * all bonds, rattle=2: bonds to hydrogen), with the gradient projected onto
+ * the constraints (src/sff/sff.h:147, sff.c:1882-2010).  md() applies the
+ * same constraints after each drift and kick when the rattle option is
+ * set (sff.c:2251-2280). */
+REAL_T mme_rattle(REAL_T *x, REAL_T *f, INT_T *iter);
+
 /* parm7 reader, writer and release (src/sff/sff.h:178-180, prm.c:584,
  * prm.c:1997, prm.c:2810). */
 PARMSTRUCT_T *rdparm(STRING_T *name);

@@ -258,6 +258,10 @@ extern "C" REAL_T mme(REAL_T *x, REAL_T *f, INT_T *iter) {
   return e;
 }
 
+// mme() on a structure whose bond lengths RATTLE first restores, with the
+// gradient projected onto the constraints (src/sff/sff.c:1882-2010).
+extern "C" REAL_T mme_rattle(REAL_T *x, REAL_T *f, INT_T *iter);
+
 namespace {
 
 // Centre-of-mass motion removal (src/sff/com.c:10-147): translation to the
@@ -326,8 +330,95 @@ void com_remove_host(int n, double *x, double *v, const double *minv, bool also_
   }
 }
 
+// Bond-length constraints (RATTLE, src/sff/rattle.c, following TINKER):
+// Gauss-Seidel sweeps over the bonds to hydrogen and, with rattle=1, the
+// other bonds, in the topology's order, correcting each bond in turn
+// (over-relaxed by 1.2) until every |req^2 - r^2| is within the tolerance.
+// The sweeps update positions and velocities in place, so their order is
+// part of the result; they run on the host.  Atom indices in the topology
+// arrays are coordinate offsets (3 * atom).
+constexpr double kRattleFac = 1.2;
+// the reference keeps this tolerance in single precision (rattle.c:22-28)
+const double kRattleEps = static_cast<double>(static_cast<float>(0.0000001));
+
+template <class F>
+void for_constrained_bonds(const PARMSTRUCT_T *prm, int irattle, F &&body) {
+  const int nh = prm->Nbonh, nb = irattle == 2 ? 0 : prm->Mbona;
+  for (int i = 0; i < nh + nb; i++) {
+    if (i < nh) body(prm->BondHAt1[i], prm->BondHAt2[i], prm->Req[prm->BondHNum[i] - 1]);
+    else body(prm->BondAt1[i - nh], prm->BondAt2[i - nh], prm->Req[prm->BondNum[i - nh] - 1]);
+  }
+}
+
+// Position part (rattle.c:12-100); xold may alias x.
+int rattle_positions(const PARMSTRUCT_T *prm, int irattle, double dt, double *x, const double *xold, double *v,
+                     const double *minv) {
+  int niter = 0;
+  bool done = false;
+  while (!done && niter < 1000) {
+    niter++;
+    done = true;
+    for_constrained_bonds(prm, irattle, [&](int a1, int a2, double req) {
+      const double xr = x[a2] - x[a1], yr = x[a2 + 1] - x[a1 + 1], zr = x[a2 + 2] - x[a1 + 2];
+      const double delta = req * req - (xr * xr + yr * yr + zr * zr);
+      if (std::fabs(delta) <= kRattleEps) return;
+      done = false;
+      const double xo = xold[a2] - xold[a1], yo = xold[a2 + 1] - xold[a1 + 1], zo = xold[a2 + 2] - xold[a1 + 2];
+      const double dot = xr * xo + yr * yo + zr * zo;
+      double ra = minv[a1], rb = minv[a2];
+      const double term = kRattleFac * delta / (2.0 * (ra + rb) * dot);
+      const double tx = xo * term, ty = yo * term, tz = zo * term;
+      x[a1] -= tx * ra;
+      x[a1 + 1] -= ty * ra;
+      x[a1 + 2] -= tz * ra;
+      x[a2] += tx * rb;
+      x[a2 + 1] += ty * rb;
+      x[a2 + 2] += tz * rb;
+      ra /= dt;
+      rb /= dt;
+      v[a1] -= tx * ra;
+      v[a1 + 1] -= ty * ra;
+      v[a1 + 2] -= tz * ra;
+      v[a2] += tx * rb;
+      v[a2 + 1] += ty * rb;
+      v[a2 + 2] += tz * rb;
+    });
+  }
+  if (niter >= 999) fatal("ERROR in RATTLE");
+  return niter;
+}
+
+// Velocity part (rattle.c:102-181).
+int rattle_velocities(const PARMSTRUCT_T *prm, int irattle, double dt, const double *x, double *v,
+                      const double *minv) {
+  const double eps = 0.0000001 / dt;
+  int niter = 0;
+  bool done = false;
+  while (!done && niter < 1000) {
+    niter++;
+    done = true;
+    for_constrained_bonds(prm, irattle, [&](int a1, int a2, double req) {
+      const double xr = x[a2] - x[a1], yr = x[a2 + 1] - x[a1 + 1], zr = x[a2 + 2] - x[a1 + 2];
+      const double xv = v[a2] - v[a1], yv = v[a2 + 1] - v[a1 + 1], zv = v[a2 + 2] - v[a1 + 2];
+      const double ra = minv[a1], rb = minv[a2];
+      const double term = -(xr * xv + yr * yv + zr * zv) * kRattleFac / ((ra + rb) * req * req);
+      if (std::fabs(term) <= eps) return;
+      done = false;
+      const double tx = xr * term, ty = yr * term, tz = zr * term;
+      v[a1] -= tx * ra;
+      v[a1 + 1] -= ty * ra;
+      v[a1 + 2] -= tz * ra;
+      v[a2] += tx * rb;
+      v[a2 + 1] += ty * rb;
+      v[a2 + 2] += tz * rb;
+    });
+  }
+  if (niter >= 999) fatal("ERROR in RATTLE2");
+  return niter;
+}
+
 // The reference's md() loop on the host around an arbitrary energy
-// function (src/sff/sff.c:2071-2366, without RATTLE).
+// function (src/sff/sff.c:2071-2366).
 int md_host(int n, int maxstep, double *x, double *f, double *v, REAL_T (*func)(REAL_T *, REAL_T *, INT_T *)) {
   Session &s = session();
   const Options &o = options();
@@ -335,7 +426,10 @@ int md_host(int n, int maxstep, double *x, double *f, double *v, REAL_T (*func)(
   std::vector<double> minv(n), xold(n), sqrmass(n), accel(n);
   int nfrozen = 0;
   for (int i = 0; s.frozen && i < s.natom; i++) nfrozen += s.frozen[i] != 0;
-  const double dtx = o.dt * 20.455, dt5 = 0.5 * dtx, rndf = n - 3.0 * nfrozen;
+  const bool rat = o.irattle && s.prm;
+  double rndf = n - 3.0 * nfrozen;  // degrees of freedom (sff.c:2142-2146)
+  if (rat) rndf -= s.prm->Nbonh + (o.irattle == 1 ? s.prm->Mbona : 0);
+  const double dtx = o.dt * 20.455, dt5 = 0.5 * dtx;
   const double ekin0 = boltz2 * rndf * o.temp0, dttp = o.dt / o.tautp, gammai = o.gamma_ln / 20.455;
   const double c_implic = 1.0 / (1.0 + gammai * dt5), c_explic = 1.0 - gammai * dt5, c_ave = 1.0 + gammai * dt5;
   const double sdfac = std::sqrt(4.0 * gammai * boltz2 * o.temp0 / dtx);
@@ -380,6 +474,7 @@ int md_host(int n, int maxstep, double *x, double *f, double *v, REAL_T (*func)(
       v[i] = v[i] < -o.vlimit ? -o.vlimit : v[i];
       x[i] += v[i] * dtx;
     }
+    if (rat) rattle_positions(s.prm, o.irattle, dtx, x, xold.data(), v, minv.data());
     epot = func(x, f, &nstep);
     for (int i = 0; i < n; i++) {
       if (gammai == 0.0) {
@@ -390,6 +485,7 @@ int md_host(int n, int maxstep, double *x, double *f, double *v, REAL_T (*func)(
         v[i] = (v[i] + accel[i]) * c_implic;
       }
     }
+    if (rat) rattle_velocities(s.prm, o.irattle, dtx, x, v, minv.data());
     for (int i = 0; i < n; i++) ekin += v[i] * v[i] / minv[i];
     ekin *= 0.5;
     if (gammai > 0.) ekin *= c_ave;
@@ -413,7 +509,9 @@ extern "C" INT_T md(INT_T n, INT_T maxstep, REAL_T *x, REAL_T *f, REAL_T *v,
                     REAL_T (*func)(REAL_T *, REAL_T *, INT_T *)) {
   Session &s = session();
   const double t0 = wall_seconds();
-  if (func != &sffg::mme || !s.batch || n != 3 * s.natom) {
+  // RATTLE's sweeps run on the host, so md with bond constraints takes the
+  // host loop (each evaluation still on the device)
+  if (func != &sffg::mme || !s.batch || n != 3 * s.natom || options().irattle) {
     const int rc = md_host(n, maxstep, x, f, v, func);
     timers().md += wall_seconds() - t0;
     return rc;
@@ -742,4 +840,40 @@ extern "C" INT_T setseed(INT_T *seed) {
   }
   rng().seed3 = *seed;
   return 0;
+}
+
+extern "C" REAL_T mme_rattle(REAL_T *x, REAL_T *f, INT_T *iter) {
+  if (*iter == -3) return mme(x, f, iter);
+  Session &s = session();
+  const Options &o = options();
+  if (!s.prm) fatal("mme_rattle: mme_init_sff has not been called");
+  const int n3 = 3 * s.natom;
+  // unit-free dummies, as the reference uses (inverse masses 2, velocities 0)
+  std::vector<double> minv(n3, 2.0), dumv(n3, 0.0);
+  rattle_positions(s.prm, o.irattle, o.dt * 20.455, x, x, dumv.data(), minv.data());
+  const double e = mme(x, f, iter);
+  int niter = 0;
+  bool done = false;
+  while (!done && niter < 50) {
+    niter++;
+    done = true;
+    for_constrained_bonds(s.prm, o.irattle, [&](int a1, int a2, double) {
+      const double xr = x[a2] - x[a1], yr = x[a2 + 1] - x[a1 + 1], zr = x[a2 + 2] - x[a1 + 2];
+      const double d2 = xr * xr + yr * yr + zr * zr;
+      const double ip = xr * (f[a1] - f[a2]) + yr * (f[a1 + 1] - f[a2 + 1]) + zr * (f[a1 + 2] - f[a2 + 2]);
+      if (ip > 0.0000001) done = false;
+      f[a1] -= (xr / (2.0 * d2)) * ip;
+      f[a1 + 1] -= (yr / (2.0 * d2)) * ip;
+      f[a1 + 2] -= (zr / (2.0 * d2)) * ip;
+      f[a2] += (xr / (2.0 * d2)) * ip;
+      f[a2 + 1] += (yr / (2.0 * d2)) * ip;
+      f[a2 + 2] += (zr / (2.0 * d2)) * ip;
+    });
+  }
+  if (*iter == -1) {
+    double frms = 0.0;
+    for (int i = 0; i < n3; i++) frms += f[i] * f[i];
+    std::fprintf(legacy_out(), "     frms:  %15.9f (corrected for rattle)\n", std::sqrt(frms / n3));
+  }
+  return e;
 }

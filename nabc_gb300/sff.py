@@ -82,6 +82,8 @@ def lib():
         L.mme_init_sff.argtypes = [PRM_P, INT_P, INT_P, REAL_P, C.c_char_p]
         L.mme_init_sff.restype = C.c_int
         L.mme.argtypes = [REAL_P, REAL_P, INT_P]
+        L.mme_rattle.restype = C.c_double
+        L.mme_rattle.argtypes = [REAL_P, REAL_P, INT_P]
         L.mme.restype = C.c_double
         L.md.argtypes = [C.c_int, C.c_int, REAL_P, REAL_P, REAL_P, C.c_void_p]
         L.md.restype = C.c_int

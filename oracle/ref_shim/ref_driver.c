@@ -9,6 +9,9 @@
  *   cg  <maxiter> <dfpred> <rmsgrad> [out.bin]   conjgrad() driven by mme
  *   md  <nsteps> [out.bin]            md() driven by mme
  *   time <nevals>                     repeated quiet mme() evaluations
+ *   spr <out.bin>                     mme_rattle() at iter=-1 on the input
+ *                                     positions shifted by 0.02 ((k mod 3) - 1) A
+ *                                     per coordinate k (bond lengths off)
  *   spc <every> <out.bin>             single point with atoms 0, every, 2 every,
  *                                     ... restrained (option wcons) to the
  *                                     input positions shifted by
@@ -112,6 +115,15 @@ int main(int argc, char **argv)
     return 0;
   }
   mme_init_sff(prm, frozen, constrained, NULL, NULL);
+  if (strcmp(mode, "spr") == 0) {
+    int k;
+    for (k = 0; k < n3; k++) x[k] += 0.02 * (double)(k % 3 - 1);
+    iter = -1;
+    e = mme_rattle(x, g, &iter);
+    printf("oracle_total: %.17g\n", e);
+    dump(argc > 5 ? argv[5] : NULL, natom, e, x, g);
+    return 0;
+  }
 
   if (strcmp(mode, "sp") == 0) {
     iter = -1;

@@ -192,6 +192,27 @@ def main():
                         "nsteps": 20, "md": md_lines}
         arrays[f"{name}_x"] = x
         arrays[f"{name}_v"] = v
+    # RATTLE: md with bonds to hydrogen (rattle=2) and all bonds (rattle=1)
+    # constrained, and mme_rattle on a structure with perturbed bonds
+    for name, opts in (("s300_md_rattle2", "gb=5, cut=999.0, rgbmax=15.0, ntpr=10, gamma_ln=5.0, temp0=300.0, "
+                                           "dt=0.002, ntpr_md=1, zerov=1, rattle=2"),
+                       ("s300_md_rattle1", "gb=5, cut=999.0, rgbmax=15.0, ntpr=10, gamma_ln=5.0, temp0=300.0, "
+                                           "dt=0.002, ntpr_md=1, zerov=1, rattle=1")):
+        out = run([SFFREF, base + ".parm7", base + ".rst7", "md", opts, "20", tmp])
+        n, e, x, v = read_dump(tmp)
+        md_lines = [[float(t) for t in line.split()[1:]] for line in out.splitlines() if line.startswith("md:")]
+        checks[name] = {"prmtop": "n300_s11.parm7", "coords": "n300_s11.rst7", "options": opts,
+                        "nsteps": 20, "md": md_lines}
+        arrays[f"{name}_x"] = x
+        arrays[f"{name}_v"] = v
+    opts = "gb=5, cut=999.0, rgbmax=15.0, ntpr=1, rattle=2"
+    out = run([SFFREF, base + ".parm7", base + ".rst7", "spr", opts, tmp])
+    n, e, x, g = read_dump(tmp)
+    checks["s300_rattle_sp"] = {"prmtop": "n300_s11.parm7", "coords": "n300_s11.rst7", "options": opts,
+                                "shift": 0.02, "energy": e,
+                                "frms": float(re.search(r"frms:\s+([0-9.eE+-]+) \(corrected", out).group(1))}
+    arrays["s300_rattle_sp_x"] = x
+    arrays["s300_rattle_sp_g"] = g
     # positional restraints (econs): every 7th atom held to shifted positions
     opts = "gb=5, cut=999.0, rgbmax=15.0, ntpr=1, wcons=2.5"
     out = run([SFFREF, base + ".parm7", base + ".rst7", "spc", opts, "7", tmp])

@@ -201,3 +201,41 @@ def test_legacy_md_centre_of_mass_removal(lib, checks, refrun, name):
     assert np.abs(x - refrun[f"{name}_x"]).max() < 1e-5
     assert np.abs(v - refrun[f"{name}_v"]).max() < 1e-4
     del session
+
+
+@pytest.mark.parametrize("name", ["s300_md_rattle2", "s300_md_rattle1"])
+def test_legacy_md_rattle(lib, checks, refrun, name):
+    """md with RATTLE bond constraints (rattle=2: bonds to hydrogen, rattle=1:
+    all bonds) at dt = 2 fs tracks the reference's trajectory."""
+    from nabc_gb300 import sff
+    c = checks[name]
+    prm, x = load_case(c)
+    session = sff.Session(prm, c["options"])
+    L = sff.lib()
+    seed = C.c_int(-1)
+    L.setseed(C.byref(seed))
+    n = 3 * prm.contents.Natom
+    v = np.zeros(n)
+    f = np.zeros(n)
+    L.md(n, c["nsteps"], sff.dptr(x), sff.dptr(f), sff.dptr(v), C.cast(L.mme, C.c_void_p))
+    assert np.abs(x - refrun[f"{name}_x"]).max() < 1e-5
+    assert np.abs(v - refrun[f"{name}_v"]).max() < 1e-4
+    del session
+
+
+def test_mme_rattle(lib, checks, refrun):
+    """mme_rattle restores the bond lengths, then projects the gradient onto
+    the constraints, as the reference does."""
+    from nabc_gb300 import sff
+    c = checks["s300_rattle_sp"]
+    prm, x = load_case(c)
+    x = x + c["shift"] * (np.arange(len(x)) % 3 - 1)
+    session = sff.Session(prm, c["options"])
+    L = sff.lib()
+    g = np.zeros_like(x)
+    it = C.c_int(-1)
+    e = L.mme_rattle(sff.dptr(x), sff.dptr(g), C.byref(it))
+    assert np.abs(x - refrun["s300_rattle_sp_x"]).max() < 1e-12
+    assert abs(e - c["energy"]) <= 1e-6 * abs(c["energy"])
+    assert np.sqrt(((g - refrun["s300_rattle_sp_g"]) ** 2).mean()) <= 1e-5
+    del session
