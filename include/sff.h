@@ -114,6 +114,64 @@ INT_T mme_timer(void);
  * set (sff.c:2251-2280). */
 REAL_T mme_rattle(REAL_T *x, REAL_T *f, INT_T *iter);
 
+/* Options of the XMIN minimiser, the reference's layout and meaning
+ * (src/sff/sff.h:64-84): method 1 PRCG, 2 L-BFGS, 3 L-BFGS-preconditioned
+ * TNCG, 4 gradient check; ls_method 1 Armijo, 2 More-Thuente (Wolfe);
+ * numdiff 1 forward, 2 central differences for TNCG's Hessian products;
+ * print_level 0 quiet, 1 every iteration, 2 with line-search details, n > 2
+ * every n-th iteration.  iter, ls_iter, xmin_time and error_flag are
+ * outputs. */
+typedef struct xmin_opt {
+  INT_T mol_struct_opt;
+  INT_T maxiter;
+  REAL_T grms_tol;
+  INT_T method;
+  INT_T numdiff;
+  INT_T m_lbfgs;
+  INT_T iter;
+  REAL_T xmin_time;
+  INT_T ls_method;
+  INT_T ls_maxiter;
+  REAL_T ls_maxatmov;
+  REAL_T beta_armijo;
+  REAL_T c_armijo;
+  REAL_T mu_armijo;
+  REAL_T ftol_wolfe;
+  REAL_T gtol_wolfe;
+  INT_T ls_iter;
+  INT_T print_level;
+  INT_T error_flag;
+} XMIN_OPT_T;
+
+/* Defaults of the XMIN options (src/sff/sff.h:168, xminC.c:2976). */
+INT_T xmin_opt_init(struct xmin_opt *xo);
+
+/* Minimise func from xyz with XMIN (src/sff/sff.h:169-170,
+ * xminC.c:2997): natm atoms (mol_struct_opt=1; atoms whose gradient in
+ * grad is exactly zero on entry stay fixed) or natm dimensions
+ * (mol_struct_opt=0).  func gets -4 (rebuild the pair list), -2 (keep it)
+ * or the iteration count as its third argument, as mme() reads it.  On
+ * return xyz, grad, energy and grms hold the minimum; the return value is
+ * the energy, or 0 with xo->error_flag < 0 on an error. */
+REAL_T xmin(REAL_T (*func)(REAL_T *, REAL_T *, INT_T *), INT_T *natm,
+            REAL_T *xyz, REAL_T *grad, REAL_T *energy, REAL_T *grms,
+            struct xmin_opt *xo);
+
+/* XMIN's reverse-communication form (src/sff/sff.h:171-176,
+ * xminC.c:2491): call with *label = 0; while it returns *label = 1,
+ * evaluate energy and gradient at xyz_ext (pair-list policy in
+ * *return_flag: 4-6 rebuild, 7-9 keep) and call again; *label = 0 and
+ * *return_flag = 0 mean done, *label < 0 an error. */
+REAL_T xminC(INT_T *xyz_min, INT_T *minim_method, INT_T *maxiter,
+             REAL_T *grms_tol, INT_T *natm_ext, INT_T *m_lbfgs,
+             INT_T *numdiff, REAL_T *xyz_ext, REAL_T *enrg,
+             REAL_T *grad_ext, REAL_T *grms, INT_T *iter,
+             REAL_T *total_time, INT_T *print_level, INT_T *ls_method,
+             INT_T *ls_maxiter, INT_T *ls_iter, REAL_T *ls_maxatmov,
+             REAL_T *beta_armijo, REAL_T *c_armijo, REAL_T *mu_armijo,
+             REAL_T *ftol_wolfe, REAL_T *gtol_wolfe, INT_T *return_flag,
+             INT_T *label);
+
 /* parm7 reader, writer and release (src/sff/sff.h:178-180, prm.c:584,
  * prm.c:1997, prm.c:2810). */
 PARMSTRUCT_T *rdparm(STRING_T *name);

@@ -23,6 +23,10 @@ ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 NVCC_FLAGS = ["-O3", "-std=c++17", "-lineinfo", "-Xcompiler", "-fPIC", "-Xptxas", "-O3",
               "--expt-relaxed-constexpr"]
 CXX_FLAGS = ["-O2", "-std=c++17", "-fPIC", "-Wall", "-Wno-unused-function"]
+# Host files whose arithmetic must match the reference's bit for bit on any
+# host: no floating-point contraction (FMA) and the C++20 coroutines the
+# minimiser is written with.
+CXX_FILE_FLAGS = {"xmin.cpp": ["-std=c++20", "-ffp-contract=off"]}
 
 
 def library_path():
@@ -50,7 +54,7 @@ def _compile(src, obj, force):
         cmd = [_nvcc()] + ARCH + NVCC_FLAGS + os.environ.get("SFFG_NVCC_EXTRA", "").split() + \
             ["-I", CSRC, "-c", src, "-o", obj]
     else:
-        cmd = ["g++"] + CXX_FLAGS + ["-I", CSRC, "-I", "/usr/local/cuda/include", "-c", src, "-o", obj]
+        cmd = ["g++"] + CXX_FLAGS + CXX_FILE_FLAGS.get(os.path.basename(src), []) + ["-I", CSRC, "-I", "/usr/local/cuda/include", "-c", src, "-o", obj]
     r = subprocess.run(cmd, capture_output=True, text=True)
     if r.returncode != 0:
         raise RuntimeError(f"compile failed: {' '.join(cmd)}\n{r.stdout}\n{r.stderr}")

@@ -49,6 +49,20 @@ class PARMSTRUCT_T(C.Structure):
 PRM_P = C.POINTER(PARMSTRUCT_T)
 FUNC_T = C.CFUNCTYPE(C.c_double, REAL_P, REAL_P, INT_P)
 
+
+class XMIN_OPT_T(C.Structure):
+    """Same field order and types as the reference's struct xmin_opt
+    (src/sff/sff.h:64-84)."""
+
+    _fields_ = [
+        ("mol_struct_opt", C.c_int), ("maxiter", C.c_int), ("grms_tol", C.c_double),
+        ("method", C.c_int), ("numdiff", C.c_int), ("m_lbfgs", C.c_int), ("iter", C.c_int),
+        ("xmin_time", C.c_double), ("ls_method", C.c_int), ("ls_maxiter", C.c_int),
+        ("ls_maxatmov", C.c_double), ("beta_armijo", C.c_double), ("c_armijo", C.c_double),
+        ("mu_armijo", C.c_double), ("ftol_wolfe", C.c_double), ("gtol_wolfe", C.c_double),
+        ("ls_iter", C.c_int), ("print_level", C.c_int), ("error_flag", C.c_int),
+    ]
+
 _lib = None
 
 
@@ -78,6 +92,14 @@ def lib():
     L.putxv.restype = C.c_int
     L.sffg_synth_molecule.argtypes = [C.c_int, C.c_ulonglong, REAL_P, REAL_P]
     L.sffg_synth_molecule.restype = PRM_P
+    L.xmin_opt_init.argtypes = [C.POINTER(XMIN_OPT_T)]
+    L.xmin_opt_init.restype = C.c_int
+    L.xmin.argtypes = [C.c_void_p, INT_P, REAL_P, REAL_P, REAL_P, REAL_P, C.POINTER(XMIN_OPT_T)]
+    L.xmin.restype = C.c_double
+    L.xminC.argtypes = [INT_P, INT_P, INT_P, REAL_P, INT_P, INT_P, INT_P, REAL_P, REAL_P, REAL_P,
+                        REAL_P, INT_P, REAL_P, INT_P, INT_P, INT_P, INT_P, REAL_P, REAL_P, REAL_P,
+                        REAL_P, REAL_P, REAL_P, INT_P, INT_P]
+    L.xminC.restype = C.c_double
     if hasattr(L, "mme_init_sff"):
         L.mme_init_sff.argtypes = [PRM_P, INT_P, INT_P, REAL_P, C.c_char_p]
         L.mme_init_sff.restype = C.c_int

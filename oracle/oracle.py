@@ -52,6 +52,21 @@ def lib():
     return _lib
 
 
+def xmin_functions():
+    """The minimiser test functions of oracle/xmin_funcs.c (extended
+    Rosenbrock and a bead chain), built without floating-point contraction:
+    the same compiled code the reference's XMIN ran on to make the golden
+    traces."""
+    path = os.path.join(HERE, "_build", "libxminf.so")
+    if not os.path.exists(path):
+        build()
+    F = C.CDLL(path)
+    for name in ("xf_rosenbrock", "xf_chain"):
+        getattr(F, name).restype = C.c_double
+        getattr(F, name).argtypes = [REAL_P, REAL_P, INT_P]
+    return F
+
+
 def _p(a):
     return a.ctypes.data_as(REAL_P)
 

@@ -16,6 +16,11 @@
  *                                     ... restrained (option wcons) to the
  *                                     input positions shifted by
  *                                     0.05 ((3 i + k) mod 5 - 2) A per coordinate
+ *   xmin <method> <maxiter> <grms_tol> <ls_maxatmov> <rattle> <out.bin> <trace.bin>
+ *                                     the reference's test/txmin.c: func(x, g, -1),
+ *                                     xmin(func) with print_level 10, func(x, g, -1),
+ *                                     func = mme_rattle (rattle=1) or mme;
+ *                                     trace.bin: every energy xmin asked for (f64)
  *
  * Coordinates come from a PDB (columns 31-54 of ATOM/HETATM records, the
  * order the prmtop uses) or an Amber ASCII restart read with getxv().
@@ -55,6 +60,18 @@ static int read_pdb(const char *name, int natom, double *x)
   }
   fclose(fp);
   return n == natom ? 0 : -1;
+}
+
+static double (*traced_func)(double *, double *, int *);
+static double trace[100000];
+static int ntraced;
+
+static double traced(double *x, double *g, int *iter)
+{
+  double e = traced_func(x, g, iter);
+  if (ntraced < 100000) trace[ntraced] = e;
+  ntraced++;
+  return e;
 }
 
 static void dump(const char *name, int natom, double e, const double *x, const double *g)
@@ -115,6 +132,32 @@ int main(int argc, char **argv)
     return 0;
   }
   mme_init_sff(prm, frozen, constrained, NULL, NULL);
+  if (strcmp(mode, "xmin") == 0) {
+    XMIN_OPT_T xo;
+    double grms = 0.0;
+    FILE *fp;
+    xmin_opt_init(&xo);
+    xo.method = atoi(argv[5]);
+    xo.maxiter = atoi(argv[6]);
+    xo.grms_tol = atof(argv[7]);
+    xo.ls_maxatmov = atof(argv[8]);
+    xo.print_level = 10;
+    traced_func = atoi(argv[9]) ? mme_rattle : mme;
+    iter = -1;
+    e = traced_func(x, g, &iter);
+    e = xmin(traced, &natom, x, g, &e, &grms, &xo);
+    printf("xmin returns %.17g iter %d ls_iter %d error %d grms %.17g\n", e, xo.iter, xo.ls_iter,
+           xo.error_flag, grms);
+    iter = -1;
+    e = traced_func(x, g, &iter);
+    printf("oracle_total: %.17g\n", e);
+    dump(argv[10], natom, e, x, g);
+    fp = fopen(argv[11], "wb");
+    if (!fp) { perror(argv[11]); return 2; }
+    fwrite(trace, sizeof(double), (size_t)(ntraced < 100000 ? ntraced : 100000), fp);
+    fclose(fp);
+    return 0;
+  }
   if (strcmp(mode, "spr") == 0) {
     int k;
     for (k = 0; k < n3; k++) x[k] += 0.02 * (double)(k % 3 - 1);

@@ -10,15 +10,16 @@ It produces
                 PDB/restart coordinates), copied unchanged;
   checks.json   the reference's expected outputs parsed from its shipped
                 .check files (test/nab/{gbrna,gbtrx,gb5trx,gb7trx,gb8trx},
-                test/nab/aspgb8.out).  test/txmin.out.check is not used: its
-                driver evaluates through mme_rattle, which first moves the
-                atoms onto the RATTLE constraints;
+                test/nab/aspgb8.out);
   synth/        small synthetic molecules (parm7 + rst7) from the
                 benchmark generator;
   refrun.npz    outputs of the reference library itself (oracle/_ref/sffref,
                 compiled from the reference sources) on those inputs:
-                energy components, full gradients, conjgrad traces and a
-                short Langevin trajectory.
+                energy components, full gradients, conjgrad traces, short
+                Langevin trajectories, XMIN minimisations of xfin (the
+                reference's test/txmin.c) and of the test functions of
+                oracle/xmin_funcs.c (oracle/_ref/xminref), each with every
+                function value XMIN asked for.
 """
 import json
 import os
@@ -34,6 +35,27 @@ ROOT = os.path.dirname(os.path.dirname(HERE))
 sys.path.insert(0, ROOT)
 
 SFFREF = os.path.join(ROOT, "oracle", "_ref", "sffref")
+XMINREF = os.path.join(ROOT, "oracle", "_ref", "xminref")
+
+# XMIN on the test functions of oracle/xmin_funcs.c: (function, method,
+# ls_method, numdiff, m_lbfgs, maxiter, grms_tol, ls_maxatmov)
+XMIN_CASES = [
+    ("rosen", 2, 2, 1, 5, 200, 1e-8, 0.5),
+    ("rosen", 1, 2, 1, 5, 200, 1e-8, 0.5),
+    ("rosen", 2, 1, 1, 5, 200, 1e-8, 0.5),
+    ("rosen", 3, 2, 1, 5, 100, 1e-8, 0.5),   # TNCG ends on y.s = 0 (error -4)
+    ("rosen", 3, 1, 2, 5, 100, 1e-8, 0.5),   # the same with Armijo, central differences
+    ("rosen", 3, 2, 1, 3, 100, 1e-8, 0.5),
+    ("rosen", 3, 2, 2, 0, 100, 1e-8, 0.5),   # TNCG without preconditioning
+    ("chain", 2, 2, 1, 5, 200, 1e-6, 0.5),
+    ("chain", 2, 1, 1, 7, 60, 1e-6, 0.05),   # steps capped by ls_maxatmov
+    ("chain", 2, 2, 1, 3, 0, 1e-6, 0.5),     # maxiter 0
+    ("chain", 1, 1, 1, 5, 200, 1e-6, 0.5),
+    ("chain", 1, 2, 1, 5, 200, 1e-6, 0.5),
+    ("chain", 3, 2, 1, 5, 100, 1e-6, 0.3),
+    ("chain", 3, 2, 2, 5, 100, 1e-6, 0.5),
+    ("chain", 3, 1, 1, 0, 100, 1e-6, 0.5),
+]
 
 # (name, prmtop, coordinates, options, conjgrad args) for the reference's
 # GB regression tests (test/nab/*.nab, test/txmin.c)
@@ -90,6 +112,16 @@ def parse_breakdown(text):
         if m and m.group(1) in BREAKDOWN and m.group(1) not in out:
             out[m.group(1)] = float(m.group(2))
     return out
+
+
+def parse_min_lines(text):
+    """[iteration, energy, gradient RMS] of every " MIN:" progress line."""
+    rows = []
+    for line in text.splitlines():
+        m = re.match(r" MIN:\s+Iter =\s*(\d+).*\sE =\s*(\S+)\s+RMSG =\s*(\S+)", line)
+        if m:
+            rows.append([float(m.group(1)), float(m.group(2)), float(m.group(3))])
+    return rows
 
 
 def read_dump(path):
@@ -220,6 +252,49 @@ def main():
     checks["s300_cons"] = {"prmtop": "n300_s11.parm7", "coords": "n300_s11.rst7", "options": opts,
                            "every": 7, "shift": 0.05, "sp": parse_breakdown(out), "energy": e}
     arrays["s300_cons_g"] = g
+    # XMIN on xfin as the reference's test/txmin.c runs it (L-BFGS through
+    # mme_rattle, 50 iterations), the same through mme, and TNCG
+    opts = "ntpr=1, gb=1, kappa=0.10395, rgbmax=99., cut=99.0, diel=C"
+    tr = os.path.join(HERE, "_trace.bin")
+    for name, method, maxiter, gtol, atmov, rattle in (("xfin_xmin", 2, 50, 0.0005, 0.15, 1),
+                                                       ("xfin_xmin_mme", 2, 50, 0.0005, 0.15, 0),
+                                                       ("xfin_tncg", 3, 10, 0.0005, 0.15, 0)):
+        out = run([SFFREF, os.path.join(HERE, "ref", "xfin.parm7"), os.path.join(HERE, "ref", "xfin.rst7"), "xmin",
+                   opts, str(method), str(maxiter), str(gtol), str(atmov), str(rattle), tmp, tr])
+        n, e, x, g = read_dump(tmp)
+        m = re.search(r"xmin returns (\S+) iter (-?\d+) ls_iter (-?\d+) error (-?\d+) grms (\S+)", out)
+        mins = parse_min_lines(out)
+        checks[name] = {"prmtop": "xfin.parm7", "coords": "xfin.rst7", "options": opts, "method": method,
+                        "maxiter": maxiter, "grms_tol": gtol, "ls_maxatmov": atmov, "rattle": rattle,
+                        "returns": float(m.group(1)), "iter": int(m.group(2)), "ls_iter": int(m.group(3)),
+                        "error_flag": int(m.group(4)), "grms": float(m.group(5)), "min_lines": mins,
+                        "final": parse_breakdown(out.split("xmin returns")[1]), "energy": e}
+        arrays[f"{name}_x"] = x
+        arrays[f"{name}_trace"] = np.fromfile(tr, np.float64)
+    os.remove(tr)
+    text = open(os.path.join(test, "txmin.out.check")).read()
+    checks["xfin_xmin"]["check_file"] = {
+        "min_lines": parse_min_lines(text),
+        "initial": parse_breakdown(text.split("setting print")[0]),
+        "final": parse_breakdown(text.split(" END:")[1])}
+    # XMIN on the test functions (bit-for-bit cases)
+    xcases = []
+    for k, (fn, method, lsm, nd, mlb, maxiter, gtol, atmov) in enumerate(XMIN_CASES):
+        out = run([XMINREF, fn, str(method), str(lsm), str(nd), str(mlb), str(maxiter), repr(gtol), repr(atmov),
+                   tmp])
+        with open(tmp, "rb") as f:
+            ndim, ncalls, it, lsit, err = np.frombuffer(f.read(20), np.int32)
+            ret, e, grms = np.frombuffer(f.read(24), np.float64)
+            rest = np.frombuffer(f.read(), np.float64)
+        xcases.append({"function": fn, "method": method, "ls_method": lsm, "numdiff": nd, "m_lbfgs": mlb,
+                       "maxiter": maxiter, "grms_tol": gtol, "ls_maxatmov": atmov, "ndim": int(ndim),
+                       "iter": int(it), "ls_iter": int(lsit), "error_flag": int(err)})
+        arrays[f"xmin{k}_scalars"] = np.array([ret, e, grms])
+        arrays[f"xmin{k}_start"] = rest[:ndim]
+        arrays[f"xmin{k}_x"] = rest[ndim:2 * ndim]
+        arrays[f"xmin{k}_g"] = rest[2 * ndim:3 * ndim]
+        arrays[f"xmin{k}_trace"] = rest[3 * ndim:3 * ndim + ncalls]
+    checks["xmin_functions"] = {"frozen_chain_atom": 4, "cases": xcases}
     os.remove(tmp)
     with open(os.path.join(HERE, "checks.json"), "w") as f:
         json.dump(checks, f, indent=1)

@@ -30,7 +30,8 @@ def test_every_declared_function_is_exported(lib, header):
 def test_reference_symbols_present(lib):
     """The entry points the reference's drivers call (src/sff/sff.h)."""
     for n in ("mm_options", "mme_init_sff", "mme", "md", "conjgrad", "mme_timer", "rdparm", "wrparm", "free_prm",
-              "getxv", "putxv", "rand2", "gauss2", "setseed", "nabout"):
+              "getxv", "putxv", "rand2", "gauss2", "setseed", "nabout", "mme_rattle", "xmin", "xminC",
+              "xmin_opt_init"):
         assert hasattr(lib, n), n
 
 
