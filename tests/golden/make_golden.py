@@ -71,7 +71,7 @@ REF_CASES = [
     ("gb8trx", "nab/prmtop.gb2", "nab/trxox.2.4ns.pdb",
      "ntpr=1, gb=8, rgbmax=15.0, cut=99.0, diel=C, e_debug=0", "gb8trx.out.check"),
 ]
-EXTRA_INPUTS = ["nab/asp.top", "nab/asp.pdb", "xfin.parm7", "xfin.rst7"]
+EXTRA_INPUTS = ["nab/asp.top", "nab/asp.pdb", "xfin.parm7", "xfin.rst7", "xfin.md1.rst7"]
 
 BREAKDOWN = ["bond", "angle", "dihedral", "enb14", "eel14", "enb", "eel", "egb", "econs", "esurf", "Total",
              "frms"]
@@ -252,6 +252,16 @@ def main():
     checks["s300_cons"] = {"prmtop": "n300_s11.parm7", "coords": "n300_s11.rst7", "options": opts,
                            "every": 7, "shift": 0.05, "sp": parse_breakdown(out), "energy": e}
     arrays["s300_cons_g"] = g
+    # the reference's md test (test/tmd.c on xfin.md1.rst7: gb=1, cut 20,
+    # Langevin 300 K, rattle=1, 500 steps of 1 fs): its shipped .check lines,
+    # which the compiled reference reproduces digit for digit
+    text = open(os.path.join(test, "tmd.out.check")).read()
+    checks["tmd"] = {"prmtop": "xfin.parm7", "coords": "xfin.md1.rst7",
+                     "options": "cut=20.0, rgbmax=20.0, ntpr=500, nsnb=10, gb=1, diel=C, gamma_ln=5.0, "
+                                "temp0=300.0, ntpr_md=100, rattle=1",
+                     "nsteps": 500, "ff": parse_ff(text),
+                     "md": [[float(t) for t in line.split()[1:]] for line in text.splitlines()
+                            if line.startswith("md:")]}
     # XMIN on xfin as the reference's test/txmin.c runs it (L-BFGS through
     # mme_rattle, 50 iterations), the same through mme, and TNCG
     opts = "ntpr=1, gb=1, kappa=0.10395, rgbmax=99., cut=99.0, diel=C"

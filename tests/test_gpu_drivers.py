@@ -5,7 +5,7 @@ import ctypes as C
 import numpy as np
 import pytest
 
-from conftest import load_case
+from conftest import golden_path, load_case
 
 pytestmark = pytest.mark.gpu
 
@@ -239,3 +239,41 @@ def test_mme_rattle(lib, checks, refrun):
     assert abs(e - c["energy"]) <= 1e-6 * abs(c["energy"])
     assert np.sqrt(((g - refrun["s300_rattle_sp_g"]) ** 2).mean()) <= 1e-5
     del session
+
+
+def test_tmd_check_file(lib, checks, tmp_path):
+    """The reference's md test (test/tmd.c: xfin.md1.rst7, gb=1, cut 20,
+    Langevin at 300 K with the reference's noise stream, rattle=1, 500 steps)
+    against its shipped tmd.out.check: every ff: and md: line (steps 0, 1,
+    100, ..., 500) to the printed digits (0.01), which the FP32 pair
+    arithmetic holds over the whole run."""
+    import os
+    from nabc_gb300 import sff
+    c = checks["tmd"]
+    prm, x = load_case(c)
+    n = prm.contents.Natom
+    _, v = sff.getxv(golden_path(c["coords"]), n)
+    session = sff.Session(prm, c["options"])
+    L = sff.lib()
+    seed = C.c_int(-1)
+    L.setseed(C.byref(seed))
+    out = str(tmp_path / "tmd.out")
+    sff.set_output(out)
+    try:
+        f = np.zeros(3 * n)
+        L.md(3 * n, c["nsteps"], sff.dptr(x), sff.dptr(f), sff.dptr(v), C.cast(L.mme, C.c_void_p))
+        sff.flush_output()
+    finally:
+        sff.set_output(os.devnull)
+    del session
+    text = open(out).read()
+    ff = [[float(t) for t in line.split()[1:]] for line in text.splitlines() if line.startswith("ff:")]
+    md = [[float(t) for t in line.split()[1:]] for line in text.splitlines() if line.startswith("md:")]
+    print("ff", ff)
+    print("md", md)
+    assert len(md) == len(c["md"]) and len(ff) == len(c["ff"])
+    for got, want in zip(ff, c["ff"]):
+        assert got[:7] == pytest.approx(want[:7], abs=0.011)
+        assert got[7] == pytest.approx(want[7], rel=0.01)  # frms, printed with 3 digits
+    for got, want in zip(md, c["md"]):
+        assert got == pytest.approx(want, abs=0.011)
