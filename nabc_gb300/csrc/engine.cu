@@ -1296,7 +1296,18 @@ int Batch::md_begin(bool rebuild, NoiseFn noise, void *noise_ctx, void *stream) 
   return SFFG_OK;
 }
 
-int Batch::md_steps(int step0, int k, NoiseFn noise, void *noise_ctx, void *stream) {
+int Batch::md_com_remove(void *stream) {
+  if (!finalized_) return SFFG_ESTATE;
+  DeviceState &d = *d_;
+  cudaStream_t st = pick(d, stream);
+  k_com_remove<<<num_systems(), kComThreads, 0, st>>>(d.x.p, d.v.p, d.minv.p, d.sys_atom_off.p, d.sys_natom.p,
+                                                      d.sys_active.p, opts_.gamma_ln == 0.0 || opts_.hcp != 0);
+  SFFG_CK(cudaGetLastError());
+  launches_++;
+  return SFFG_OK;
+}
+
+int Batch::md_steps(int step0, int k, NoiseFn noise, void *noise_ctx, void *stream, bool com_at_end) {
   if (!finalized_) return SFFG_ESTATE;
   DeviceState &d = *d_;
   cudaStream_t st = pick(d, stream);
@@ -1333,7 +1344,7 @@ int Batch::md_steps(int step0, int k, NoiseFn noise, void *noise_ctx, void *stre
     const int nstep = step0 + i;
     const bool rebuild = opts_.nsnb > 0 && nstep % opts_.nsnb == 0;
     // centre-of-mass motion removal every nscm steps (sff.c:2346-2351)
-    const bool com = opts_.nscm > 0 && nstep % opts_.nscm == 0;
+    const bool com = opts_.nscm > 0 && nstep % opts_.nscm == 0 && (i < k || com_at_end);
     if (!rebuild && !noise && !com && graphs_ok()) {
       if ((rc = ensure_tuned(st))) break;
       if ((rc = capture(d.g_step, d.sig_step, d.launches_step, [&](cudaStream_t cs) { return step_body(cs, false, true); })))
@@ -1344,12 +1355,7 @@ int Batch::md_steps(int step0, int k, NoiseFn noise, void *noise_ctx, void *stre
     } else if ((rc = step_body(st, rebuild, false))) {
       break;
     }
-    if (com) {
-      k_com_remove<<<nsys, kComThreads, 0, st>>>(d.x.p, d.v.p, d.minv.p, d.sys_atom_off.p, d.sys_natom.p,
-                                                 d.sys_active.p, a.gammai == 0.0 || opts_.hcp != 0);
-      SFFG_CK(cudaGetLastError());
-      launches_++;
-    }
+    if (com && (rc = md_com_remove(st))) break;
   }
   return rc;
 }

@@ -99,7 +99,11 @@ class Batch {
   // non-frozen coordinate in the reference's order.
   using NoiseFn = void (*)(void *ctx, int sys, int n, double *out);
   int md_begin(bool rebuild, NoiseFn noise, void *noise_ctx, void *stream);
-  int md_steps(int step0, int k, NoiseFn noise, void *noise_ctx, void *stream);
+  // com_at_end=false leaves out the centre-of-mass removal a last step that
+  // is a multiple of nscm would end with; md_com_remove applies it later
+  // (md() writes its trajectory frame between the two, as the reference).
+  int md_steps(int step0, int k, NoiseFn noise, void *noise_ctx, void *stream, bool com_at_end = true);
+  int md_com_remove(void *stream);
   // Kinetic energy after the last md step (reference convention,
   // sff.c:2294-2306) and Berendsen factor for the next step.
   int md_kinetic(std::vector<double> &ekin, void *stream);

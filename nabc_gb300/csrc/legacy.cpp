@@ -28,6 +28,7 @@ struct Session {
   std::unique_ptr<Batch> batch;
   int natom = 0;
   bool list_built = false;
+  NcTrajectory traj;  // md()'s trajectory when mme_init_sff got a file name
 };
 
 Session &session() {
@@ -184,7 +185,6 @@ extern "C" REAL_T mme(REAL_T *x, REAL_T *f, INT_T *iter);
 using namespace sffg;
 
 extern "C" INT_T mme_init_sff(PARMSTRUCT_T *prm, INT_T *frozen, INT_T *constrained, REAL_T *x0, STRING_T *ncname) {
-  (void)ncname;
   const double t0 = wall_seconds();
   Session &s = session();
   s.batch.reset();
@@ -198,6 +198,10 @@ extern "C" INT_T mme_init_sff(PARMSTRUCT_T *prm, INT_T *frozen, INT_T *constrain
     std::fprintf(legacy_out(), "Error in egb: rgbmax = %f is greater than cutoff = %f\n", o.rgbmax, o.cut);
     std::exit(1);
   }
+  // md()'s Amber NetCDF trajectory, written every ntwx steps (sff.c:1164-1168)
+  s.traj.close();
+  if (ncname && !s.traj.create(ncname, prm->Natom))
+    std::fprintf(stderr, "Error: cannot create NetCDF trajectory %s\n", ncname);
   // positional restraints (src/sff/sff.c:1169-1178): counted and reported
   // here, applied from the first mme() on
   s.constrained = nullptr;
@@ -495,6 +499,7 @@ int md_host(int n, int maxstep, double *x, double *f, double *v, REAL_T (*func)(
                    ekin + epot, ekin / (boltz2 * rndf));
       std::fflush(legacy_out());
     }
+    if (o.ntwx > 0 && nstep % o.ntwx == 0 && s.traj.open()) s.traj.write_frame(x, t);
     if (o.nscm > 0 && nstep % o.nscm == 0) com_remove_host(n, x, v, minv.data(), gammai == 0.0 || o.hcp);
   }
   options().t = t;
@@ -563,19 +568,23 @@ extern "C" INT_T md(INT_T n, INT_T maxstep, REAL_T *x, REAL_T *f, REAL_T *v,
   while (step < maxstep) {
     // run to the next step that prints something
     int next = maxstep;
+    const bool frames = o.ntwx > 0 && s.traj.open();
     for (int k = step + 1; k <= maxstep; k++) {
-      if (k == 1 || k % o.ntpr_md == 0 || k % o.ntpr == 0) {
+      if (k == 1 || k % o.ntpr_md == 0 || k % o.ntpr == 0 || (frames && k % o.ntwx == 0)) {
         next = k;
         break;
       }
     }
+    // a frame is written before that step's centre-of-mass removal (sff.c:2341-2351)
+    const bool frame = frames && next % o.ntwx == 0;
+    const bool com_after = frame && o.nscm > 0 && next % o.nscm == 0;
     if (step == 0 && gammai == 0.0) {
       // Berendsen: the first step's factor comes from the initial kinetic
       // energy; the device derives the later ones (sff.c:2225-2228)
       std::vector<double> ts(1, ekin > 0.01 ? std::sqrt(1. + dttp * (ekin0 / ekin - 1.)) : 1.0);
       check(b.md_set_tscal(ts, nullptr), "md");
     }
-    check(b.md_steps(step, next - step, noise, nullptr, nullptr), "md");
+    check(b.md_steps(step, next - step, noise, nullptr, nullptr, !com_after), "md");
     t += o.dt * (next - step);
     step = next;
     std::vector<double> ek;
@@ -592,6 +601,11 @@ extern "C" INT_T md(INT_T n, INT_T maxstep, REAL_T *x, REAL_T *f, REAL_T *v,
       std::fprintf(legacy_out(), "md:       %5d %10.3f %10.2f %10.2f %10.2f %10.2f\n", step, t, ekin, ene[0],
                    ekin + ene[0], ekin / (boltz2 * rndf));
       std::fflush(legacy_out());
+    }
+    if (frame) {
+      check(b.get_coords(0, x, nullptr), "get_coords");
+      s.traj.write_frame(x, t);
+      if (com_after) check(b.md_com_remove(nullptr), "md");
     }
   }
   o.t = t;

@@ -48,6 +48,23 @@ FILE *legacy_out();  // the caller's nabout, or stdout
 // otherwise -1 is returned and the item copied to *bad.
 int parse_options(const char *opts, Options &o, bool echo, bool fail_stop, std::string *bad);
 
+// An Amber NetCDF trajectory (csrc/netcdf.cpp): created by mme_init_sff when
+// it gets a file name, appended to by md() every ntwx steps.
+class NcTrajectory {
+ public:
+  ~NcTrajectory() { close(); }
+  bool create(const char *path, int natom);
+  bool write_frame(const double *x, double time_ps);
+  void close();
+  bool open() const { return fp_ != nullptr; }
+  int frames() const { return frames_; }
+
+ private:
+  FILE *fp_ = nullptr;
+  int natom_ = 0, frames_ = 0;
+  unsigned long long data_begin_ = 0, record_bytes_ = 0;
+};
+
 // ---------------------------------------------------------------- model
 enum GbModel { GB_NONE = 0, GB_HCT = 1, GB_OBC1 = 2, GB_OBC2 = 5, GB_NECK = 7, GB_NECK2 = 8 };
 

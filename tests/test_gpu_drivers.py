@@ -277,3 +277,40 @@ def test_tmd_check_file(lib, checks, tmp_path):
         assert got[7] == pytest.approx(want[7], rel=0.01)  # frms, printed with 3 digits
     for got, want in zip(md, c["md"]):
         assert got == pytest.approx(want, abs=0.011)
+
+
+def test_md_trajectory_device_path(lib, tmp_path):
+    """md() through the device-resident path writes its Amber NetCDF frames
+    from device state: every ntwx steps, the last frame equal to the final
+    structure in single precision, and a frame that falls on an nscm step
+    taken before the centre-of-mass removal (sff.c:2341-2351)."""
+    from scipy.io import netcdf_file
+    from nabc_gb300 import sff
+    prm = sff.rdparm(golden_path("xfin.parm7"))
+    n = prm.contents.Natom
+    x, _ = sff.getxv(golden_path("xfin.rst7"), n)
+    L = sff.lib()
+    for nscm, nsteps in ((0, 20), (10, 20)):
+        L.sffg_options_reset()
+        L.mm_options(f"gb=1, cut=99.0, rgbmax=15.0, ntwx=5, ntpr_md=5, nscm={nscm}, gamma_ln=5.0, "
+                     "temp0=300.0, zerov=1, dt=0.001".encode())
+        frozen = np.zeros(n, np.int32)
+        cons = np.zeros(n, np.int32)
+        path = str(tmp_path / f"md{nscm}.nc")
+        L.mme_init_sff(prm, sff.iptr(frozen), sff.iptr(cons), None, path.encode())
+        xx = x.copy()
+        v = np.zeros(3 * n)
+        f = np.zeros(3 * n)
+        L.md(3 * n, nsteps, sff.dptr(xx), sff.dptr(f), sff.dptr(v), C.cast(L.mme, C.c_void_p))
+        nc = netcdf_file(path, "r", mmap=False)
+        coords = nc.variables["coordinates"][:].astype(np.float64)
+        times = nc.variables["time"][:].copy()
+        nc.close()
+        assert coords.shape == (nsteps // 5, n, 3)
+        np.testing.assert_allclose(times, 0.005 * np.arange(1, nsteps // 5 + 1), rtol=1e-6)
+        if nscm == 0:
+            np.testing.assert_array_equal(coords[-1].ravel(), xx.astype(np.float32).astype(np.float64))
+        else:
+            shift = coords[-1] - xx.reshape(n, 3)
+            assert np.abs(shift - shift.mean(0)).max() < 1e-4
+            assert np.abs(shift.mean(0)).max() > 1e-6
