@@ -41,6 +41,10 @@ struct DBuf {
 
 struct DeviceState {
   cudaStream_t stream = nullptr;
+  // the bonded FP64 terms run on a side stream, beside the list upkeep and
+  // the FP32 pair passes (fork after the pack, join before the gather)
+  cudaStream_t side = nullptr;
+  cudaEvent_t fork_ev = nullptr, join_ev = nullptr;
   int nsm = 0;
   cudaEvent_t tune_ev[3][2] = {};  // pass timing while the work split is tuned
   // per slot
@@ -116,6 +120,9 @@ struct DeviceState {
       for (auto &pe : ring)
         for (auto &e : pe)
           if (e) cudaEventDestroy(e);
+    if (fork_ev) cudaEventDestroy(fork_ev);
+    if (join_ev) cudaEventDestroy(join_ev);
+    if (side) cudaStreamDestroy(side);
     if (stream) cudaStreamDestroy(stream);
     // DBuf members release in their own destructors? they are PODs: free here
     auto rel = [](auto &b) { b.release(); };
@@ -243,6 +250,9 @@ int Batch::finalize() {
   }
   d_.reset(new DeviceState());
   SFFG_CK(cudaStreamCreateWithFlags(&d_->stream, cudaStreamNonBlocking));
+  SFFG_CK(cudaStreamCreateWithFlags(&d_->side, cudaStreamNonBlocking));
+  SFFG_CK(cudaEventCreateWithFlags(&d_->fork_ev, cudaEventDisableTiming));
+  SFFG_CK(cudaEventCreateWithFlags(&d_->join_ev, cudaEventDisableTiming));
   SFFG_CK(cudaDeviceGetAttribute(&d_->nsm, cudaDevAttrMultiProcessorCount, dev));
   // slot and tile layout
   int slot = 0, tile = 0;
@@ -1024,15 +1034,12 @@ int Batch::run_eval_direct(bool rebuild, void *stream) {
                                                d.acc_fy.p, d.acc_fz.p, d.nonfinite.p, d.tile_sys.p, d.xb.p,
                                                kListMove * kListMove, d.counters.p + 4, d.tile_flagB.p);
   SFFG_CK(cudaGetLastError());
-  if (rebuild) {
-    const int rc = build_lists(st);
-    if (rc) return rc;
-  } else {
-    rebuild_list_b(st);
-    SFFG_CK(cudaGetLastError());
-  }
-  const double fsmax = fsmax_all();
-  // bonded and 1-4 terms (FP64)
+  // bonded and 1-4 terms (FP64) on the side stream: they need only x and the
+  // zeroed accumulators, and keep the FP64 units busy while the list upkeep
+  // and the FP32 pair passes run
+  SFFG_CK(cudaEventRecord(d.fork_ev, st));
+  SFFG_CK(cudaStreamWaitEvent(d.side, d.fork_ev, 0));
+  const cudaStream_t bs = d.side;
   BondedArgs ba;
   ba.x = d.x.p;
   ba.atom_slot = d.atom_slot.p;
@@ -1043,15 +1050,24 @@ int Batch::run_eval_direct(bool rebuild, void *stream) {
   ba.energy = d.energy.p;
   ba.sys_active = d.sys_active.p;
   auto blocks = [](size_t n) { return static_cast<int>((n + 127) / 128); };
-  if (d.bond_atoms.n) k_bonds<<<blocks(d.bond_atoms.n), 128, 0, st>>>(ba, d.bond_atoms.p, d.bond_par.p, static_cast<int>(d.bond_atoms.n));
-  if (d.angle_atoms.n) k_angles<<<blocks(d.angle_atoms.n), 128, 0, st>>>(ba, d.angle_atoms.p, d.angle_par.p, static_cast<int>(d.angle_atoms.n));
-  if (d.dih_atoms.n) k_dihedrals<<<blocks(d.dih_atoms.n), 128, 0, st>>>(ba, d.dih_atoms.p, d.dih_par.p, static_cast<int>(d.dih_atoms.n));
-  if (d.p14_atoms.n) k_pairs14<<<blocks(d.p14_atoms.n), 128, 0, st>>>(ba, d.p14_atoms.p, d.p14_par.p, static_cast<int>(d.p14_atoms.n));
+  if (d.bond_atoms.n) k_bonds<<<blocks(d.bond_atoms.n), 128, 0, bs>>>(ba, d.bond_atoms.p, d.bond_par.p, static_cast<int>(d.bond_atoms.n));
+  if (d.angle_atoms.n) k_angles<<<blocks(d.angle_atoms.n), 128, 0, bs>>>(ba, d.angle_atoms.p, d.angle_par.p, static_cast<int>(d.angle_atoms.n));
+  if (d.dih_atoms.n) k_dihedrals<<<blocks(d.dih_atoms.n), 128, 0, bs>>>(ba, d.dih_atoms.p, d.dih_par.p, static_cast<int>(d.dih_atoms.n));
+  if (d.p14_atoms.n) k_pairs14<<<blocks(d.p14_atoms.n), 128, 0, bs>>>(ba, d.p14_atoms.p, d.p14_par.p, static_cast<int>(d.p14_atoms.n));
   if (d.cons_w.n) {
-    k_restraints<<<blocks(d.cons_w.n), 128, 0, st>>>(ba, d.cons_w.p, d.cons_x0.p, static_cast<int>(d.cons_w.n));
+    k_restraints<<<blocks(d.cons_w.n), 128, 0, bs>>>(ba, d.cons_w.p, d.cons_x0.p, static_cast<int>(d.cons_w.n));
     launches_++;
   }
   SFFG_CK(cudaGetLastError());
+  SFFG_CK(cudaEventRecord(d.join_ev, bs));
+  if (rebuild) {
+    const int rc = build_lists(st);
+    if (rc) return rc;
+  } else {
+    rebuild_list_b(st);
+    SFFG_CK(cudaGetLastError());
+  }
+  const double fsmax = fsmax_all();
   // pass 1
   const bool neck = mp_.gb == 7 || mp_.gb == 8;
   const int ring = static_cast<int>(d.ev_head % DeviceState::kRing);
@@ -1123,6 +1139,7 @@ int Batch::run_eval_direct(bool rebuild, void *stream) {
     SFFG_CK(cudaEventRecord(d.events[ring][2][1], st));
     d.ev_head++;
   }
+  SFFG_CK(cudaStreamWaitEvent(st, d.join_ev, 0));
   k_gather_grad<<<(natom_total_ + 255) / 256, 256, 0, st>>>(d.acc_fx.p, d.acc_fy.p, d.acc_fz.p, d.atom_slot.p,
                                                             d.atom_frozen.p, d.atom_sys.p, d.sys_active.p,
                                                             d.grad.p, natom_total_);

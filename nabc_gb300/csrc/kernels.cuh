@@ -400,9 +400,11 @@ __global__ void __launch_bounds__(256, 3) k_born(const DevTables t) {
 // (src/sff/eff.c:1902-2063) over list A.
 template <bool KAPPA>
 __global__ void __launch_bounds__(256, 3) k_gbpair(const DevTables t) {
+  // j-entries of the chunk: position (hi, lo + Born radius) and
+  // (1/R_j^2 / 4, Lennard-Jones row offset type_j * ntypes, column mask,
+  // exclusion mask), three 16-byte reads per step
   __shared__ float4 sm_hi[8][32], sm_lo[8][32];
-  __shared__ float2 sm_aux[8][32];
-  __shared__ unsigned sm_col[8][32], sm_exc[8][32];
+  __shared__ uint4 sm_aux[8][32];
   const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
   const int nchunk = *t.la.nchunk;
   int cur_I = -1, cur_sys = -1;
@@ -450,7 +452,7 @@ __global__ void __launch_bounds__(256, 3) k_gbpair(const DevTables t) {
         xi = h.x; yi = h.y; zi = h.z; qi = h.w; xli = l.x; yli = l.y; zli = l.z;
         ri = t.reff32[sl];
         rvi = t.rinv2[sl];
-        ti = (t.param[sl] & 0xffff) * nt;
+        ti = t.param[sl] & 0xffff;
       }
       unsigned mycol;
       const int sj = chunk_entry(t.la, k, lane, mycol);
@@ -459,9 +461,8 @@ __global__ void __launch_bounds__(256, 3) k_gbpair(const DevTables t) {
         l.w = t.reff32[sj];
         sm_hi[w][lane] = t.pos_hi[sj];
         sm_lo[w][lane] = l;
-        sm_aux[w][lane] = make_float2(t.rinv2[sj], __int_as_float(t.param[sj] & 0xffff));
-        sm_col[w][lane] = mycol;
-        sm_exc[w][lane] = t.la.exc[static_cast<size_t>(k) * 32 + lane];
+        sm_aux[w][lane] = make_uint4(__float_as_uint(t.rinv2[sj]), (t.param[sj] & 0xffff) * nt, mycol,
+                                     t.la.exc[static_cast<size_t>(k) * 32 + lane]);
       }
       const unsigned cols = __ballot_sync(kFull, mycol != 0u);
       __syncwarp();
@@ -476,15 +477,17 @@ __global__ void __launch_bounds__(256, 3) k_gbpair(const DevTables t) {
           ax[s] = ay[s] = az[s] = as[s] = 0.0f;
           if (!((cols >> j) & 1u)) continue;  // padding entry
           const float4 h = sm_hi[w][j], l = sm_lo[w][j];
-          const float2 au = sm_aux[w][j];
+          const uint4 au = sm_aux[w][j];
           const float dx = (xi - h.x) + (xli - l.x);
           const float dy = (yi - h.y) + (yli - l.y);
           const float dz = (zi - h.z) + (zli - l.z);
           const float r2 = fmaf(dx, dx, fmaf(dy, dy, dz * dz));
-          const bool in = (sm_col[w][j] >> lane) & 1u;
-          const bool coul = !((sm_exc[w][j] >> lane) & 1u);
-          const float2 ab = lj[ti + __float_as_int(au.y)];
-          const PairOut o = gb_pair<KAPPA>(t.pair, r2, qi * h.w, ri, l.w, rvi, au.x, coul, ab.x, ab.y);
+          const bool in = (au.z >> lane) & 1u;
+          const bool coul = !((au.w >> lane) & 1u);
+          // row type_j: the lanes' i types fall in one row of the symmetric table
+          const float2 ab = lj[au.y + ti];
+          const PairOut o = gb_pair<KAPPA>(t.pair, r2, qi * h.w, ri, l.w, rvi, __uint_as_float(au.x), coul, ab.x,
+                                           ab.y);
           const float de = in ? o.de : 0.0f;
           fix = fmaf(de, dx, fix);
           fiy = fmaf(de, dy, fiy);

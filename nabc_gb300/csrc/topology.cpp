@@ -113,6 +113,13 @@ void build_host_system(PARMSTRUCT_T *prm, const int *frozen, const Options &o, b
   hs.ntypes = prm->Ntypes;
   hs.lj_a.assign(static_cast<size_t>(prm->Ntypes) * prm->Ntypes, 0.0f);
   hs.lj_b.assign(static_cast<size_t>(prm->Ntypes) * prm->Ntypes, 0.0f);
+  // the pair kernel reads row type_j, column type_i, which is the
+  // reference's row type_i (eff.c:1915, 2015) when the index is symmetric, as
+  // Amber's NONBONDED_PARM_INDEX is by construction
+  for (int a = 0; a < prm->Ntypes; a++)
+    for (int b = 0; b < a; b++)
+      if (prm->Cno[a * prm->Ntypes + b] != prm->Cno[b * prm->Ntypes + a])
+        init_fail("Error: the Lennard-Jones type index (NONBONDED_PARM_INDEX) is not symmetric.");
   for (int a = 0; a < prm->Ntypes; a++)
     for (int b = 0; b < prm->Ntypes; b++) {
       int ic = prm->Cno[a * prm->Ntypes + b] - 1;
