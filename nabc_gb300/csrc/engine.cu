@@ -662,6 +662,19 @@ int Batch::get_energy(int s, double *ene, void *stream) {
   return SFFG_OK;
 }
 
+int Batch::get_energy_grad(int s, double *ene, double *g, void *stream) {
+  if (!finalized_ || s < 0 || s >= num_systems()) return SFFG_EINVAL;
+  const SystemInfo &si = sys_[s];
+  long long e[kEnergySlots];
+  cudaStream_t st = pick(*d_, stream);
+  SFFG_CK(cudaMemcpyAsync(g, d_->grad.p + 3 * static_cast<size_t>(si.atom_off), 3 * sizeof(double) * si.natom,
+                          cudaMemcpyDeviceToHost, st));
+  SFFG_CK(cudaMemcpyAsync(e, d_->energy.p + kEnergySlots * s, sizeof(e), cudaMemcpyDeviceToHost, st));
+  SFFG_CK(cudaStreamSynchronize(st));
+  ene_from_fixed(e, ene);
+  return SFFG_OK;
+}
+
 int Batch::get_all_energies(std::vector<double> &out, void *stream) {
   if (!finalized_) return SFFG_ESTATE;
   const int nsys = num_systems();
@@ -688,6 +701,7 @@ DevTables make_tables(DeviceState &d, const ModelParams &mp, double fsmax, int q
   t.sys_lj_off = d.sys_lj_off.p;
   t.sys_ntypes = d.sys_ntypes.p;
   t.lj = d.lj.p;
+  t.lj_n = static_cast<int>(d.lj.n);
   t.la.chunk_i = d.chunkA_i.p;
   t.la.slot = d.entA_slot.p;
   t.la.col = d.entA_col.p;
@@ -1117,6 +1131,7 @@ int Batch::run_eval_direct(bool rebuild, void *stream) {
   {
     DevTables t = make_tables(d, mp_, fsmax, 6);
     t.claim = cfg_[1].claim;
+    t.lj_shared = opts_.sffg_lj_shared != 0;
     if (tuning_) SFFG_CK(cudaEventRecord(d.tune_ev[1][0], st));
     launch_gbpair(mp_.kappa != 0.0, cfg_[1].blocks, st, t);
     if (tuning_) SFFG_CK(cudaEventRecord(d.tune_ev[1][1], st));

@@ -84,6 +84,8 @@ class Batch {
   // Energy components of the last evaluation in the reference's ene[]
   // layout (13 entries); synchronous.
   int get_energy(int sys, double *ene, void *stream);
+  // Energy components and gradient of one system with a single wait.
+  int get_energy_grad(int sys, double *ene, double *g, void *stream);
   int get_all_energies(std::vector<double> &ene13, void *stream);
 
   // One energy+gradient evaluation of every active system.  rebuild

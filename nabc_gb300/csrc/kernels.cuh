@@ -47,6 +47,8 @@ struct DevTables {
   const int *sys_lj_off;
   const int *sys_ntypes;
   const float2 *lj;       // (A, B) per type pair, per system blocks
+  int lj_n;               // entries of lj
+  bool lj_shared;         // pass 2 may stage lj in shared memory
   // lists: la (r < cut) for pass 2; lb and lc (r < rgbmax + Fsmax + skin,
   // lc the pairs within near-field range) for passes 1 and 3
   ChunkList la, lb, lc;
@@ -398,19 +400,29 @@ __global__ void __launch_bounds__(256, 3) k_born(const DevTables t) {
 // ------------------------------------------------------------------ pass 2
 // GB + Coulomb + Lennard-Jones pair energies, dE/dr and sumdeijda
 // (src/sff/eff.c:1902-2063) over list A.
-template <bool KAPPA>
+// Lennard-Jones tables of up to this many (A, B) entries (all systems of the
+// batch together) are read from shared memory in pass 2.
+constexpr int kLjShared = 4096;
+
+template <bool KAPPA, bool LJS>
 __global__ void __launch_bounds__(256, 3) k_gbpair(const DevTables t) {
   // j-entries of the chunk: position (hi, lo + Born radius) and
   // (1/R_j^2 / 4, Lennard-Jones row offset type_j * ntypes, column mask,
   // exclusion mask), three 16-byte reads per step
   __shared__ float4 sm_hi[8][32], sm_lo[8][32];
   __shared__ uint4 sm_aux[8][32];
+  __shared__ float2 s_lj[LJS ? kLjShared : 1];
+  if (LJS) {
+    for (int i = threadIdx.x; i < t.lj_n; i += blockDim.x) s_lj[i] = t.lj[i];
+    __syncthreads();
+  }
+  const float2 *const lj_all = LJS ? s_lj : t.lj;
   const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
   const int nchunk = *t.la.nchunk;
   int cur_I = -1, cur_sys = -1;
   float xi = 0, yi = 0, zi = 0, xli = 0, yli = 0, zli = 0, qi = 0, ri = 1, rvi = 0;
   int ti = 0, nt = 1;
-  const float2 *lj = t.lj;
+  const float2 *lj = lj_all;
   long long fx64 = 0, fy64 = 0, fz64 = 0, sd64 = 0, ep64 = 0, ee64 = 0, ev64 = 0;
   const float FS = 4294967296.0f;
   auto flush_i = [&]() {
@@ -440,7 +452,7 @@ __global__ void __launch_bounds__(256, 3) k_gbpair(const DevTables t) {
       if (sys != cur_sys) {
         if (cur_sys >= 0) flush_e();
         cur_sys = sys;
-        lj = t.lj + t.sys_lj_off[sys];
+        lj = lj_all + t.sys_lj_off[sys];
         nt = t.sys_ntypes[sys];
       }
       if (I != cur_I) {

@@ -29,6 +29,7 @@ struct Session {
   int natom = 0;
   bool list_built = false;
   NcTrajectory traj;  // md()'s trajectory when mme_init_sff got a file name
+  std::vector<double> scratch;
 };
 
 Session &session() {
@@ -167,12 +168,21 @@ double finish_eval(int iter, double *f) {
   Session &s = session();
   Batch &b = *s.batch;
   double ene[13];
-  check(b.get_energy(0, ene, nullptr), "get_energy");
-  std::vector<double> g(3 * static_cast<size_t>(s.natom));
-  check(b.get_grad(0, g.data(), nullptr), "get_grad");
-  if (f) std::memcpy(f, g.data(), g.size() * sizeof(double));
+  // the gradient goes straight into the caller's f (scratch when f is NULL)
+  double *g = f;
+  if (!g) {
+    s.scratch.resize(3 * static_cast<size_t>(s.natom));
+    g = s.scratch.data();
+  }
+  check(b.get_energy_grad(0, ene, g, nullptr), "get_energy");
   if (options().gb_debug) print_radii(b);
-  print_energies(iter, ene, frms_of(g));
+  // frms only for the lines that print it
+  const Options &o = options();
+  if (iter == -1 || (iter > -1 && (iter == 0 || iter % o.ntpr == 0))) {
+    double frms = 0.0;
+    for (int i = 0; i < 3 * s.natom; i++) frms += g[i] * g[i];
+    print_energies(iter, ene, std::sqrt(frms / (3 * s.natom)));
+  }
   return ene[0];
 }
 

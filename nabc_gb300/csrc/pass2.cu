@@ -4,14 +4,22 @@
 namespace sffg {
 
 void launch_gbpair(bool kappa, int grid, cudaStream_t st, const DevTables &t) {
-  if (kappa) k_gbpair<true><<<grid, 256, 0, st>>>(t);
-  else k_gbpair<false><<<grid, 256, 0, st>>>(t);
+  const bool ljs = t.lj_shared && t.lj_n <= kLjShared;
+  if (kappa) {
+    if (ljs) k_gbpair<true, true><<<grid, 256, 0, st>>>(t);
+    else k_gbpair<true, false><<<grid, 256, 0, st>>>(t);
+  } else {
+    if (ljs) k_gbpair<false, true><<<grid, 256, 0, st>>>(t);
+    else k_gbpair<false, false><<<grid, 256, 0, st>>>(t);
+  }
 }
 
+// Resident blocks per SM of the shared-table form (the one the tuner and
+// the default grid size use; the global-table form fits at least as many).
 int gbpair_blocks_per_sm(bool kappa) {
   int occ = 0;
-  if (kappa) cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, k_gbpair<true>, 256, 0);
-  else cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, k_gbpair<false>, 256, 0);
+  if (kappa) cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, k_gbpair<true, true>, 256, 0);
+  else cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, k_gbpair<false, true>, 256, 0);
   return occ > 0 ? occ : 1;
 }
 

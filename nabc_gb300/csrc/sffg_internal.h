@@ -37,6 +37,7 @@ struct Options {
   unsigned long long sffg_seed = 0x5eedULL;
   int sffg_graph = 1;           // capture the md/cg step in a CUDA graph
   int sffg_tune = 1;            // autotune the pair passes' work split
+  int sffg_lj_shared = 1;       // pass 2 reads small Lennard-Jones tables from shared memory
   int sffg_warps = 8;           // warps per CTA for the pair kernels (0 = tuned)
   int sffg_verbose = 0;
 };

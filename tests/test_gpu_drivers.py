@@ -131,6 +131,30 @@ def test_graph_replay_bit_identical(lib):
     sff.free_prm(prm)
 
 
+def test_lj_table_shared_and_global_bit_identical(lib, checks):
+    """Pass 2 reads the Lennard-Jones table from shared memory when it is
+    small (sffg_lj_shared=1) and from global memory otherwise; both give the
+    same bits, on a batch of the reference's test systems with kappa and
+    without."""
+    from nabc_gb300.batch import Batch
+    out = []
+    for kappa in (0.0, 0.10395):
+        for ljs in (1, 0):
+            b = Batch(f"gb=5, cut=99.0, rgbmax=15.0, kappa={kappa}, sffg_lj_shared={ljs}")
+            prms = []
+            for name in ("gbrna", "gbtrx", "xfin"):
+                prm, x = load_case(checks[name])
+                prms.append(prm)
+                b.add(prm, x)
+            b.finalize()
+            b.eval()
+            out.append([(b.energy(s), b.grad(s)) for s in range(3)])
+            b.close()
+    for a, c in ((out[0], out[1]), (out[2], out[3])):
+        for (e1, g1), (e2, g2) in zip(a, c):
+            assert np.array_equal(e1, e2) and np.array_equal(g1, g2)
+
+
 def test_autotuned_split_bit_identical(lib):
     """The autotuner picks the work split of each pass by timing; the
     results are the same bits with or without it."""
