@@ -1155,14 +1155,14 @@ int Batch::run_eval_direct(bool rebuild, void *stream) {
     d.ev_head++;
   }
   SFFG_CK(cudaStreamWaitEvent(st, d.join_ev, 0));
+  // natom_total_ >= nsys: the gather's threads also cover the totals
   k_gather_grad<<<(natom_total_ + 255) / 256, 256, 0, st>>>(d.acc_fx.p, d.acc_fy.p, d.acc_fz.p, d.atom_slot.p,
                                                             d.atom_frozen.p, d.atom_sys.p, d.sys_active.p,
-                                                            d.grad.p, natom_total_);
-  k_energy_total<<<(nsys + 127) / 128, 128, 0, st>>>(d.energy.p, d.etot.p, nsys);
+                                                            d.grad.p, natom_total_, d.energy.p, d.etot.p, nsys);
   SFFG_CK(cudaGetLastError());
   // pack, four bonded kinds (when present), three pair kernels, Born finish,
-  // chain prep, gather, energy total
-  launches_ += 9 + (d.bond_atoms.n > 0) + (d.angle_atoms.n > 0) + (d.dih_atoms.n > 0) + (d.p14_atoms.n > 0);
+  // chain prep, gather with the energy totals
+  launches_ += 8 + (d.bond_atoms.n > 0) + (d.angle_atoms.n > 0) + (d.dih_atoms.n > 0) + (d.p14_atoms.n > 0);
   timers().nevals++;
   return SFFG_OK;
 }

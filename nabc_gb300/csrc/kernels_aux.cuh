@@ -461,24 +461,9 @@ __global__ void __launch_bounds__(kComThreads) k_com_remove(double *x, double *v
   }
 }
 
-__global__ void k_gather_grad(const long long *acc_fx, const long long *acc_fy, const long long *acc_fz,
-                              const int *atom_slot, const int *atom_frozen, const int *atom_sys,
-                              const int *sys_active, double *grad, int natom) {
-  const int a = blockIdx.x * blockDim.x + threadIdx.x;
-  if (a >= natom || !sys_active[atom_sys[a]]) return;
-  const int s = atom_slot[a];
-  const double k = 1.0 / 4294967296.0;
-  const bool fz = atom_frozen[a];
-  grad[3 * a] = fz ? 0.0 : static_cast<double>(acc_fx[s]) * k;
-  grad[3 * a + 1] = fz ? 0.0 : static_cast<double>(acc_fy[s]) * k;
-  grad[3 * a + 2] = fz ? 0.0 : static_cast<double>(acc_fz[s]) * k;
-}
-
-// Total energy per system from the fixed-point slots, summed in the
+// Total energy of system s from the fixed-point slots, summed in the
 // reference's ene[1..12] order (src/sff/eff.c:2871-2874).
-__global__ void k_energy_total(const long long *energy, double *etot, int nsys) {
-  const int s = blockIdx.x * blockDim.x + threadIdx.x;
-  if (s >= nsys) return;
+__device__ __forceinline__ double energy_total(const long long *energy, int s) {
   const double k = 1.0 / 4294967296.0;
   const long long *e = energy + s * kEnergySlots;
   double ene[13] = {0};
@@ -493,7 +478,24 @@ __global__ void k_energy_total(const long long *energy, double *etot, int nsys) 
   ene[10] = e[E_EGB] * k;
   double t = 0.0;
   for (int i = 1; i <= 12; i++) t += ene[i];
-  etot[s] = t;
+  return t;
+}
+
+// The gradient of every atom and, on the first nsys threads, every
+// system's total energy.
+__global__ void k_gather_grad(const long long *acc_fx, const long long *acc_fy, const long long *acc_fz,
+                              const int *atom_slot, const int *atom_frozen, const int *atom_sys,
+                              const int *sys_active, double *grad, int natom, const long long *energy,
+                              double *etot, int nsys) {
+  const int a = blockIdx.x * blockDim.x + threadIdx.x;
+  if (a < nsys) etot[a] = energy_total(energy, a);
+  if (a >= natom || !sys_active[atom_sys[a]]) return;
+  const int s = atom_slot[a];
+  const double k = 1.0 / 4294967296.0;
+  const bool fz = atom_frozen[a];
+  grad[3 * a] = fz ? 0.0 : static_cast<double>(acc_fx[s]) * k;
+  grad[3 * a + 1] = fz ? 0.0 : static_cast<double>(acc_fy[s]) * k;
+  grad[3 * a + 2] = fz ? 0.0 : static_cast<double>(acc_fz[s]) * k;
 }
 
 // ------------------------------------------------------------ dynamics

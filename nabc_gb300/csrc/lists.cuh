@@ -209,8 +209,18 @@ __global__ void k_list_columns(const ListArgs a) {
   const unsigned prevA = GB_ONLY ? a.colA[static_cast<size_t>(c) * 32 + lane] : 0u;
   unsigned colA = 0, colB = 0, colC = 0, colE = 0;
   const float gbb = a.gbb2f * 1.0001f + 1e-3f;
-  for (int i = 0; i < 32; i++) {
-    if (!((vI >> i) & 1u)) continue;  // warp-uniform
+  // rows to test (warp-uniform): every valid i-atom, or for a remake only
+  // those with a list-A pair in this tile pair
+  unsigned rows = prevA;
+  if (GB_ONLY) {
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) rows |= __shfl_xor_sync(kFull, rows, o);
+  } else {
+    rows = ~0u;
+  }
+  rows &= vI;
+  for (; rows; rows &= rows - 1u) {
+    const int i = __ffs(rows) - 1;
     const float4 hi = s_hi[w][i], li = s_lo[w][i];
     const float dx = (hi.x - hj.x) + (li.x - lj.x);
     const float dy = (hi.y - hj.y) + (li.y - lj.y);
