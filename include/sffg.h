@@ -108,6 +108,21 @@ int sffg_batch_get_velocities(sffg_batch *b, int sys, double *v, void *stream);
 int sffg_batch_cg(sffg_batch *b, int maxiter, double rmsgrad, double dfpred, int *status,
                   double *energy, void *stream);
 
+/* XMIN on every system at once (no counterpart in the reference, whose
+ * xmin(), src/sff/xminC.c:2997, minimises one system): each system runs its
+ * own copy of the reference's minimiser with the options xo
+ * (mol_struct_opt must be 1; print_level is ignored), and their energy
+ * evaluations are batched on the GPU.  The pair lists are rebuilt for the
+ * whole batch whenever any system's minimiser asks for a rebuild; that
+ * regroups the other systems' lists (and, with a finite cutoff, may change
+ * their pair sets), so a system of a mixed batch follows its lone run only
+ * to FP32 rounding, while a one-system batch ends bit for bit where xmin()
+ * over mme() ends.  Runs are deterministic.  status[s] receives the system's error_flag (0
+ * or the reference's negative code), iters[s] its iteration count and
+ * energy[s] its final energy (0 on an error); any may be NULL.  The
+ * minimised coordinates stay in the batch (sffg_batch_get_coords). */
+int sffg_batch_xmin(sffg_batch *b, const XMIN_OPT_T *xo, int *status, int *iters, double *energy, void *stream);
+
 /* Kernel launches issued by this batch since it was created. */
 long long sffg_batch_launch_count(const sffg_batch *b);
 /* With profiling on, the three pair passes of every evaluation are

@@ -94,6 +94,23 @@ class Batch:
                "cg")
         return st, en
 
+    def xmin(self, stream=None, **opts):
+        """The reference's XMIN on every system (sffg_batch_xmin); opts set
+        fields of XMIN_OPT_T over xmin_opt_init's defaults (method, maxiter,
+        grms_tol, ls_maxatmov, ...).  Returns (status, iterations, energy)
+        per system; the minimised coordinates stay in the batch."""
+        L = sff.lib()
+        xo = sff.XMIN_OPT_T()
+        L.xmin_opt_init(C.byref(xo))
+        for k, v in opts.items():
+            setattr(xo, k, v)
+        n = len(self.natoms)
+        st = np.zeros(n, np.int32)
+        it = np.zeros(n, np.int32)
+        en = np.zeros(n)
+        _check(L.sffg_batch_xmin(self.h, C.byref(xo), sff.iptr(st), sff.iptr(it), sff.dptr(en), stream), "xmin")
+        return st, it, en
+
     def md_begin(self, stream=None):
         _check(sff.lib().sffg_batch_md_begin(self.h, stream), "md_begin")
 

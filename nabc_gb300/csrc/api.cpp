@@ -119,6 +119,21 @@ extern "C" int sffg_batch_cg(sffg_batch *b, int maxiter, double rmsgrad, double 
   return SFFG_OK;
 }
 
+extern "C" int sffg_batch_xmin(sffg_batch *b, const XMIN_OPT_T *xo, int *status, int *iters, double *energy,
+                               void *stream) {
+  if (!b || !xo) return fail(SFFG_EINVAL, "null batch or options");
+  std::vector<int> st, it;
+  std::vector<double> en;
+  const int rc = b->impl->xmin(*xo, st, it, en, stream);
+  if (rc) return pass(b->impl, rc);
+  for (size_t s = 0; s < st.size(); s++) {
+    if (status) status[s] = st[s];
+    if (iters) iters[s] = it[s];
+    if (energy) energy[s] = en[s];
+  }
+  return SFFG_OK;
+}
+
 extern "C" int sffg_batch_md_begin(sffg_batch *b, void *stream) {
   SFFG_WRAP(b->impl->md_begin(false, nullptr, nullptr, stream));
 }

@@ -675,6 +675,33 @@ int Batch::get_energy_grad(int s, double *ene, double *g, void *stream) {
   return SFFG_OK;
 }
 
+int Batch::set_all_coords(const double *x, void *stream) {
+  if (!finalized_) return SFFG_ESTATE;
+  SFFG_CK(cudaMemcpyAsync(d_->x.p, x, 3 * sizeof(double) * natom_total_, cudaMemcpyHostToDevice, pick(*d_, stream)));
+  return SFFG_OK;
+}
+
+int Batch::set_all_active(const std::vector<int> &on, void *stream) {
+  if (!finalized_ || static_cast<int>(on.size()) != num_systems()) return SFFG_EINVAL;
+  note_active(on);
+  SFFG_CK(cudaMemcpyAsync(d_->sys_active.p, ones_.data(), ones_.size() * sizeof(int), cudaMemcpyHostToDevice,
+                          pick(*d_, stream)));
+  return SFFG_OK;
+}
+
+int Batch::get_all_energy_grad(std::vector<double> &out, double *grad, void *stream) {
+  if (!finalized_) return SFFG_ESTATE;
+  const int nsys = num_systems();
+  std::vector<long long> e(kEnergySlots * static_cast<size_t>(nsys));
+  cudaStream_t st = pick(*d_, stream);
+  SFFG_CK(cudaMemcpyAsync(grad, d_->grad.p, 3 * sizeof(double) * natom_total_, cudaMemcpyDeviceToHost, st));
+  SFFG_CK(cudaMemcpyAsync(e.data(), d_->energy.p, e.size() * sizeof(long long), cudaMemcpyDeviceToHost, st));
+  SFFG_CK(cudaStreamSynchronize(st));
+  out.resize(13 * static_cast<size_t>(nsys));
+  for (int s = 0; s < nsys; s++) ene_from_fixed(&e[kEnergySlots * s], &out[13 * s]);
+  return SFFG_OK;
+}
+
 int Batch::get_all_energies(std::vector<double> &out, void *stream) {
   if (!finalized_) return SFFG_ESTATE;
   const int nsys = num_systems();
@@ -884,6 +911,7 @@ int Batch::build_lists(void *stream) {
     launches_ += 3;
   }
   have_list_ = true;
+  list_builds_++;
   return SFFG_OK;
 }
 
@@ -1693,8 +1721,9 @@ int Batch::cg_begin(const std::vector<int> &maxiter, const std::vector<double> &
   }
   cg_host_.assign(init.begin(), init.end());
   SFFG_CK(cudaMemcpyAsync(d.cg_state.p, cg_host_.data(), nsys * sizeof(CgState), cudaMemcpyHostToDevice, st));
-  ones_.assign(nsys, 1);
+  note_active(std::vector<int>(nsys, 1));
   SFFG_CK(cudaMemcpyAsync(d.sys_active.p, ones_.data(), nsys * sizeof(int), cudaMemcpyHostToDevice, st));
+  cg_list_builds_ = list_builds_;
   cg_nsys_ = nsys;
   SFFG_CK(cudaMemcpyAsync(d.cg_nactive.p, &cg_nsys_, sizeof(int), cudaMemcpyHostToDevice, st));
   cg_turn_ = 0;
@@ -1765,10 +1794,21 @@ int Batch::set_noise_key(int sys, unsigned long long key) {
   return SFFG_OK;
 }
 
+// List builds leave out inactive systems, so a system switched back on
+// needs a rebuild before its next evaluation.
+void Batch::note_active(const std::vector<int> &on) {
+  ones_.resize(num_systems(), 1);
+  for (size_t s = 0; s < on.size(); s++) {
+    if (on[s] && !ones_[s]) have_list_ = false;
+    ones_[s] = on[s];
+  }
+}
+
 int Batch::set_active(int sys, bool on, void *stream) {
   if (!finalized_ || sys < 0 || sys >= num_systems()) return SFFG_EINVAL;
   DeviceState &d = *d_;
-  ones_.resize(num_systems());
+  ones_.resize(num_systems(), 1);
+  if (on && !ones_[sys]) have_list_ = false;
   ones_[sys] = on ? 1 : 0;
   SFFG_CK(cudaMemcpyAsync(d.sys_active.p + sys, &ones_[sys], sizeof(int), cudaMemcpyHostToDevice, pick(d, stream)));
   return SFFG_OK;
@@ -1777,7 +1817,10 @@ int Batch::set_active(int sys, bool on, void *stream) {
 int Batch::cg_end(void *stream) {
   DeviceState &d = *d_;
   cudaStream_t st = pick(d, stream);
-  ones_.assign(num_systems(), 1);
+  // a system the minimiser switched off on the device misses the list
+  // rebuilds made after it ended
+  if (num_systems() > 1 && list_builds_ != cg_list_builds_) have_list_ = false;
+  note_active(std::vector<int>(num_systems(), 1));
   SFFG_CK(cudaMemcpyAsync(d.sys_active.p, ones_.data(), ones_.size() * sizeof(int), cudaMemcpyHostToDevice, st));
   SFFG_CK(cudaStreamSynchronize(st));
   return SFFG_OK;

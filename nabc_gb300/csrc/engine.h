@@ -87,6 +87,16 @@ class Batch {
   // Energy components and gradient of one system with a single wait.
   int get_energy_grad(int sys, double *ene, double *g, void *stream);
   int get_all_energies(std::vector<double> &ene13, void *stream);
+  // Whole-batch transfers with one wait: coordinates of every system (atom
+  // order, systems in order), the active flags, and every system's energy
+  // components (13 each) with the whole gradient.
+  int set_all_coords(const double *x, void *stream);
+  int set_all_active(const std::vector<int> &on, void *stream);
+  int get_all_energy_grad(std::vector<double> &ene13, double *grad, void *stream);
+  // XMIN on every system at once (csrc/batch_xmin.cpp): status, iteration
+  // count and final energy per system.
+  int xmin(const XMIN_OPT_T &xo, std::vector<int> &status, std::vector<int> &iters, std::vector<double> &energy,
+           void *stream);
 
   // One energy+gradient evaluation of every active system.  rebuild
   // requests a pair-list rebuild first (always done on the first call).
@@ -179,7 +189,9 @@ class Batch {
   bool tuned_ = false, tuning_ = false;
   // conjgrad driver state (host copies of the device state machines)
   std::vector<CgState> cg_host_;
-  std::vector<int> ones_;
+  std::vector<int> ones_;  // the active flags last sent to the device
+  long long list_builds_ = 0, cg_list_builds_ = 0;
+  void note_active(const std::vector<int> &on);
   int cg_nsys_ = 0, cg_turn_ = 0, cg_maxiter_ = 0;
   long long cand_max_ = 0;  // candidate tile pairs the batch could ever need
   int ncand_ = 0;           // candidates of the current pair list

@@ -5,6 +5,7 @@
 
 #include <cstdint>
 #include <cstdio>
+#include <memory>
 #include <string>
 #include <vector>
 
@@ -64,6 +65,30 @@ class NcTrajectory {
   FILE *fp_ = nullptr;
   int natom_ = 0, frames_ = 0;
   unsigned long long data_begin_ = 0, record_bytes_ = 0;
+};
+
+// One XMIN minimisation driven by reverse communication (csrc/xmin.cpp):
+// start() takes the options, the coordinates and the gradient at them;
+// while start() or resume() return 1, evaluate energy and gradient at xyz
+// (request: the reference's return_flag, 4-6 rebuild the pair list, 7-9
+// keep it) and resume().  0: done, xyz holds the result; < 0: the
+// reference's error status.
+class XminJob {
+ public:
+  XminJob();
+  ~XminJob();
+  int start(const XMIN_OPT_T &xo, int natm, double *xyz, const double *grad, double energy, int *request);
+  int resume(double energy, const double *grad, double *xyz, int *request);
+  int iter() const { return iter_; }
+  int ls_iter() const { return ls_iter_; }
+  double grms() const { return grms_; }
+  double time() const { return time_; }
+
+ private:
+  struct Impl;
+  std::unique_ptr<Impl> impl_;
+  int iter_ = 0, ls_iter_ = 0;
+  double grms_ = 0.0, time_ = 0.0;
 };
 
 // ---------------------------------------------------------------- model

@@ -839,22 +839,18 @@ class Run {
   }
 };
 
-// The reverse-communication run in progress (xminC keeps one, as the
-// reference's file-scope state does).
+// One run's reverse-communication state: the moving atoms and the
+// coroutine.
 struct Active {
   std::unique_ptr<Run> run;
   std::unique_ptr<Gen> gen;
   bool mol = true;
   std::vector<int> atoms;  // moving atoms, in order (mol_struct_opt = 1)
 };
-Active &active() {
-  static Active a;
-  return a;
-}
 
-void load_in(Active &a, const double *enrg, const double *grad_ext) {
+void load_in(Active &a, double enrg, const double *grad_ext) {
   Run &r = *a.run;
-  r.e = *enrg;
+  r.e = enrg;
   if (a.mol) {
     for (size_t k = 0; k < a.atoms.size(); k++)
       for (int c = 0; c < 3; c++) r.g[3 * k + c] = grad_ext[3 * a.atoms[k] + c];
@@ -910,6 +906,107 @@ int check_params(int maxiter, double grms_tol, int m, int print_level, int natm,
 
 }  // namespace
 
+namespace sffg {
+
+struct XminJob::Impl {
+  Active a;
+};
+
+XminJob::XminJob() : impl_(new Impl) {}
+XminJob::~XminJob() = default;
+
+int XminJob::start(const XMIN_OPT_T &xo, int natm, double *xyz, const double *grad, double energy, int *request) {
+  Active &a = impl_->a;
+  a.gen.reset();
+  a.run.reset();
+  int rc = check_params(xo.maxiter, xo.grms_tol, xo.m_lbfgs, xo.print_level, natm, xo.ls_maxiter, xo.ls_maxatmov,
+                        xo.beta_armijo, xo.c_armijo, xo.mu_armijo);
+  if (!rc && (xo.method < 1 || xo.method > 4)) {
+    std::fprintf(stderr, "\nERROR in xmin(): Unknown minimization method.\n");
+    rc = kParamsError;
+  }
+  if (!rc && xo.method != 4 && xo.ls_method != 1 && xo.ls_method != 2) {
+    std::fprintf(stderr, "\nERROR in xmin(): Unknown line search method.\n");
+    rc = kParamsError;
+  }
+  if (!rc && xo.method != 4 && xo.numdiff != 1 && xo.numdiff != 2) {
+    std::fprintf(stderr, "\nERROR in xmin(): Unknown finite difference method.\n");
+    rc = kParamsError;
+  }
+  a.mol = xo.mol_struct_opt != 0;
+  a.atoms.clear();
+  if (!rc && a.mol) {
+    for (int i = 0; i < natm; i++)
+      if (grad[3 * i] != 0 || grad[3 * i + 1] != 0 || grad[3 * i + 2] != 0) a.atoms.push_back(i);
+    if (a.atoms.size() < 2) {
+      std::fprintf(stderr, "\nERROR in xmin(): Too few moving atoms.\n");
+      rc = kParamsError;
+    }
+  }
+  if (rc) return rc;
+  Params p;
+  p.method = xo.method;
+  p.numdiff = xo.numdiff;
+  p.m = xo.m_lbfgs;
+  p.ls_method = xo.ls_method;
+  p.ls_maxiter = xo.ls_maxiter;
+  p.maxiter = xo.maxiter;
+  p.grms_tol = xo.grms_tol;
+  p.ls_maxatmov = xo.ls_maxatmov;
+  p.beta_armijo = xo.beta_armijo;
+  p.c_armijo = xo.c_armijo;
+  p.mu_armijo = xo.mu_armijo;
+  p.ftol_wolfe = xo.ftol_wolfe;
+  p.gtol_wolfe = xo.gtol_wolfe;
+  const int ndim = a.mol ? 3 * static_cast<int>(a.atoms.size()) : natm;
+  a.run = std::make_unique<Run>(p, ndim);
+  if (a.mol) {
+    for (size_t k = 0; k < a.atoms.size(); k++)
+      for (int c = 0; c < 3; c++) a.run->x[3 * k + c] = xyz[3 * a.atoms[k] + c];
+  } else {
+    for (int i = 0; i < ndim; i++) a.run->x[i] = xyz[i];
+  }
+  a.gen = std::make_unique<Gen>(a.run->main());
+  return resume(energy, grad, xyz, request);
+}
+
+int XminJob::resume(double energy, const double *grad, double *xyz, int *request) {
+  Active &a = impl_->a;
+  if (!a.gen) {
+    std::fprintf(stderr, "\nERROR in xmin(): Illegal status.\n");
+    return -2;
+  }
+  load_in(a, energy, grad);
+  Run &r = *a.run;
+  const bool more = a.gen->next();
+  iter_ = r.iter_out;
+  ls_iter_ = r.ls_iter_out;
+  time_ = r.total_time;
+  grms_ = r.grms_out;
+  if (more) {
+    store_out(a, xyz);
+    *request = a.gen->request();
+    return 1;
+  }
+  const int status = a.gen->status();
+  if (status >= 0) store_out(a, xyz);
+  *request = kDone;
+  a.gen.reset();
+  a.run.reset();
+  return status < 0 ? status : 0;
+}
+
+}  // namespace sffg
+
+namespace {
+// The reverse-communication run of xminC (one at a time, as the reference's
+// file-scope state).
+sffg::XminJob &active_job() {
+  static sffg::XminJob j;
+  return j;
+}
+}  // namespace
+
 extern "C" {
 
 // Reverse-communication XMIN (src/sff/xminC.c:2491-2972).  Call with
@@ -923,90 +1020,53 @@ double xminC(int *xyz_min, int *minim_method, int *maxiter, double *grms_tol, in
              double *total_time, int *print_level, int *ls_method, int *ls_maxiter, int *ls_iter,
              double *ls_maxatmov, double *beta_armijo, double *c_armijo, double *mu_armijo, double *ftol_wolfe,
              double *gtol_wolfe, int *return_flag, int *label) {
-  Active &a = active();
+  sffg::XminJob &job = active_job();
+  int request = 0, rc;
   if (*label == 0) {
-    a.gen.reset();
-    a.run.reset();
-    int rc = check_params(*maxiter, *grms_tol, *m_lbfgs, *print_level, *natm_ext, *ls_maxiter, *ls_maxatmov,
-                          *beta_armijo, *c_armijo, *mu_armijo);
-    if (!rc && (*minim_method < 1 || *minim_method > 4)) {
-      std::fprintf(stderr, "\nERROR in xmin(): Unknown minimization method.\n");
-      rc = kParamsError;
-    }
-    if (!rc && *minim_method != 4 && *ls_method != 1 && *ls_method != 2) {
-      std::fprintf(stderr, "\nERROR in xmin(): Unknown line search method.\n");
-      rc = kParamsError;
-    }
-    if (!rc && *minim_method != 4 && *numdiff != 1 && *numdiff != 2) {
-      std::fprintf(stderr, "\nERROR in xmin(): Unknown finite difference method.\n");
-      rc = kParamsError;
-    }
-    a.mol = *xyz_min != 0;
-    a.atoms.clear();
-    if (!rc && a.mol) {
-      for (int i = 0; i < *natm_ext; i++)
-        if (grad_ext[3 * i] != 0 || grad_ext[3 * i + 1] != 0 || grad_ext[3 * i + 2] != 0) a.atoms.push_back(i);
-      if (a.atoms.size() < 2) {
-        std::fprintf(stderr, "\nERROR in xmin(): Too few moving atoms.\n");
-        rc = kParamsError;
-      }
-    }
-    if (rc) {
+    XMIN_OPT_T xo;
+    xo.mol_struct_opt = *xyz_min;
+    xo.method = *minim_method;
+    xo.maxiter = *maxiter;
+    xo.grms_tol = *grms_tol;
+    xo.m_lbfgs = *m_lbfgs;
+    xo.numdiff = *numdiff;
+    xo.print_level = *print_level;
+    xo.ls_method = *ls_method;
+    xo.ls_maxiter = *ls_maxiter;
+    xo.ls_maxatmov = *ls_maxatmov;
+    xo.beta_armijo = *beta_armijo;
+    xo.c_armijo = *c_armijo;
+    xo.mu_armijo = *mu_armijo;
+    xo.ftol_wolfe = *ftol_wolfe;
+    xo.gtol_wolfe = *gtol_wolfe;
+    rc = job.start(xo, *natm_ext, xyz_ext, grad_ext, *enrg, &request);
+    if (rc == kParamsError) {  // before any run: outputs untouched
       *label = rc;
       return 0.0;
     }
-    Params p;
-    p.method = *minim_method;
-    p.numdiff = *numdiff;
-    p.m = *m_lbfgs;
-    p.ls_method = *ls_method;
-    p.ls_maxiter = *ls_maxiter;
-    p.maxiter = *maxiter;
-    p.grms_tol = *grms_tol;
-    p.ls_maxatmov = *ls_maxatmov;
-    p.beta_armijo = *beta_armijo;
-    p.c_armijo = *c_armijo;
-    p.mu_armijo = *mu_armijo;
-    p.ftol_wolfe = *ftol_wolfe;
-    p.gtol_wolfe = *gtol_wolfe;
-    const int ndim = a.mol ? 3 * static_cast<int>(a.atoms.size()) : *natm_ext;
-    a.run = std::make_unique<Run>(p, ndim);
-    if (a.mol) {
-      for (size_t k = 0; k < a.atoms.size(); k++)
-        for (int c = 0; c < 3; c++) a.run->x[3 * k + c] = xyz_ext[3 * a.atoms[k] + c];
-    } else {
-      for (int i = 0; i < ndim; i++) a.run->x[i] = xyz_ext[i];
-    }
-    a.gen = std::make_unique<Gen>(a.run->main());
-  } else if (*label != 1 || !a.gen) {
+  } else if (*label != 1) {
     std::fprintf(stderr, "\nERROR in xmin(): Illegal status.\n");
     *label = -2;
     return 0.0;
+  } else {
+    rc = job.resume(*enrg, grad_ext, xyz_ext, &request);
   }
-  load_in(a, enrg, grad_ext);
-  const bool more = a.gen->next();
-  Run &r = *a.run;
-  *iter = r.iter_out;
-  *ls_iter = r.ls_iter_out;
-  *total_time = r.total_time;
-  *grms = r.grms_out;
-  if (more) {
-    store_out(a, xyz_ext);
-    *return_flag = a.gen->request();
+  *iter = job.iter();
+  *ls_iter = job.ls_iter();
+  *total_time = job.time();
+  *grms = job.grms();
+  if (rc == 1) {
+    *return_flag = request;
     *label = 1;
     return 0.0;
   }
-  const int status = a.gen->status();
-  if (status < 0) {
-    *label = status;
-  } else {
-    store_out(a, xyz_ext);
-    *return_flag = kDone;
-    *label = 0;
+  if (rc < 0) {
+    *label = rc;
+    return 0.0;
   }
-  a.gen.reset();
-  a.run.reset();
-  return status < 0 ? 0.0 : *enrg;
+  *return_flag = kDone;
+  *label = 0;
+  return *enrg;
 }
 
 // The options' defaults (src/sff/xminC.c:2976-2995).

@@ -133,6 +133,7 @@ def lib():
         L.sffg_batch_num_pairs.restype = C.c_longlong
         L.sffg_batch_md.argtypes = [vp, C.c_int, vp]
         L.sffg_batch_cg.argtypes = [vp, C.c_int, C.c_double, C.c_double, INT_P, REAL_P, vp]
+        L.sffg_batch_xmin.argtypes = [vp, C.POINTER(XMIN_OPT_T), INT_P, INT_P, REAL_P, vp]
         L.sffg_batch_md_begin.argtypes = [vp, vp]
         L.sffg_batch_md_steps.argtypes = [vp, C.c_int, C.c_int, vp]
         L.sffg_batch_launch_count.argtypes = [vp]
