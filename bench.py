@@ -215,6 +215,21 @@ def bench_batched(args, stream, sp, flush):
     res["cg_ms_per_step"] = (time.perf_counter() - t0) * 1e3 / args.cg_steps
     res["cg_conformer_steps_per_s"] = args.conformers * args.cg_steps / (time.perf_counter() - t0)
     b.close()
+    # the same conformers through batched XMIN (L-BFGS, the reference's
+    # minimiser per conformer, evaluations batched)
+    from nabc_gb300.batch import Batch
+    bx = Batch(CONFORMER_OPTS)
+    for prm_c, x_c in confs:
+        bx.add(prm_c, x_c)
+    bx.finalize()
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    st, it, en = bx.xmin(method=2, maxiter=args.xmin_iters, grms_tol=0.01)
+    xs = time.perf_counter() - t0
+    bx.close()
+    res["xmin_lbfgs_iterations"] = args.xmin_iters
+    res["xmin_conformer_iterations_per_s"] = float(np.sum(it)) / xs
+    res["xmin_seconds"] = xs
     out["conformers"] = res
     return out
 
@@ -312,6 +327,7 @@ def main():
     ap.add_argument("--uneven", type=int, default=512, help="molecules in the uneven-size batch (2048: full size)")
     ap.add_argument("--conformers", type=int, default=512, help="conformers in the conformer batch")
     ap.add_argument("--cg-steps", type=int, default=200, help="batched conjgrad steps on the conformers")
+    ap.add_argument("--xmin-iters", type=int, default=50, help="batched L-BFGS iterations on the conformers")
     ap.add_argument("--no-batched", action="store_true", help="skip the batched-versus-plain measurements")
     ap.add_argument("--no-tune", action="store_true",
                     help="default work split instead of the autotuned one (for profiler runs, whose timing the "

@@ -17,6 +17,8 @@
 // pair sets), so a system in a mixed batch follows its lone run to rounding
 // only; a one-system batch has the lone run's rebuild points and ends bit
 // for bit where xmin() over mme() ends.  Runs are deterministic.
+#include <algorithm>
+#include <thread>
 #include <vector>
 
 #include "engine.h"
@@ -75,11 +77,25 @@ int Batch::xmin(const XMIN_OPT_T &xo_in, std::vector<int> &status, std::vector<i
     if ((rc = set_all_coords(x.data(), stream))) return rc;
     if ((rc = eval(rebuild, stream))) return rc;
     if ((rc = get_all_energy_grad(ene, g.data(), stream))) return rc;
-    for (int s = 0; s < nsys; s++) {
-      if (!state[s]) continue;
-      const size_t o = 3 * static_cast<size_t>(sys_[s].atom_off);
-      energy[s] = ene[13 * s];
-      settle(s, jobs[s].resume(ene[13 * s], g.data() + o, x.data() + o, &request[s]));
+    // the minimisers are independent: resume them on the host's cores
+    // (each system's arithmetic is the same on any thread)
+    auto resume_range = [&](int s0, int s1) {
+      for (int s = s0; s < s1; s++) {
+        if (!state[s]) continue;
+        const size_t o = 3 * static_cast<size_t>(sys_[s].atom_off);
+        energy[s] = ene[13 * s];
+        settle(s, jobs[s].resume(ene[13 * s], g.data() + o, x.data() + o, &request[s]));
+      }
+    };
+    const int nthr = std::min<int>(std::max(1u, std::thread::hardware_concurrency()), (nsys + 3) / 4);
+    if (nthr <= 1) {
+      resume_range(0, nsys);
+    } else {
+      std::vector<std::thread> pool;
+      for (int k = 0; k < nthr; k++)
+        pool.emplace_back(resume_range, static_cast<int>(static_cast<long long>(nsys) * k / nthr),
+                          static_cast<int>(static_cast<long long>(nsys) * (k + 1) / nthr));
+      for (auto &th : pool) th.join();
     }
   }
   // the final structures on the device, every system switched on again
