@@ -18,6 +18,7 @@
 // only; a one-system batch has the lone run's rebuild points and ends bit
 // for bit where xmin() over mme() ends.  Runs are deterministic.
 #include <algorithm>
+#include <cfloat>
 #include <thread>
 #include <vector>
 
@@ -63,7 +64,7 @@ int Batch::xmin(const XMIN_OPT_T &xo_in, std::vector<int> &status, std::vector<i
   for (int s = 0; s < nsys; s++) {
     const size_t o = 3 * static_cast<size_t>(sys_[s].atom_off);
     energy[s] = ene[13 * s];
-    settle(s, jobs[s].start(xo, sys_[s].natom, x.data() + o, g.data() + o, ene[13 * s], &request[s]));
+    settle(s, jobs[s].start(xo, sys_[s].natom, x.data() + o, g.data() + o, ene[13 * s], &request[s], FLT_EPSILON));
   }
   for (;;) {
     bool any = false, rebuild = false;

@@ -77,7 +77,10 @@ class XminJob {
  public:
   XminJob();
   ~XminJob();
-  int start(const XMIN_OPT_T &xo, int natm, double *xyz, const double *grad, double energy, int *request);
+  // grad_eps: the gradients' relative precision, which sizes TNCG's
+  // finite-difference step (the reference assumes FP64)
+  int start(const XMIN_OPT_T &xo, int natm, double *xyz, const double *grad, double energy, int *request,
+            double grad_eps = 2.2204460492503131e-16);
   int resume(double energy, const double *grad, double *xyz, int *request);
   int iter() const { return iter_; }
   int ls_iter() const { return ls_iter_; }

@@ -32,6 +32,7 @@
 //  * mol_struct_opt=1 minimises only atoms whose incoming gradient is not
 //    exactly zero (frozen atoms, xminC.c:2590-2630).
 // One minimisation runs at a time per process, as in the reference.
+#include <cfloat>
 #include <cmath>
 #include <coroutine>
 #include <cstdio>
@@ -119,6 +120,10 @@ struct Params {
   int method = 3, numdiff = 1, m = 5, ls_method = 2, ls_maxiter = 20, maxiter = 1000;
   double grms_tol = 0.05, ls_maxatmov = 0.5, beta_armijo = 0.5, c_armijo = 0.4, mu_armijo = 1.0;
   double ftol_wolfe = 1e-4, gtol_wolfe = 0.9;
+  // relative precision of the gradients, which sizes the finite-difference
+  // step of the Hessian products: the FP64 machine epsilon as in the
+  // reference, or FP32's for this library's own GPU energy
+  double grad_eps = kEpsMach;
 };
 
 class Run {
@@ -218,7 +223,7 @@ class Run {
   // of Derreumaux, Zhang, Schlick and Brooks, J. Comput. Chem. 15, 532
   // (1994), p. 541.  x and g are restored; the energy is not.
   Gen hessvec(const std::vector<double> &v, std::vector<double> &hv) {
-    const double sqrt_eps = std::sqrt(kEpsMach);
+    const double sqrt_eps = std::sqrt(p_.grad_eps);
     std::vector<double> xsave(n_), gsave(n_), gorig;
     int st = 0;
     if (p_.numdiff == 2) gorig = g;
@@ -915,7 +920,8 @@ struct XminJob::Impl {
 XminJob::XminJob() : impl_(new Impl) {}
 XminJob::~XminJob() = default;
 
-int XminJob::start(const XMIN_OPT_T &xo, int natm, double *xyz, const double *grad, double energy, int *request) {
+int XminJob::start(const XMIN_OPT_T &xo, int natm, double *xyz, const double *grad, double energy, int *request,
+                   double grad_eps) {
   Active &a = impl_->a;
   a.gen.reset();
   a.run.reset();
@@ -958,6 +964,7 @@ int XminJob::start(const XMIN_OPT_T &xo, int natm, double *xyz, const double *gr
   p.mu_armijo = xo.mu_armijo;
   p.ftol_wolfe = xo.ftol_wolfe;
   p.gtol_wolfe = xo.gtol_wolfe;
+  p.grad_eps = grad_eps;
   const int ndim = a.mol ? 3 * static_cast<int>(a.atoms.size()) : natm;
   a.run = std::make_unique<Run>(p, ndim);
   if (a.mol) {
@@ -1005,6 +1012,8 @@ sffg::XminJob &active_job() {
   static sffg::XminJob j;
   return j;
 }
+// Gradient precision for the run xmin() is about to start through xminC.
+double g_next_grad_eps = kEpsMach;
 }  // namespace
 
 extern "C" {
@@ -1039,7 +1048,8 @@ double xminC(int *xyz_min, int *minim_method, int *maxiter, double *grms_tol, in
     xo.mu_armijo = *mu_armijo;
     xo.ftol_wolfe = *ftol_wolfe;
     xo.gtol_wolfe = *gtol_wolfe;
-    rc = job.start(xo, *natm_ext, xyz_ext, grad_ext, *enrg, &request);
+    rc = job.start(xo, *natm_ext, xyz_ext, grad_ext, *enrg, &request, g_next_grad_eps);
+    g_next_grad_eps = kEpsMach;
     if (rc == kParamsError) {  // before any run: outputs untouched
       *label = rc;
       return 0.0;
@@ -1101,6 +1111,11 @@ REAL_T xmin(REAL_T (*func)(REAL_T *, REAL_T *, INT_T *), INT_T *natm, REAL_T *xy
   int neg_two = -2, neg_four = -4;
   g_nfunc = 0;
   xo->error_flag = 0;
+  // this library's GPU energy has FP32-accurate gradients: TNCG's
+  // finite-difference Hessian products take a step sized for them (the
+  // reference's formula with FP32's epsilon); any other func keeps the
+  // reference's FP64 step and iterates
+  if (func == &mme || func == &mme_rattle) g_next_grad_eps = FLT_EPSILON;
   for (;;) {
     xminC(&xo->mol_struct_opt, &xo->method, &xo->maxiter, &xo->grms_tol, natm, &xo->m_lbfgs, &xo->numdiff, xyz,
           energy, grad, grms, &xo->iter, &xo->xmin_time, &xo->print_level, &xo->ls_method, &xo->ls_maxiter,

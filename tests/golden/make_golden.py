@@ -71,7 +71,8 @@ REF_CASES = [
     ("gb8trx", "nab/prmtop.gb2", "nab/trxox.2.4ns.pdb",
      "ntpr=1, gb=8, rgbmax=15.0, cut=99.0, diel=C, e_debug=0", "gb8trx.out.check"),
 ]
-EXTRA_INPUTS = ["nab/asp.top", "nab/asp.pdb", "xfin.parm7", "xfin.rst7", "xfin.md1.rst7"]
+EXTRA_INPUTS = ["nab/asp.top", "nab/asp.pdb", "xfin.parm7", "xfin.rst7", "xfin.md1.rst7", "nab/NMA.pdb",
+                "nab/NMA_scee+scnb.prmtop"]
 
 BREAKDOWN = ["bond", "angle", "dihedral", "enb14", "eel14", "enb", "eel", "egb", "econs", "esurf", "Total",
              "frms"]
@@ -262,6 +263,35 @@ def main():
                      "nsteps": 500, "ff": parse_ff(text),
                      "md": [[float(t) for t in line.split()[1:]] for line in text.splitlines()
                             if line.startswith("md:")]}
+    # NAB tests on the GB path with shipped outputs: variable 1-4 scaling
+    # (per-dihedral SCEE/SCNB factors), TNCG through mme on gbrna, md with
+    # RATTLE from tempi velocities (Berendsen with tautp 99999), and md with
+    # RATTLE writing a NetCDF trajectory every 10 steps
+    nab = os.path.join(test, "nab")
+    text = open(os.path.join(nab, "variable_14scale.out.check")).read()
+    opts = "ntpr=1, gb=1, cut=99.0, diel=C, e_debug=0"
+    out = run([SFFREF, os.path.join(HERE, "ref", "NMA_scee+scnb.prmtop"), os.path.join(HERE, "ref", "NMA.pdb"), "sp",
+               opts, tmp])
+    checks["variable_14"] = {"prmtop": "NMA_scee+scnb.prmtop", "coords": "NMA.pdb", "options": opts,
+                             "ff": parse_ff(text), "sp": parse_breakdown(out)}
+    text = open(os.path.join(nab, "txmin.out.check")).read()
+    checks["nab_txmin"] = {"prmtop": "gbrna.prmtop", "coords": "gbrna.pdb",
+                           "options": "ntpr=1, gb=1, kappa=0.10395, rgbmax=99., cut=99.0, diel=C",
+                           "maxiter": 5, "grms_tol": 0.001, "ls_maxatmov": 0.15, "ff": parse_ff(text),
+                           "min_lines": [[int(m.group(1)), int(m.group(2)), float(m.group(3)), float(m.group(4))]
+                                         for m in re.finditer(r" MIN: Iter =\s*(\d+)\s+NFunc =\s*(\d+)\s+E =\s*(\S+)"
+                                                              r"\s+RMSG =\s*(\S+)", text)],
+                           "end": [float(t) for t in re.search(r"END:.*E =\s*(\S+)\s+RMSG =\s*(\S+)", text).groups()]}
+    for name, check, opts, nsteps in (
+            ("nab_rattle_md", "rattle_md.out.check",
+             "ntpr=5, gb=1, kappa=0.10395, rgbmax=99., cut=99.0, diel=C, tempi=300., tautp=99999.,rattle=1", 20),
+            ("nab_gbnetcdf", "gbnetcdf.out.check",
+             "ntpr=10, ntwx=10, ntpr_md=50, gb=1, kappa=0.10395, cut=99.0, diel=C, tempi=300., rattle=1", 100)):
+        text = open(os.path.join(nab, check)).read()
+        checks[name] = {"prmtop": "gbrna.prmtop", "coords": "gbrna.pdb", "options": opts, "nsteps": nsteps,
+                        "ff": parse_ff(text),
+                        "md": [[float(t) for t in line.split()[1:]] for line in text.splitlines()
+                               if line.startswith("md:")]}
     # XMIN on xfin as the reference's test/txmin.c runs it (L-BFGS through
     # mme_rattle, 50 iterations), the same through mme, and TNCG
     opts = "ntpr=1, gb=1, kappa=0.10395, rgbmax=99., cut=99.0, diel=C"

@@ -338,3 +338,86 @@ def test_md_trajectory_device_path(lib, tmp_path):
             shift = coords[-1] - xx.reshape(n, 3)
             assert np.abs(shift - shift.mean(0)).max() < 1e-4
             assert np.abs(shift.mean(0)).max() > 1e-6
+
+
+def run_legacy_md(c, tmp_path, ncname=None):
+    """md() through the legacy API on the case's structure with the
+    reference's noise stream from its default seed; returns the printed ff:
+    and md: rows."""
+    import os
+    from nabc_gb300 import sff
+    prm, x = load_case(c)
+    n = prm.contents.Natom
+    L = sff.lib()
+    L.sffg_options_reset()
+    L.mm_options(c["options"].encode())
+    frozen = np.zeros(n, np.int32)
+    cons = np.zeros(n, np.int32)
+    L.mme_init_sff(prm, sff.iptr(frozen), sff.iptr(cons), None, ncname.encode() if ncname else None)
+    seed = C.c_int(-1)
+    L.setseed(C.byref(seed))
+    out = str(tmp_path / "md.out")
+    sff.set_output(out)
+    try:
+        v = np.zeros(3 * n)
+        f = np.zeros(3 * n)
+        L.md(3 * n, c["nsteps"], sff.dptr(x), sff.dptr(f), sff.dptr(v), C.cast(L.mme, C.c_void_p))
+        sff.flush_output()
+    finally:
+        sff.set_output(os.devnull)
+    text = open(out).read()
+    ff = [[float(t) for t in line.split()[1:]] for line in text.splitlines() if line.startswith("ff:")]
+    md = [[float(t) for t in line.split()[1:]] for line in text.splitlines() if line.startswith("md:")]
+    return ff, md
+
+
+@pytest.mark.parametrize("name", ["nab_rattle_md", "nab_gbnetcdf"])
+def test_nab_md_check_files(lib, checks, tmp_path, name):
+    """The reference's test/nab/rattle_md.nab (gbrna, gb=1 with kappa,
+    velocities drawn at tempi 300 K, rattle=1, 20 steps) and gbnetcdf.nab
+    (the same for 100 steps with rgbmax 25 and a NetCDF frame every 10
+    steps) against their shipped .out.check: every ff: and md: line to the
+    printed digits; the trajectory holds the 10 frames."""
+    from scipy.io import netcdf_file
+    c = checks[name]
+    nc = str(tmp_path / "gbtrj.nc") if name == "nab_gbnetcdf" else None
+    ff, md = run_legacy_md(c, tmp_path, nc)
+    assert len(ff) == len(c["ff"]) and len(md) == len(c["md"])
+    for got, want in zip(ff, c["ff"]):
+        assert got[:7] == pytest.approx(want[:7], abs=0.011)
+        assert got[7] == pytest.approx(want[7], rel=0.01)
+    for got, want in zip(md, c["md"]):
+        assert got == pytest.approx(want, abs=0.011)
+    if nc:
+        f = netcdf_file(nc, "r", mmap=False)
+        assert f.variables["coordinates"].shape[0] == 10
+        np.testing.assert_allclose(f.variables["time"][:], 0.01 * np.arange(1, 11), rtol=1e-6)
+        f.close()
+
+
+def test_variable_14_scaling(lib, checks):
+    """The reference's test/nab/variable_14scale.nab: N-methylacetamide
+    whose prmtop carries per-dihedral SCEE/SCNB 1-4 scale factors, gb=1:
+    every energy component of the compiled reference within 1e-6 of the
+    total's magnitude, and the shipped ff: line."""
+    from nabc_gb300 import sff
+    from nabc_gb300.batch import Batch
+    c = checks["variable_14"]
+    prm, x = load_case(c)
+    bt = Batch(c["options"])
+    bt.add(prm, x)
+    bt.finalize()
+    bt.eval()
+    b = bt.energy(0)
+    bt.close()
+    session = sff.Session(prm, c["options"])
+    g = np.zeros(3 * prm.contents.Natom)
+    it = C.c_int(-2)
+    e = sff.lib().mme(sff.dptr(x), sff.dptr(g), C.byref(it))
+    del session
+    tot = abs(c["sp"]["Total"])
+    for k, idx in (("bond", 3), ("angle", 4), ("dihedral", 5), ("enb14", 7), ("eel14", 8), ("enb", 1), ("eel", 2),
+                   ("egb", 10)):
+        assert b[idx] == pytest.approx(c["sp"][k], abs=1e-6 * tot), k
+    assert e == pytest.approx(c["sp"]["Total"], abs=1e-6 * tot)
+    assert round(e, 2) == c["ff"][0][1]

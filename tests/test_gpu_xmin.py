@@ -16,7 +16,7 @@ from conftest import load_case
 pytestmark = pytest.mark.gpu
 
 
-def run_case(c, print_level=0):
+def run_case(c, print_level=0, trace_calls=True):
     from nabc_gb300 import sff
     L = sff.lib()
     prm, x = load_case(c)
@@ -43,8 +43,10 @@ def run_case(c, print_level=0):
     e = np.array([e0])
     grms = np.zeros(1)
     nn = C.c_int(n)
-    ret = L.xmin(C.cast(rec, C.c_void_p), C.byref(nn), sff.dptr(x), sff.dptr(g), sff.dptr(e), sff.dptr(grms),
-                 C.byref(xo))
+    # handing xmin() the library's own function (not a recording wrapper)
+    # lets TNCG size its finite-difference step for the FP32 gradient
+    fn = C.cast(rec, C.c_void_p) if trace_calls else C.cast(func, C.c_void_p)
+    ret = L.xmin(fn, C.byref(nn), sff.dptr(x), sff.dptr(g), sff.dptr(e), sff.dptr(grms), C.byref(xo))
     del session
     return ret, x, g, grms[0], xo, np.array(trace), e0
 
@@ -83,16 +85,59 @@ def test_xmin_lbfgs_mme(lib, checks, refrun):
 
 def test_xmin_tncg_mme(lib, checks, refrun):
     """TNCG (the default method) through mme, 10 outer iterations.  Its
-    Hessian products are forward differences of gradients at displacements
-    of about 1e-6 A, where FP32 rounding of the GPU gradient is a sizeable
-    part of the difference (a few per cent of it here), and the truncated
-    CG takes another path; the reference's own TNCG moves by 1e-6 relative
-    between runs from OpenMP summation order alone.  So the outcome is
-    compared: no error, every outer iteration downhill, and the final
-    energy within 5e-3 relative of the reference's (measured 1.3e-3)."""
+    Hessian products are forward differences of gradients; handed this
+    library's mme, xmin() sizes the step for FP32-accurate gradients (the
+    reference's formula with FP32's epsilon), since at the reference's FP64
+    step (displacements of ~1e-6 A) FP32 rounding is a sizeable part of the
+    difference.  TNCG is still the most rounding-sensitive method (the
+    reference's own run moves by 1e-6 relative between runs from OpenMP
+    summation order), so the outcome is compared: no error, downhill, and the
+    final energy within 3e-3 relative of the reference's (measured 1.5e-3
+    here; the same test file's nab txmin case lands within 3.6e-4)."""
     c = checks["xfin_tncg"]
-    ret, x, g, grms, xo, trace, e0 = run_case(c)
-    print("tncg", ret, c["returns"], "iter", xo.iter, "calls", len(trace), len(refrun["xfin_tncg_trace"]))
+    ret, x, g, grms, xo, trace, e0 = run_case(c, trace_calls=False)
+    print("tncg", ret, c["returns"], "iter", xo.iter)
     assert xo.error_flag == 0 and xo.iter == c["iter"]
     assert ret < e0 - 250.0
-    assert abs(ret - c["returns"]) <= 5e-3 * abs(c["returns"])
+    assert abs(ret - c["returns"]) <= 3e-3 * abs(c["returns"])
+
+
+def test_nab_txmin_gpu(lib, checks, tmp_path):
+    """The reference's test/nab/txmin.nab (gbrna, the default TNCG, 5
+    iterations) through the GPU mme: the same iteration count, and each MIN
+    energy within 1e-3 relative of txmin.out.check (measured: 3.6e-4 at
+    most; TNCG's Hessian products are differences of FP32-rounded
+    gradients, while the FP64 oracle reproduces the file digit for digit,
+    tests/test_xmin.py)."""
+    import os
+    import re
+    from nabc_gb300 import sff
+    c = checks["nab_txmin"]
+    prm, x = load_case(c)
+    L = sff.lib()
+    session = sff.Session(prm, c["options"])
+    n = prm.contents.Natom
+    g = np.zeros(3 * n)
+    it = C.c_int(0)
+    e = np.array([L.mme(sff.dptr(x), sff.dptr(g), C.byref(it))])
+    xo = sff.XMIN_OPT_T()
+    L.xmin_opt_init(C.byref(xo))
+    xo.maxiter, xo.grms_tol, xo.ls_maxatmov, xo.print_level = c["maxiter"], c["grms_tol"], c["ls_maxatmov"], 1
+    out = str(tmp_path / "txmin.out")
+    sff.set_output(out)
+    try:
+        grms = np.zeros(1)
+        nn = C.c_int(n)
+        ret = L.xmin(C.cast(L.mme, C.c_void_p), C.byref(nn), sff.dptr(x), sff.dptr(g), sff.dptr(e), sff.dptr(grms),
+                     C.byref(xo))
+        sff.flush_output()
+    finally:
+        sff.set_output(os.devnull)
+    del session
+    rows = [[int(m.group(1)), float(m.group(3))]
+            for m in re.finditer(r" MIN: Iter =\s*(\d+)\s+NFunc =\s*(\d+)\s+E =\s*(\S+)", open(out).read())]
+    print("gpu txmin", rows, ret)
+    assert [r[0] for r in rows] == [w[0] for w in c["min_lines"]]
+    for got, want in zip(rows, c["min_lines"]):
+        assert got[1] == pytest.approx(want[2], rel=1e-3)
+    assert xo.error_flag == 0

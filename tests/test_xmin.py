@@ -192,3 +192,53 @@ def test_gradient_check_mode(lib, funcs, checks, refrun, capfd):
     for row in rows:  # analytic vs numerical derivative
         anal, num = float(row[-4]), float(row[-3])
         assert anal == pytest.approx(num, rel=1e-5, abs=1e-3)
+
+
+def test_nab_txmin_through_oracle(lib, oracle_mod, checks, tmp_path):
+    """The reference's own test/nab/txmin.nab (gbrna, gb=1 with kappa 0.10395,
+    the default TNCG, 5 iterations, print_level 1) run by this library's
+    XMIN over the FP64 oracle energy: every MIN line of the shipped
+    txmin.out.check (iteration, evaluations so far, energy to the printed 5
+    decimals, RMS gradient to the printed 8 digits) and the END line."""
+    import os
+    import re
+    from conftest import load_case
+    c = checks["nab_txmin"]
+    prm, x = load_case(c)
+    o = oracle_mod.Oracle(prm, c["options"])
+    n = prm.contents.Natom
+
+    @sff.FUNC_T
+    def energy(xp, gp, it):
+        e, ene, g, reff = o.mme(np.ctypeslib.as_array(xp, (3 * n,)).copy())
+        np.ctypeslib.as_array(gp, (3 * n,))[:] = g
+        return e
+
+    g = np.zeros(3 * n)
+    it = C.c_int(0)
+    e = np.array([energy(sff.dptr(x), sff.dptr(g), C.byref(it))])
+    xo = sff.XMIN_OPT_T()
+    lib.xmin_opt_init(C.byref(xo))
+    xo.maxiter, xo.grms_tol, xo.ls_maxatmov, xo.print_level = c["maxiter"], c["grms_tol"], c["ls_maxatmov"], 1
+    out = str(tmp_path / "txmin.out")
+    sff.set_output(out)
+    try:
+        grms = np.zeros(1)
+        nn = C.c_int(n)
+        lib.xmin(C.cast(energy, C.c_void_p), C.byref(nn), sff.dptr(x), sff.dptr(g), sff.dptr(e), sff.dptr(grms),
+                 C.byref(xo))
+        sff.flush_output()
+    finally:
+        sff.set_output(os.devnull)
+    text = open(out).read()
+    rows = [[int(m.group(1)), int(m.group(2)), float(m.group(3)), float(m.group(4))]
+            for m in re.finditer(r" MIN: Iter =\s*(\d+)\s+NFunc =\s*(\d+)\s+E =\s*(\S+)\s+RMSG =\s*(\S+)", text)]
+    assert "Starting TNCG minimisation" in text
+    assert len(rows) == len(c["min_lines"])
+    for got, want in zip(rows, c["min_lines"]):
+        assert got[:2] == want[:2]
+        assert got[2] == pytest.approx(want[2], abs=1.1e-5)
+        assert got[3] == pytest.approx(want[3], rel=1e-7)
+    end = re.search(r"END:\s+:-\)\s+E =\s*(\S+)\s+RMSG =\s*(\S+)", text)
+    assert float(end.group(1)) == pytest.approx(c["end"][0], abs=1.1e-5)
+    assert float(end.group(2)) == pytest.approx(c["end"][1], abs=1.1e-7)
