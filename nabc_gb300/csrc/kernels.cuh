@@ -273,8 +273,13 @@ __global__ void __launch_bounds__(256, 3) k_born(const DevTables t) {
     const int sj = chunk_entry(t.lb, k, lane, mycol);
     sm_hi[w][lane] = t.pos_hi[sj];
     sm_lo[w][lane] = t.pos_lo[sj];
-    sm_gb[w][lane] = t.gbpar[sj];
-    sm_col[w][lane] = mycol;
+    {
+      // far chunks never read the radius rho in gbpar.x: it carries the
+      // entry's column mask, one shared read per step fewer
+      float4 gq = t.gbpar[sj];
+      gq.x = __uint_as_float(mycol);
+      sm_gb[w][lane] = gq;
+    }
     if (NECK) sm_par[w][lane] = t.param[sj];
     const unsigned cols = __ballot_sync(kFull, mycol != 0u);
     __syncwarp();
@@ -292,7 +297,7 @@ __global__ void __launch_bounds__(256, 3) k_born(const DevTables t) {
         const float dy = (yi - h.y) + (yli - l.y);
         const float dz = (zi - h.z) + (zli - l.z);
         const float r2 = fmaf(dx, dx, fmaf(dy, dy, dz * dz));
-        const bool in = ((sm_col[w][j] >> lane) & 1u) && r2 <= t.born.cutoff2;
+        const bool in = ((__float_as_uint(gp.x) >> lane) & 1u) && r2 <= t.born.cutoff2;
         if (!__any_sync(kFull, in)) continue;  // every lane out of range
         const float dij1i = rsqrt_nr(r2);
         const float dij = r2 * dij1i;
@@ -583,8 +588,9 @@ __global__ void __launch_bounds__(256, 3) k_chain(const DevTables t) {
       l.w = t.sumda32[sj];
       sm_hi[w][lane] = t.pos_hi[sj];
       sm_lo[w][lane] = l;
-      sm_gb[w][lane] = t.gbpar[sj];
-      sm_col[w][lane] = mycol;
+      float4 gq = t.gbpar[sj];
+      gq.x = __uint_as_float(mycol);  // the column mask, as in pass 1
+      sm_gb[w][lane] = gq;
       if (NECK) sm_par[w][lane] = t.param[sj];
     }
     const unsigned cols = __ballot_sync(kFull, mycol != 0u);
@@ -603,7 +609,7 @@ __global__ void __launch_bounds__(256, 3) k_chain(const DevTables t) {
         const float dy = (yi - h.y) + (yli - l.y);
         const float dz = (zi - h.z) + (zli - l.z);
         const float r2 = fmaf(dx, dx, fmaf(dy, dy, dz * dz));
-        const bool in = ((sm_col[w][j] >> lane) & 1u) && r2 <= t.born.cutoff2;
+        const bool in = ((__float_as_uint(gp.x) >> lane) & 1u) && r2 <= t.born.cutoff2;
         if (!__any_sync(kFull, in)) continue;
         const float dij1i = rsqrt_nr(r2);
         const float dij = r2 * dij1i;
