@@ -923,12 +923,12 @@ void Batch::rebuild_list_b(void *stream) {
   const int tile_blocks = (ntile_ * 32 + 255) / 256;
   const int cand_blocks = 16 * d.nsm;  // grid-stride over the candidates (fixed, for graph capture)
   const ListArgs a = list_args(fsmax_all());
-  k_list_columns<true><<<cand_blocks, 256, 0, st>>>(a);
-  k_list_offsets<true><<<tile_blocks, 256, 0, st>>>(a);
-  k_list_scan<true><<<1, 1024, 0, st>>>(a);
-  k_list_fill<true><<<cand_blocks, 256, 0, st>>>(a);
-  k_list_pad<true><<<tile_blocks, 256, 0, st>>>(a);
-  k_list_done<<<(a.ntile + 255) / 256, 256, 0, st>>>(a.flagB, a.tile_flagB, a.ntile);
+  launch_pdl(k_list_columns<true>, cand_blocks, 256, st, a);
+  launch_pdl(k_list_offsets<true>, tile_blocks, 256, st, a);
+  launch_pdl(k_list_scan<true>, 1, 1024, st, a);
+  launch_pdl(k_list_fill<true>, cand_blocks, 256, st, a);
+  launch_pdl(k_list_pad<true>, tile_blocks, 256, st, a);
+  launch_pdl(k_list_done, (a.ntile + 255) / 256, 256, st, a.flagB, a.tile_flagB, a.ntile);
   launches_ += 6;
 }
 
@@ -1069,12 +1069,11 @@ int Batch::run_eval_direct(bool rebuild, void *stream) {
   DeviceState &d = *d_;
   cudaStream_t st = pick(d, stream);
   const int nsys = num_systems();
-  SFFG_CK(cudaMemsetAsync(d.counters.p + 5, 0, 5 * sizeof(int), st));
-  SFFG_CK(cudaMemsetAsync(d.energy.p, 0, d.energy.bytes(), st));
-  k_pack<<<(nslot_ + 255) / 256, 256, 0, st>>>(d.x.p, d.slot_atom.p, d.q32.p, d.tile_valid.p, nslot_, d.pos_hi.p,
-                                               d.pos_lo.p, d.box_lo.p, d.box_hi.p, d.acc_sumi.p, d.acc_fx.p,
-                                               d.acc_fy.p, d.acc_fz.p, d.nonfinite.p, d.tile_sys.p, d.xb.p,
-                                               kListMove * kListMove, d.counters.p + 4, d.tile_flagB.p);
+  // k_pack also clears the pass queues' counters and the energy slots
+  SFFG_CK(launch_pdl(k_pack, (nslot_ + 255) / 256, 256, st, d.x.p, d.slot_atom.p, d.q32.p, d.tile_valid.p, nslot_,
+                     d.pos_hi.p, d.pos_lo.p, d.box_lo.p, d.box_hi.p, d.acc_sumi.p, d.acc_fx.p, d.acc_fy.p,
+                     d.acc_fz.p, d.nonfinite.p, d.tile_sys.p, d.xb.p, kListMove * kListMove, d.counters.p + 4,
+                     d.tile_flagB.p, d.counters.p + 5, d.energy.p, static_cast<int>(d.energy.n)));
   SFFG_CK(cudaGetLastError());
   // bonded and 1-4 terms (FP64) on the side stream: they need only x and the
   // zeroed accumulators, and keep the FP64 units busy while the list upkeep
@@ -1151,7 +1150,7 @@ int Batch::run_eval_direct(bool rebuild, void *stream) {
     f.gboffset = mp_.gboffset;
     f.kappa = mp_.kappa;
     f.epsext = mp_.epsext;
-    k_born_finish<<<(nslot_ + 255) / 256, 256, 0, st>>>(f);
+    launch_pdl(k_born_finish, (nslot_ + 255) / 256, 256, st, f);
     SFFG_CK(cudaGetLastError());
   }
   // pass 2
@@ -1166,7 +1165,7 @@ int Batch::run_eval_direct(bool rebuild, void *stream) {
     SFFG_CK(cudaGetLastError());
   }
   if (profile_) SFFG_CK(cudaEventRecord(d.events[ring][1][1], st));
-  k_chain_prep<<<(nslot_ + 255) / 256, 256, 0, st>>>(d.acc_sd.p, d.chainfac.p, d.param.p, d.slot_atom.p,
+  launch_pdl(k_chain_prep, (nslot_ + 255) / 256, 256, st, d.acc_sd.p, d.chainfac.p, d.param.p, d.slot_atom.p,
                                                      d.sumda32.p, nslot_);
   // pass 3
   if (profile_) SFFG_CK(cudaEventRecord(d.events[ring][2][0], st));
@@ -1184,7 +1183,7 @@ int Batch::run_eval_direct(bool rebuild, void *stream) {
   }
   SFFG_CK(cudaStreamWaitEvent(st, d.join_ev, 0));
   // natom_total_ >= nsys: the gather's threads also cover the totals
-  k_gather_grad<<<(natom_total_ + 255) / 256, 256, 0, st>>>(d.acc_fx.p, d.acc_fy.p, d.acc_fz.p, d.atom_slot.p,
+  launch_pdl(k_gather_grad, (natom_total_ + 255) / 256, 256, st, d.acc_fx.p, d.acc_fy.p, d.acc_fz.p, d.atom_slot.p,
                                                             d.atom_frozen.p, d.atom_sys.p, d.sys_active.p,
                                                             d.grad.p, natom_total_, d.energy.p, d.etot.p, nsys);
   SFFG_CK(cudaGetLastError());
@@ -1267,6 +1266,7 @@ int Batch::kernel_times(double ms[3], long long *nevals) {
 // (apply) and the Philox step counter.
 __global__ void k_md_tscal(const long long *ekin, double *tscal, double *ekin_out, int nsys, double ekin0_per_dof,
                            const double *rndf, double dttp, double c_ave_factor, int apply, unsigned *step) {
+  pdl_wait();
   const int s = blockIdx.x * blockDim.x + threadIdx.x;
   if (s == 0) ++*step;
   if (s >= nsys) return;
@@ -1384,18 +1384,18 @@ int Batch::md_steps(int step0, int k, NoiseFn noise, void *noise_ctx, void *stre
   SFFG_CK(cudaMemcpyAsync(d.step.p, &step_host_, sizeof(unsigned), cudaMemcpyHostToDevice, st));
   // one step after the drift: evaluation, kick, kinetic energy, counter
   auto step_body = [&](cudaStream_t s, bool rebuild, bool capturing) -> int {
-    k_md_drift<<<nb, 256, 0, s>>>(a);
+    SFFG_CK(cudaMemsetAsync(d.ekin.p, 0, d.ekin.bytes(), s));
+    launch_pdl(k_md_drift, nb, 256, s, a);
     int r = capturing ? run_eval_direct(false, s) : run_eval(rebuild, s);
     if (r) return r;
     if (noise && a.gammai != 0.0) {
       if ((r = upload_noise(*this, d, noise, noise_ctx, s, h))) return r;
       a.noise = d.noise.p;
     }
-    SFFG_CK(cudaMemsetAsync(d.ekin.p, 0, d.ekin.bytes(), s));
-    k_md_kick<<<nb, 256, 0, s>>>(a, 0);
-    k_md_tscal<<<(nsys + 127) / 128, 128, 0, s>>>(d.ekin.p, d.tscal.p, nullptr, nsys, boltz2 * opts_.temp0,
-                                                  d.rndf.p, opts_.dt / opts_.tautp, c_ave, a.gammai == 0.0,
-                                                  d.step.p);
+    launch_pdl(k_md_kick, nb, 256, s, a, 0);
+    launch_pdl(k_md_tscal, (nsys + 127) / 128, 128, s, d.ekin.p, d.tscal.p, static_cast<double *>(nullptr), nsys,
+               boltz2 * opts_.temp0, static_cast<const double *>(d.rndf.p), opts_.dt / opts_.tautp, c_ave,
+               a.gammai == 0.0, d.step.p);
     launches_ += 3;  // drift, kick, tscal
     SFFG_CK(cudaGetLastError());
     return SFFG_OK;
@@ -1487,6 +1487,7 @@ struct CgArgs {
 // L10) or to its end (L100).  Every thread follows the same scalar control
 // flow; vector loops and dot products are spread over the block.
 __global__ void __launch_bounds__(kCgThreads) k_cg_post(CgArgs a) {
+  pdl_wait();
   const int s = blockIdx.x;
   if (!a.sys_active[s]) return;
   __shared__ double red[kCgThreads / 32];

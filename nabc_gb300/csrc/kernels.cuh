@@ -123,6 +123,13 @@ __device__ __forceinline__ long long warp_sum_ll(long long v) {
   return v;
 }
 
+// Programmatic dependent launch: a kernel launched with the programmatic
+// stream-serialization attribute (launch_pdl) may be scheduled while the
+// kernel before it on the stream drains; it waits here, before reading
+// anything that kernel wrote, until that grid has completed and its writes
+// are visible.  A kernel launched without the attribute passes at once.
+__device__ __forceinline__ void pdl_wait() { asm volatile("griddepcontrol.wait;" ::: "memory"); }
+
 __device__ __forceinline__ void atomic_add_ll(long long *p, long long v) {
   if (v != 0) atomicAdd(reinterpret_cast<unsigned long long *>(p), static_cast<unsigned long long>(v));
 }
@@ -252,13 +259,14 @@ __global__ void __launch_bounds__(256, 3) k_born(const DevTables t) {
   __shared__ unsigned sm_col[8][32];
   __shared__ int sm_par[8][32], si_par[8][32], s_pre[8][32];
   __shared__ float s_npos[NECK ? 441 : 1], s_nval[NECK ? 441 : 1];
-  if (NECK) {
+  if (NECK) {  // static tables: staged before the wait
     for (int i = threadIdx.x; i < 441; i += blockDim.x) {
       s_npos[i] = t.neck_pos[i];
       s_nval[i] = t.neck_val[i];
     }
     __syncthreads();
   }
+  pdl_wait();
   const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
   const int nB = *t.lb.nchunk, nC = *t.lc.nchunk, nitem = nB + nC;
   const float FB = 1099511627776.0f;
@@ -417,10 +425,11 @@ __global__ void __launch_bounds__(256, 3) k_gbpair(const DevTables t) {
   __shared__ float4 sm_hi[8][32], sm_lo[8][32];
   __shared__ uint4 sm_aux[8][32];
   __shared__ float2 s_lj[LJS ? kLjShared : 1];
-  if (LJS) {
+  if (LJS) {  // a static table: staged before the wait
     for (int i = threadIdx.x; i < t.lj_n; i += blockDim.x) s_lj[i] = t.lj[i];
     __syncthreads();
   }
+  pdl_wait();
   const float2 *const lj_all = LJS ? s_lj : t.lj;
   const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
   const int nchunk = *t.la.nchunk;
@@ -554,13 +563,14 @@ __global__ void __launch_bounds__(256, 3) k_chain(const DevTables t) {
   __shared__ unsigned sm_col[8][32];
   __shared__ int sm_par[8][32], si_par[8][32], s_pre[8][32];
   __shared__ float s_npos[NECK ? 441 : 1], s_nval[NECK ? 441 : 1];
-  if (NECK) {
+  if (NECK) {  // static tables: staged before the wait
     for (int i = threadIdx.x; i < 441; i += blockDim.x) {
       s_npos[i] = t.neck_pos[i];
       s_nval[i] = t.neck_val[i];
     }
     __syncthreads();
   }
+  pdl_wait();
   const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
   const int nB = *t.lb.nchunk, nC = *t.lc.nchunk, nitem = nB + nC;
   const float FS = 4294967296.0f;

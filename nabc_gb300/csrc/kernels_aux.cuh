@@ -19,7 +19,14 @@ __global__ void k_pack(const double *__restrict__ x, const int *__restrict__ slo
                        int nslot, float4 *pos_hi, float4 *pos_lo, float4 *box_lo, float4 *box_hi,
                        long long *acc_sumi, long long *acc_fx, long long *acc_fy, long long *acc_fz,
                        int *nonfinite_sys, const int *tile_sys, const float4 *xb, float xb_lim2,
-                       int *flagB, int *tile_flagB) {
+                       int *flagB, int *tile_flagB, int *queue_counters, long long *energy, int nenergy) {
+  pdl_wait();
+  {
+    // the evaluation's fresh sums: pass work-queue counters and energy slots
+    const int tid = blockIdx.x * blockDim.x + threadIdx.x, nthr = gridDim.x * blockDim.x;
+    if (tid < 5) queue_counters[tid] = 0;
+    for (int i = tid; i < nenergy; i += nthr) energy[i] = 0;
+  }
   const int slot = blockIdx.x * blockDim.x + threadIdx.x;
   const int lane = threadIdx.x & 31;
   if (slot - lane >= nslot) return;  // whole warp beyond the last tile
@@ -93,6 +100,7 @@ struct FinishArgs {
 };
 
 __global__ void k_born_finish(const FinishArgs a) {
+  pdl_wait();
   const int slot = blockIdx.x * blockDim.x + threadIdx.x;
   const int lane = threadIdx.x & 31;
   if (slot - lane >= a.nslot) return;
@@ -142,6 +150,7 @@ __global__ void k_born_finish(const FinishArgs a) {
 // Chain-rule weight of each atom for pass 3 (src/sff/eff.c:2211-2231).
 __global__ void k_chain_prep(const long long *acc_sd, const double *chainfac, const int *param,
                              const int *slot_atom, float *sumda32, int nslot) {
+  pdl_wait();
   const int slot = blockIdx.x * blockDim.x + threadIdx.x;
   if (slot >= nslot) return;
   double v = 0.0;
@@ -184,6 +193,7 @@ __device__ __forceinline__ void add_energy(const BondedArgs &a, int sys, int slo
 
 // Harmonic bonds: src/sff/eff.c:116-154.
 __global__ void k_bonds(const BondedArgs a, const int2 *atoms, const double2 *par, int n) {
+  pdl_wait();
   const int i = blockIdx.x * blockDim.x + threadIdx.x;
   int sys = -1;
   double e = 0.0;
@@ -208,6 +218,7 @@ __global__ void k_bonds(const BondedArgs a, const int2 *atoms, const double2 *pa
 
 // Harmonic angles: src/sff/eff.c:216-300.
 __global__ void k_angles(const BondedArgs a, const int4 *atoms, const double2 *par, int n) {
+  pdl_wait();
   const int i = blockIdx.x * blockDim.x + threadIdx.x;
   int sys = -1;
   double e = 0.0;
@@ -245,6 +256,7 @@ __global__ void k_angles(const BondedArgs a, const int4 *atoms, const double2 *p
 
 // Cosine dihedrals: src/sff/eff.c:373-618 (one expanded term per thread).
 __global__ void k_dihedrals(const BondedArgs a, const int4 *atoms, const double4_32a *par, int n) {
+  pdl_wait();
   const int i = blockIdx.x * blockDim.x + threadIdx.x;
   int sys = -1;
   double e = 0.0;
@@ -312,6 +324,7 @@ __global__ void k_dihedrals(const BondedArgs a, const int4 *atoms, const double4
 // src/sff/eff.c:1212-1310).  atoms = (i, j, 10-12 flag, 0);
 // par = (q_i q_j scee, c12, c6, scnb).
 __global__ void k_pairs14(const BondedArgs a, const int4 *atoms, const double4_32a *par, int n) {
+  pdl_wait();
   const int i = blockIdx.x * blockDim.x + threadIdx.x;
   int sys = -1;
   double eel = 0.0, evdw = 0.0;
@@ -349,6 +362,7 @@ __global__ void k_pairs14(const BondedArgs a, const int4 *atoms, const double4_3
 // Harmonic positional restraints (src/sff/eff.c:17-80, econs):
 // wcons |x - x0|^2 for every constrained atom; w[atom] = wcons or 0.
 __global__ void k_restraints(const BondedArgs a, const double *w, const double *x0, int natom) {
+  pdl_wait();
   const int i = blockIdx.x * blockDim.x + threadIdx.x;
   int sys = -1;
   double e = 0.0;
@@ -389,6 +403,7 @@ __device__ double block_sum(double v, double *sh) {
 __global__ void __launch_bounds__(kComThreads) k_com_remove(double *x, double *v, const double *minv,
                                                              const int *sys_atom_off, const int *sys_natom,
                                                              const int *sys_active, int also_v) {
+  pdl_wait();
   __shared__ double sh[kComThreads];
   const int s = blockIdx.x;
   if (!sys_active[s]) return;
@@ -487,6 +502,7 @@ __global__ void k_gather_grad(const long long *acc_fx, const long long *acc_fy, 
                               const int *atom_slot, const int *atom_frozen, const int *atom_sys,
                               const int *sys_active, double *grad, int natom, const long long *energy,
                               double *etot, int nsys) {
+  pdl_wait();
   const int a = blockIdx.x * blockDim.x + threadIdx.x;
   if (a < nsys) etot[a] = energy_total(energy, a);
   if (a >= natom || !sys_active[atom_sys[a]]) return;
@@ -541,6 +557,7 @@ struct MdArgs {
 
 // First half of a step (src/sff/sff.c:2243-2248): half-kick and drift.
 __global__ void k_md_drift(const MdArgs a) {
+  pdl_wait();
   const int i = blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= a.n3) return;
   const int sys = a.atom_sys[i / 3];
@@ -556,6 +573,7 @@ __global__ void k_md_drift(const MdArgs a) {
 // kinetic energy (2294-2306).  init = 1 only sets the accelerations of the
 // first force evaluation (2197-2215).
 __global__ void k_md_kick(const MdArgs a, int init) {
+  pdl_wait();
   const int i = blockIdx.x * blockDim.x + threadIdx.x;
   int sys = -1;
   double ek = 0.0;

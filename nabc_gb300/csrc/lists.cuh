@@ -97,6 +97,7 @@ struct ListArgs {
 
 // ---- stage 1 -------------------------------------------------------------
 __global__ void k_list_candidates(const ListArgs a) {
+  pdl_wait();
   const int lane = threadIdx.x & 31;
   const int I = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
   if (I >= a.ntile) return;
@@ -156,6 +157,7 @@ __global__ void k_list_candidates(const ListArgs a) {
 // columns.
 template <bool GB_ONLY>
 __global__ void k_list_columns(const ListArgs a) {
+  pdl_wait();
   __shared__ float4 s_hi[8][32], s_lo[8][32];
   __shared__ float s_s[8][32];
   __shared__ int s_atom[8][32];
@@ -268,6 +270,7 @@ __global__ void k_list_columns(const ListArgs a) {
 // ---- stage 3 -------------------------------------------------------------
 template <bool GB_ONLY>
 __global__ void k_list_offsets(const ListArgs a) {
+  pdl_wait();
   if (GB_ONLY && !*a.flagB) return;
   const int lane = threadIdx.x & 31;
   const int I = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
@@ -308,6 +311,7 @@ __global__ void k_list_offsets(const ListArgs a) {
 // Exclusive scan of chunks per i-tile, one block of 1024 threads.
 template <bool GB_ONLY>
 __global__ void __launch_bounds__(1024) k_list_scan(const ListArgs a) {
+  pdl_wait();
   __shared__ int s_a[1024], s_b[1024], s_c[1024];
   if (GB_ONLY && !*a.flagB) return;
   const int t = threadIdx.x, n = a.ntile;
@@ -351,6 +355,7 @@ __global__ void __launch_bounds__(1024) k_list_scan(const ListArgs a) {
 // ---- stage 5 -------------------------------------------------------------
 template <bool GB_ONLY>
 __global__ void k_list_fill(const ListArgs a) {
+  pdl_wait();
   if (GB_ONLY && !*a.flagB) return;
   const int lane = threadIdx.x & 31;
   const int ncand = *a.ncand, nwarps = (gridDim.x * blockDim.x) >> 5;
@@ -396,6 +401,7 @@ __global__ void k_list_fill(const ListArgs a) {
 // empty column, so the passes load harmless data for it.
 template <bool GB_ONLY>
 __global__ void k_list_pad(const ListArgs a) {
+  pdl_wait();
   if (GB_ONLY && !*a.flagB) return;
   const int lane = threadIdx.x & 31;
   const int I = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
@@ -429,6 +435,7 @@ __global__ void k_list_pad(const ListArgs a) {
 
 // Clears the list-B flag after a (re)build; launched last.
 __global__ void k_list_done(int *flagB, int *tile_flagB, int ntile) {
+  pdl_wait();
   const int s = blockIdx.x * blockDim.x + threadIdx.x;
   if (s == 0) *flagB = 0;
   if (s < ntile) tile_flagB[s] = 0;

@@ -4,8 +4,8 @@
 namespace sffg {
 
 void launch_born(bool neck, int grid, cudaStream_t st, const DevTables &t) {
-  if (neck) k_born<true><<<grid, 256, 0, st>>>(t);
-  else k_born<false><<<grid, 256, 0, st>>>(t);
+  if (neck) launch_pdl(k_born<true>, grid, 256, st, t);
+  else launch_pdl(k_born<false>, grid, 256, st, t);
 }
 
 int born_blocks_per_sm(bool neck) {

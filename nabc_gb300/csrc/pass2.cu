@@ -6,11 +6,11 @@ namespace sffg {
 void launch_gbpair(bool kappa, int grid, cudaStream_t st, const DevTables &t) {
   const bool ljs = t.lj_shared && t.lj_n <= kLjShared;
   if (kappa) {
-    if (ljs) k_gbpair<true, true><<<grid, 256, 0, st>>>(t);
-    else k_gbpair<true, false><<<grid, 256, 0, st>>>(t);
+    if (ljs) launch_pdl(k_gbpair<true, true>, grid, 256, st, t);
+    else launch_pdl(k_gbpair<true, false>, grid, 256, st, t);
   } else {
-    if (ljs) k_gbpair<false, true><<<grid, 256, 0, st>>>(t);
-    else k_gbpair<false, false><<<grid, 256, 0, st>>>(t);
+    if (ljs) launch_pdl(k_gbpair<false, true>, grid, 256, st, t);
+    else launch_pdl(k_gbpair<false, false>, grid, 256, st, t);
   }
 }
 

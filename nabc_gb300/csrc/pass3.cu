@@ -5,8 +5,8 @@
 namespace sffg {
 
 void launch_chain(bool neck, int grid, cudaStream_t st, const DevTables &t) {
-  if (neck) k_chain<true><<<grid, 256, 0, st>>>(t);
-  else k_chain<false><<<grid, 256, 0, st>>>(t);
+  if (neck) launch_pdl(k_chain<true>, grid, 256, st, t);
+  else launch_pdl(k_chain<false>, grid, 256, st, t);
 }
 
 int chain_blocks_per_sm(bool neck) {

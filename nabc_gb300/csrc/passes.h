@@ -4,9 +4,29 @@
 
 #include <cuda_runtime.h>
 
+#include <utility>
+
 #include "kernels.cuh"
 
 namespace sffg {
+
+// Launches kernel k with programmatic stream serialization: it may be
+// scheduled while the previous kernel on the stream drains, hiding the
+// launch gap; k must call pdl_wait() before reading that kernel's output.
+template <typename... P, typename... A>
+cudaError_t launch_pdl(void (*k)(P...), dim3 grid, dim3 block, cudaStream_t st, A &&...args) {
+  cudaLaunchConfig_t c = {};
+  c.gridDim = grid;
+  c.blockDim = block;
+  c.dynamicSmemBytes = 0;
+  c.stream = st;
+  cudaLaunchAttribute at[1];
+  at[0].id = cudaLaunchAttributeProgrammaticStreamSerialization;
+  at[0].val.programmaticStreamSerializationAllowed = 1;
+  c.attrs = at;
+  c.numAttrs = 1;
+  return cudaLaunchKernelEx(&c, k, std::forward<A>(args)...);
+}
 
 // grid: 256-thread blocks of the persistent kernel.
 void launch_born(bool neck, int grid, cudaStream_t st, const DevTables &t);
