@@ -97,7 +97,7 @@ struct DeviceState {
   DBuf<float> neck_pos, neck_val;
   // dynamics
   DBuf<double> tscal, noise, rndf;
-  DBuf<long long> ekin;
+  DBuf<long long> ekin, ekin_last;  // the step's kinetic sum, and the last finished step's
   // minimisation
   DBuf<double> cg_w;
   DBuf<CgState> cg_state;
@@ -140,7 +140,7 @@ struct DeviceState {
     rel(chunk0B); rel(chunk0C); rel(chunkA_i); rel(entA_slot); rel(chunkB_i); rel(entB_slot);
     rel(chunkC_i); rel(entC_slot); rel(entA_col); rel(entA_exc); rel(entB_col); rel(entC_col);
     rel(xb); rel(counters); rel(step); rel(cg_nactive); rel(sys_key); rel(tile_flagB); rel(cons_w); rel(cons_x0); rel(neck_pos); rel(neck_val); rel(tscal);
-    rel(noise); rel(rndf); rel(ekin); rel(cg_w); rel(cg_state);
+    rel(noise); rel(rndf); rel(ekin); rel(ekin_last); rel(cg_w); rel(cg_state);
   }
 };
 
@@ -524,6 +524,7 @@ int Batch::upload() {
   SFFG_CK(cudaMemset(d.counters.p, 0, d.counters.bytes()));
   SFFG_CK(d.tscal.alloc(nsys));
   SFFG_CK(d.ekin.alloc(nsys));
+  SFFG_CK(d.ekin_last.alloc(nsys));
   {
     // kinetic degrees of freedom per system: 3N minus frozen (sff.c:2142)
     std::vector<double> rndf(nsys);
@@ -1264,13 +1265,19 @@ int Batch::kernel_times(double ms[3], long long *nevals) {
 
 // End of an md step: kinetic energy, the Berendsen factor of the next step
 // (apply) and the Philox step counter.
-__global__ void k_md_tscal(const long long *ekin, double *tscal, double *ekin_out, int nsys, double ekin0_per_dof,
-                           const double *rndf, double dttp, double c_ave_factor, int apply, unsigned *step) {
+// The step's kinetic sum moves to ekin_last and ekin is cleared for the
+// next step's kick.
+__global__ void k_md_tscal(long long *ekin, long long *ekin_last, double *tscal, double *ekin_out, int nsys,
+                           double ekin0_per_dof, const double *rndf, double dttp, double c_ave_factor, int apply,
+                           unsigned *step) {
   pdl_wait();
   const int s = blockIdx.x * blockDim.x + threadIdx.x;
   if (s == 0) ++*step;
   if (s >= nsys) return;
-  double ek = 0.5 * static_cast<double>(ekin[s]) * (1.0 / 4294967296.0) * c_ave_factor;
+  const long long e = ekin[s];
+  ekin_last[s] = e;
+  ekin[s] = 0;
+  double ek = 0.5 * static_cast<double>(e) * (1.0 / 4294967296.0) * c_ave_factor;
   if (ekin_out) ekin_out[s] = ek;
   if (apply) {
     const double ekin0 = ekin0_per_dof * rndf[s];
@@ -1352,6 +1359,10 @@ int Batch::md_begin(bool rebuild, NoiseFn noise, void *noise_ctx, void *stream) 
   const int nb = (a.n3 + 255) / 256;
   k_md_kick<<<nb, 256, 0, st>>>(a, 1);
   SFFG_CK(cudaGetLastError());
+  // the kinetic sum of the first kick is not a step's: each step's kick
+  // starts from zero (k_md_tscal clears it afterwards)
+  SFFG_CK(cudaMemcpyAsync(d.ekin_last.p, d.ekin.p, d.ekin.bytes(), cudaMemcpyDeviceToDevice, st));
+  SFFG_CK(cudaMemsetAsync(d.ekin.p, 0, d.ekin.bytes(), st));
   launches_++;
   return SFFG_OK;
 }
@@ -1384,7 +1395,6 @@ int Batch::md_steps(int step0, int k, NoiseFn noise, void *noise_ctx, void *stre
   SFFG_CK(cudaMemcpyAsync(d.step.p, &step_host_, sizeof(unsigned), cudaMemcpyHostToDevice, st));
   // one step after the drift: evaluation, kick, kinetic energy, counter
   auto step_body = [&](cudaStream_t s, bool rebuild, bool capturing) -> int {
-    SFFG_CK(cudaMemsetAsync(d.ekin.p, 0, d.ekin.bytes(), s));
     launch_pdl(k_md_drift, nb, 256, s, a);
     int r = capturing ? run_eval_direct(false, s) : run_eval(rebuild, s);
     if (r) return r;
@@ -1393,7 +1403,8 @@ int Batch::md_steps(int step0, int k, NoiseFn noise, void *noise_ctx, void *stre
       a.noise = d.noise.p;
     }
     launch_pdl(k_md_kick, nb, 256, s, a, 0);
-    launch_pdl(k_md_tscal, (nsys + 127) / 128, 128, s, d.ekin.p, d.tscal.p, static_cast<double *>(nullptr), nsys,
+    launch_pdl(k_md_tscal, (nsys + 127) / 128, 128, s, d.ekin.p, d.ekin_last.p, d.tscal.p,
+               static_cast<double *>(nullptr), nsys,
                boltz2 * opts_.temp0, static_cast<const double *>(d.rndf.p), opts_.dt / opts_.tautp, c_ave,
                a.gammai == 0.0, d.step.p);
     launches_ += 3;  // drift, kick, tscal
@@ -1426,7 +1437,7 @@ int Batch::md_kinetic(std::vector<double> &ekin, void *stream) {
   cudaStream_t st = pick(d, stream);
   const int nsys = num_systems();
   std::vector<long long> e(nsys);
-  SFFG_CK(cudaMemcpyAsync(e.data(), d.ekin.p, nsys * sizeof(long long), cudaMemcpyDeviceToHost, st));
+  SFFG_CK(cudaMemcpyAsync(e.data(), d.ekin_last.p, nsys * sizeof(long long), cudaMemcpyDeviceToHost, st));
   SFFG_CK(cudaStreamSynchronize(st));
   const double dt5 = 0.5 * opts_.dt * 20.455, gammai = opts_.gamma_ln / 20.455;
   const double c_ave = gammai > 0.0 ? 1.0 + gammai * dt5 : 1.0;
