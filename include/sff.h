@@ -104,6 +104,12 @@ INT_T conjgrad(REAL_T *x, INT_T *n, REAL_T *f,
                REAL_T (*func)(REAL_T *, REAL_T *, INT_T *),
                REAL_T *rmsgrad, REAL_T *dfpred, INT_T *maxiter);
 
+/* Name the checkpoint files mme() writes every nchk iterations (option
+ * nchk, default 10000): the coordinates in the reference's Cartesian
+ * format, the name's leftmost "%d" replaced by the iteration number or the
+ * number appended (src/sff/sff.h:140, sff.c:789-830, 2056; eff.c:2536). */
+void mm_set_checkpoint(STRING_T **fname);
+
 /* Print the timing summary (src/sff/sff.h:149, src/sff/timer.c:71). */
 INT_T mme_timer(void);
 

@@ -85,6 +85,12 @@ int sffg_batch_get_energy(sffg_batch *b, int sys, double *ene, void *stream);
 int sffg_batch_get_grad(sffg_batch *b, int sys, double *g, void *stream);
 /* Effective Born radii of the last evaluation, in atom order. */
 int sffg_batch_get_reff(sffg_batch *b, int sys, double *reff, void *stream);
+/* Per-system status: status[s] is SFFG_OK, or SFFG_ENONFINITE once an
+ * evaluation met a non-finite coordinate of system s (its results are then
+ * meaningless; the other systems' results are unaffected).  Setting the
+ * system's coordinates again clears it.  Synchronises the stream. */
+int sffg_batch_status(sffg_batch *b, int *status, void *stream);
+
 /* Number of unordered pairs on the current pair lists of one system. */
 long long sffg_batch_num_pairs(sffg_batch *b, int sys);
 
@@ -117,10 +123,12 @@ int sffg_batch_cg(sffg_batch *b, int maxiter, double rmsgrad, double dfpred, int
  * regroups the other systems' lists (and, with a finite cutoff, may change
  * their pair sets), so a system of a mixed batch follows its lone run only
  * to FP32 rounding, while a one-system batch ends bit for bit where xmin()
- * over mme() ends.  Runs are deterministic.  status[s] receives the system's error_flag (0
- * or the reference's negative code), iters[s] its iteration count and
- * energy[s] its final energy (0 on an error); any may be NULL.  The
- * minimised coordinates stay in the batch (sffg_batch_get_coords). */
+ * over mme() ends.  Runs are deterministic.  status[s] receives the
+ * system's error_flag (0, the reference's negative code -1..-6, or -7 when
+ * the system's energy turned non-finite, which ends that system alone),
+ * iters[s] its iteration count and energy[s] its final energy (0 on an
+ * error); any may be NULL.  The minimised coordinates stay in the batch
+ * (sffg_batch_get_coords). */
 int sffg_batch_xmin(sffg_batch *b, const XMIN_OPT_T *xo, int *status, int *iters, double *energy, void *stream);
 
 /* Kernel launches issued by this batch since it was created. */

@@ -94,6 +94,13 @@ class Batch:
                "cg")
         return st, en
 
+    def status(self, stream=None):
+        """Per system: 0, or sffg's SFFG_ENONFINITE (-5) once an evaluation
+        met a non-finite coordinate of that system."""
+        st = np.zeros(len(self.natoms), np.int32)
+        _check(sff.lib().sffg_batch_status(self.h, sff.iptr(st), stream), "status")
+        return st
+
     def xmin(self, stream=None, **opts):
         """The reference's XMIN on every system (sffg_batch_xmin); opts set
         fields of XMIN_OPT_T over xmin_opt_init's defaults (method, maxiter,

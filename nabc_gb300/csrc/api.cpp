@@ -119,6 +119,15 @@ extern "C" int sffg_batch_cg(sffg_batch *b, int maxiter, double rmsgrad, double 
   return SFFG_OK;
 }
 
+extern "C" int sffg_batch_status(sffg_batch *b, int *status, void *stream) {
+  if (!b || !status) return fail(SFFG_EINVAL, "null batch or status");
+  std::vector<int> st;
+  const int rc = b->impl->system_status(st, stream);
+  if (rc) return pass(b->impl, rc);
+  for (size_t s = 0; s < st.size(); s++) status[s] = st[s];
+  return SFFG_OK;
+}
+
 extern "C" int sffg_batch_xmin(sffg_batch *b, const XMIN_OPT_T *xo, int *status, int *iters, double *energy,
                                void *stream) {
   if (!b || !xo) return fail(SFFG_EINVAL, "null batch or options");

@@ -19,12 +19,17 @@
 // for bit where xmin() over mme() ends.  Runs are deterministic.
 #include <algorithm>
 #include <cfloat>
+#include <cmath>
 #include <thread>
 #include <vector>
 
 #include "engine.h"
 
 namespace sffg {
+
+// Status of a system whose energy turned non-finite (the reference's own
+// codes run from -1 to -6).
+constexpr int kXminNonFinite = -7;
 
 int Batch::xmin(const XMIN_OPT_T &xo_in, std::vector<int> &status, std::vector<int> &iters,
                 std::vector<double> &energy, void *stream) {
@@ -61,9 +66,15 @@ int Batch::xmin(const XMIN_OPT_T &xo_in, std::vector<int> &status, std::vector<i
       iters[s] = jobs[s].iter();
     }
   };
+  std::vector<int> health;
+  if ((rc = system_status(health, stream))) return rc;
   for (int s = 0; s < nsys; s++) {
     const size_t o = 3 * static_cast<size_t>(sys_[s].atom_off);
     energy[s] = ene[13 * s];
+    if (health[s] != SFFG_OK || !std::isfinite(ene[13 * s])) {  // never starts
+      status[s] = kXminNonFinite;
+      continue;
+    }
     settle(s, jobs[s].start(xo, sys_[s].natom, x.data() + o, g.data() + o, ene[13 * s], &request[s], FLT_EPSILON));
   }
   for (;;) {
@@ -78,6 +89,7 @@ int Batch::xmin(const XMIN_OPT_T &xo_in, std::vector<int> &status, std::vector<i
     if ((rc = set_all_coords(x.data(), stream))) return rc;
     if ((rc = eval(rebuild, stream))) return rc;
     if ((rc = get_all_energy_grad(ene, g.data(), stream))) return rc;
+    if ((rc = system_status(health, stream))) return rc;
     // the minimisers are independent: resume them on the host's cores
     // (each system's arithmetic is the same on any thread)
     auto resume_range = [&](int s0, int s1) {
@@ -85,6 +97,12 @@ int Batch::xmin(const XMIN_OPT_T &xo_in, std::vector<int> &status, std::vector<i
         if (!state[s]) continue;
         const size_t o = 3 * static_cast<size_t>(sys_[s].atom_off);
         energy[s] = ene[13 * s];
+        if (health[s] != SFFG_OK || !std::isfinite(ene[13 * s])) {  // a non-finite system ends alone
+          state[s] = 0;
+          status[s] = kXminNonFinite;
+          iters[s] = jobs[s].iter();
+          continue;
+        }
         settle(s, jobs[s].resume(ene[13 * s], g.data() + o, x.data() + o, &request[s]));
       }
     };

@@ -582,8 +582,10 @@ static cudaStream_t pick(DeviceState &d, void *stream) {
 int Batch::set_coords(int s, const double *x, void *stream) {
   if (!finalized_ || s < 0 || s >= num_systems()) return SFFG_EINVAL;
   const SystemInfo &si = sys_[s];
+  cudaStream_t st = pick(*d_, stream);
   SFFG_CK(cudaMemcpyAsync(d_->x.p + 3 * static_cast<size_t>(si.atom_off), x, 3 * sizeof(double) * si.natom,
-                          cudaMemcpyHostToDevice, pick(*d_, stream)));
+                          cudaMemcpyHostToDevice, st));
+  SFFG_CK(cudaMemsetAsync(d_->nonfinite.p + s, 0, sizeof(int), st));
   return SFFG_OK;
 }
 
@@ -678,7 +680,21 @@ int Batch::get_energy_grad(int s, double *ene, double *g, void *stream) {
 
 int Batch::set_all_coords(const double *x, void *stream) {
   if (!finalized_) return SFFG_ESTATE;
-  SFFG_CK(cudaMemcpyAsync(d_->x.p, x, 3 * sizeof(double) * natom_total_, cudaMemcpyHostToDevice, pick(*d_, stream)));
+  cudaStream_t st = pick(*d_, stream);
+  SFFG_CK(cudaMemcpyAsync(d_->x.p, x, 3 * sizeof(double) * natom_total_, cudaMemcpyHostToDevice, st));
+  SFFG_CK(cudaMemsetAsync(d_->nonfinite.p, 0, d_->nonfinite.bytes(), st));
+  return SFFG_OK;
+}
+
+int Batch::system_status(std::vector<int> &status, void *stream) {
+  if (!finalized_) return SFFG_ESTATE;
+  const int nsys = num_systems();
+  std::vector<int> bad(nsys);
+  cudaStream_t st = pick(*d_, stream);
+  SFFG_CK(cudaMemcpyAsync(bad.data(), d_->nonfinite.p, nsys * sizeof(int), cudaMemcpyDeviceToHost, st));
+  SFFG_CK(cudaStreamSynchronize(st));
+  status.resize(nsys);
+  for (int s = 0; s < nsys; s++) status[s] = bad[s] ? SFFG_ENONFINITE : SFFG_OK;
   return SFFG_OK;
 }
 

@@ -91,6 +91,9 @@ class Batch {
   // order, systems in order), the active flags, and every system's energy
   // components (13 each) with the whole gradient.
   int set_all_coords(const double *x, void *stream);
+  // Per system: SFFG_OK, or SFFG_ENONFINITE once an evaluation met a
+  // non-finite coordinate (cleared when its coordinates are set again).
+  int system_status(std::vector<int> &status, void *stream);
   int set_all_active(const std::vector<int> &on, void *stream);
   int get_all_energy_grad(std::vector<double> &ene13, double *grad, void *stream);
   // XMIN on every system at once (csrc/batch_xmin.cpp): status, iteration

@@ -255,6 +255,32 @@ void ensure_finalized(const double *x) {
 
 }  // namespace
 
+// The checkpoint name mm_set_checkpoint() set (sff.c:2056); empty: none.
+std::string &checkpoint_name() {
+  static std::string name;
+  return name;
+}
+
+// Coordinates of iteration iter in the Cartesian format of the reference's
+// putxyz (sff.c:606-636); the name's leftmost "%d" becomes the iteration
+// number, or the number is appended (sff.c:789-830); "-" writes to nabout.
+void write_checkpoint(const std::string &tmpl, int natom, const double *x, int iter) {
+  if (iter < 0) return;
+  const std::string num = std::to_string(iter);
+  std::string name = tmpl;
+  const size_t at = name.find("%d");
+  if (at == std::string::npos) name += num;
+  else name.replace(at, 2, num);
+  FILE *fp = name == "-" ? legacy_out() : std::fopen(name.c_str(), "w");
+  if (!fp) {
+    std::fprintf(stderr, "Can't open file %s\n", name.c_str());
+    return;
+  }
+  std::fprintf(fp, "%6d\n", natom);
+  for (int i = 0; i < 3 * natom; i += 3) std::fprintf(fp, "%20.15f%20.15f%20.15f\n", x[i], x[i + 1], x[i + 2]);
+  if (fp != legacy_out()) std::fclose(fp);
+}
+
 extern "C" REAL_T mme(REAL_T *x, REAL_T *f, INT_T *iter) {
   Session &s = session();
   if (*iter == -3) return 0.0;  // the reference frees scratch here (eff.c:2504-2521)
@@ -263,6 +289,9 @@ extern "C" REAL_T mme(REAL_T *x, REAL_T *f, INT_T *iter) {
   Batch &b = *s.batch;
   if (*iter == 0) print_header();
   const Options &o = options();
+  // checkpoint every nchk iterations once a name is set (eff.c:2536-2538)
+  if (!checkpoint_name().empty() && *iter > 0 && o.nchk > 0 && *iter % o.nchk == 0)
+    write_checkpoint(checkpoint_name(), s.natom, x, *iter);
   const bool rebuild = !s.list_built || (*iter > 0 && o.nsnb > 0 && *iter % o.nsnb == 0) || *iter == -4;
   check(b.set_coords(0, x, nullptr), "set_coords");
   check(b.eval(rebuild, nullptr), "eval");
@@ -275,6 +304,7 @@ extern "C" REAL_T mme(REAL_T *x, REAL_T *f, INT_T *iter) {
 // mme() on a structure whose bond lengths RATTLE first restores, with the
 // gradient projected onto the constraints (src/sff/sff.c:1882-2010).
 extern "C" REAL_T mme_rattle(REAL_T *x, REAL_T *f, INT_T *iter);
+extern "C" void mm_set_checkpoint(STRING_T **fname);
 
 namespace {
 
@@ -856,6 +886,12 @@ extern "C" INT_T mme_timer(void) {
 extern "C" REAL_T rand2(void) { return rng().uniform(); }
 
 extern "C" REAL_T gauss2(REAL_T *mean, REAL_T *sd) { return rng().gauss(*mean, *sd); }
+
+extern "C" void mm_set_checkpoint(STRING_T **fname) {
+  checkpoint_name() = (fname && *fname) ? *fname : "";
+  std::fprintf(legacy_out(), "\tcheckpoint:  %s\n", checkpoint_name().c_str());
+  std::fflush(legacy_out());
+}
 
 extern "C" INT_T setseed(INT_T *seed) {
   if (*seed >= 0) {

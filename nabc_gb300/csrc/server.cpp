@@ -215,10 +215,23 @@ class Server {
   }
 
   // Takes the results of systems that ended and retires finished groups.
+  // A request whose coordinates turned non-finite ends at once with
+  // SFFG_ENONFINITE; the others in its group go on unaffected.
   int collect(std::string &err) {
     for (size_t gi = 0; gi < groups_.size();) {
       Group &g = groups_[gi];
       const int nsys = static_cast<int>(g.ids.size());
+      std::vector<int> health;
+      int rc0 = g.batch->system_status(health, g.stream);
+      if (rc0) {
+        err = g.batch->last_error;
+        return rc0;
+      }
+      for (int s = 0; s < nsys; s++) {
+        if (g.finished[s] || health[s] == SFFG_OK) continue;
+        g.batch->set_active(s, false, g.stream);
+        finish(g, s, SFFG_ENONFINITE, std::nan(""));
+      }
       bool all = true;
       if (g.kind == SFFG_REQ_MINIMIZE) {
         int na = 0;
