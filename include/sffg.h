@@ -106,6 +106,20 @@ int sffg_batch_md_steps(sffg_batch *b, int step0, int nsteps, void *stream);
 int sffg_batch_set_velocities(sffg_batch *b, int sys, const double *v, void *stream);
 int sffg_batch_get_velocities(sffg_batch *b, int sys, double *v, void *stream);
 
+/* Checkpoint and resume of batched md (no counterpart in the reference,
+ * whose md() cannot resume: its noise generator's state is not saved,
+ * src/sff/rand2.c:22-25).  save writes every system's coordinates,
+ * velocities, accelerations and Berendsen factors; load reads them into a
+ * batch of the same systems and evaluates there with fresh pair lists.
+ * Continued with sffg_batch_md_steps from the saved step number (the noise
+ * is counter-based), a run repeats the original bit for bit when the batch
+ * was built from the same topologies and initial coordinates and the state
+ * was saved right after a step whose number is a multiple of nsnb (where md
+ * rebuilds its lists) and not of nscm.  SFFG_EINVAL for a file of another
+ * batch. */
+int sffg_batch_save(sffg_batch *b, const char *path, void *stream);
+int sffg_batch_load(sffg_batch *b, const char *path, void *stream);
+
 /* Batched conjgrad() (src/sff/conjgrad.c:34): each system runs its own
  * copy of the reference's state machine; at most maxiter evaluations.
  * status[sys] receives the reference's return code (>0 converged after that

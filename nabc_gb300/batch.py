@@ -1,5 +1,6 @@
 """Python handle for the batched C API (include/sffg.h)."""
 import ctypes as C
+import os
 
 import numpy as np
 
@@ -93,6 +94,14 @@ class Batch:
         _check(sff.lib().sffg_batch_cg(self.h, maxiter, rmsgrad, dfpred, sff.iptr(st), sff.dptr(en), stream),
                "cg")
         return st, en
+
+    def save(self, path, stream=None):
+        """Write every system's md state (sffg_batch_save)."""
+        _check(sff.lib().sffg_batch_save(self.h, os.fsencode(path), stream), "save")
+
+    def load(self, path, stream=None):
+        """Read a saved md state into this batch (sffg_batch_load)."""
+        _check(sff.lib().sffg_batch_load(self.h, os.fsencode(path), stream), "load")
 
     def status(self, stream=None):
         """Per system: 0, or sffg's SFFG_ENONFINITE (-5) once an evaluation

@@ -119,6 +119,16 @@ extern "C" int sffg_batch_cg(sffg_batch *b, int maxiter, double rmsgrad, double 
   return SFFG_OK;
 }
 
+extern "C" int sffg_batch_save(sffg_batch *b, const char *path, void *stream) {
+  if (!b || !path) return fail(SFFG_EINVAL, "null batch or path");
+  SFFG_WRAP(b->impl->save_state(path, stream));
+}
+
+extern "C" int sffg_batch_load(sffg_batch *b, const char *path, void *stream) {
+  if (!b || !path) return fail(SFFG_EINVAL, "null batch or path");
+  SFFG_WRAP(b->impl->load_state(path, stream));
+}
+
 extern "C" int sffg_batch_status(sffg_batch *b, int *status, void *stream) {
   if (!b || !status) return fail(SFFG_EINVAL, "null batch or status");
   std::vector<int> st;

@@ -686,6 +686,68 @@ int Batch::set_all_coords(const double *x, void *stream) {
   return SFFG_OK;
 }
 
+namespace {
+constexpr char kStateMagic[8] = {'S', 'F', 'F', 'G', 'M', 'D', '1', 0};
+}
+
+int Batch::save_state(const char *path, void *stream) {
+  if (!finalized_) return SFFG_ESTATE;
+  DeviceState &d = *d_;
+  cudaStream_t st = pick(d, stream);
+  const size_t n3 = 3 * static_cast<size_t>(natom_total_), nsys = num_systems();
+  std::vector<double> buf(3 * n3 + nsys);
+  SFFG_CK(cudaMemcpyAsync(buf.data(), d.x.p, n3 * sizeof(double), cudaMemcpyDeviceToHost, st));
+  SFFG_CK(cudaMemcpyAsync(buf.data() + n3, d.v.p, n3 * sizeof(double), cudaMemcpyDeviceToHost, st));
+  SFFG_CK(cudaMemcpyAsync(buf.data() + 2 * n3, d.accel.p, n3 * sizeof(double), cudaMemcpyDeviceToHost, st));
+  SFFG_CK(cudaMemcpyAsync(buf.data() + 3 * n3, d.tscal.p, nsys * sizeof(double), cudaMemcpyDeviceToHost, st));
+  SFFG_CK(cudaStreamSynchronize(st));
+  FILE *fp = std::fopen(path, "wb");
+  if (!fp) {
+    last_error = std::string("save_state: cannot open ") + path;
+    return SFFG_EINVAL;
+  }
+  const long long hdr[2] = {natom_total_, static_cast<long long>(nsys)};
+  bool ok = std::fwrite(kStateMagic, 1, 8, fp) == 8 && std::fwrite(hdr, sizeof(hdr), 1, fp) == 1 &&
+            std::fwrite(buf.data(), sizeof(double), buf.size(), fp) == buf.size();
+  ok = (std::fclose(fp) == 0) && ok;
+  if (!ok) {
+    last_error = std::string("save_state: write failed: ") + path;
+    return SFFG_EINVAL;
+  }
+  return SFFG_OK;
+}
+
+int Batch::load_state(const char *path, void *stream) {
+  if (!finalized_) return SFFG_ESTATE;
+  DeviceState &d = *d_;
+  cudaStream_t st = pick(d, stream);
+  const size_t n3 = 3 * static_cast<size_t>(natom_total_), nsys = num_systems();
+  FILE *fp = std::fopen(path, "rb");
+  if (!fp) {
+    last_error = std::string("load_state: cannot open ") + path;
+    return SFFG_EINVAL;
+  }
+  char magic[8] = {};
+  long long hdr[2] = {0, 0};
+  std::vector<double> buf(3 * n3 + nsys);
+  bool ok = std::fread(magic, 1, 8, fp) == 8 && std::memcmp(magic, kStateMagic, 8) == 0 &&
+            std::fread(hdr, sizeof(hdr), 1, fp) == 1 && hdr[0] == natom_total_ &&
+            hdr[1] == static_cast<long long>(nsys) && std::fread(buf.data(), sizeof(double), buf.size(), fp) == buf.size();
+  std::fclose(fp);
+  if (!ok) {
+    last_error = std::string("load_state: not a state of this batch: ") + path;
+    return SFFG_EINVAL;
+  }
+  SFFG_CK(cudaMemcpyAsync(d.x.p, buf.data(), n3 * sizeof(double), cudaMemcpyHostToDevice, st));
+  SFFG_CK(cudaMemcpyAsync(d.v.p, buf.data() + n3, n3 * sizeof(double), cudaMemcpyHostToDevice, st));
+  SFFG_CK(cudaMemcpyAsync(d.accel.p, buf.data() + 2 * n3, n3 * sizeof(double), cudaMemcpyHostToDevice, st));
+  SFFG_CK(cudaMemcpyAsync(d.tscal.p, buf.data() + 3 * n3, nsys * sizeof(double), cudaMemcpyHostToDevice, st));
+  SFFG_CK(cudaMemsetAsync(d.ekin.p, 0, d.ekin.bytes(), st));
+  SFFG_CK(cudaMemsetAsync(d.nonfinite.p, 0, d.nonfinite.bytes(), st));
+  SFFG_CK(cudaStreamSynchronize(st));  // the staging buffer goes out of scope
+  return run_eval(true, stream);
+}
+
 int Batch::system_status(std::vector<int> &status, void *stream) {
   if (!finalized_) return SFFG_ESTATE;
   const int nsys = num_systems();

@@ -94,6 +94,14 @@ class Batch {
   // Per system: SFFG_OK, or SFFG_ENONFINITE once an evaluation met a
   // non-finite coordinate (cleared when its coordinates are set again).
   int system_status(std::vector<int> &status, void *stream);
+  // The md state of every system (coordinates, velocities, accelerations,
+  // Berendsen factors) to or from a file.  load_state evaluates at the
+  // loaded coordinates with fresh pair lists, so md continued from a state
+  // saved right after a list-rebuild step (step % nsnb == 0, without a
+  // centre-of-mass removal there) in a batch built from the same
+  // topologies and initial coordinates repeats the original run bit for bit.
+  int save_state(const char *path, void *stream);
+  int load_state(const char *path, void *stream);
   int set_all_active(const std::vector<int> &on, void *stream);
   int get_all_energy_grad(std::vector<double> &ene13, double *grad, void *stream);
   // XMIN on every system at once (csrc/batch_xmin.cpp): status, iteration

@@ -117,3 +117,48 @@ def test_mme_checkpoint_files(lib, tmp_path):
         assert int(lines[0]) == n and len(lines) == n + 1
         xyz = np.array([[float(line[20 * c:20 * (c + 1)]) for c in range(3)] for line in lines[1:]])
         np.testing.assert_allclose(xyz.ravel(), x, atol=1e-14)
+
+
+def test_md_checkpoint_resume_bit_identical(lib, tmp_path):
+    """Batched Langevin md saved after step 10 (a list-rebuild step,
+    nsnb 5) and resumed in a new batch built from the same inputs repeats
+    the uninterrupted run's coordinates and velocities bit for bit at step
+    20; a state file of another batch is refused."""
+    from nabc_gb300.batch import Batch
+    from nabc_gb300 import sff
+    mols = molecules()[:2]
+    opts = "gb=5, cut=12.0, rgbmax=10.0, nsnb=5, dt=0.002, gamma_ln=5.0, temp0=300.0"
+
+    def make():
+        b = Batch(opts)
+        for prm, x in mols:
+            b.add(prm, x)
+        b.finalize()
+        return b
+
+    b = make()
+    b.md_begin()
+    b.md_steps(0, 20)
+    want = [(b.coords(s), b.velocities(s)) for s in range(2)]
+    b.close()
+    path = str(tmp_path / "md.state")
+    b = make()
+    b.md_begin()
+    b.md_steps(0, 10)
+    b.save(path)
+    b.close()
+    b = make()
+    b.load(path)
+    b.md_steps(10, 10)
+    got = [(b.coords(s), b.velocities(s)) for s in range(2)]
+    b.close()
+    for (x1, v1), (x2, v2) in zip(want, got):
+        assert np.array_equal(x1, x2) and np.array_equal(v1, v2)
+    other = Batch(opts)
+    prm, x = mols[0]
+    other.add(prm, x)
+    other.finalize()
+    from nabc_gb300.batch import SffgError
+    with pytest.raises(SffgError):
+        other.load(path)
+    other.close()
