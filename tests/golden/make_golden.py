@@ -72,7 +72,7 @@ REF_CASES = [
      "ntpr=1, gb=8, rgbmax=15.0, cut=99.0, diel=C, e_debug=0", "gb8trx.out.check"),
 ]
 EXTRA_INPUTS = ["nab/asp.top", "nab/asp.pdb", "xfin.parm7", "xfin.rst7", "xfin.md1.rst7", "nab/NMA.pdb",
-                "nab/NMA_scee+scnb.prmtop"]
+                "nab/NMA_scee+scnb.prmtop", "nab/Na+.parm7", "nab/Na+.pdb"]
 
 BREAKDOWN = ["bond", "angle", "dihedral", "enb14", "eel14", "enb", "eel", "egb", "econs", "esurf", "Total",
              "frms"]
@@ -274,6 +274,13 @@ def main():
                opts, tmp])
     checks["variable_14"] = {"prmtop": "NMA_scee+scnb.prmtop", "coords": "NMA.pdb", "options": opts,
                              "ff": parse_ff(text), "sp": parse_breakdown(out)}
+    # a single ion: the Born self-energy alone (one atom, no pairs)
+    for gbk in (1, 5, 8):
+        opts = f"gb={gbk}, cut=999.0, rgbmax=15.0"
+        out = run([SFFREF, os.path.join(HERE, "ref", "Na+.parm7"), os.path.join(HERE, "ref", "Na+.pdb"), "sp", opts,
+                   tmp])
+        checks[f"na_gb{gbk}"] = {"prmtop": "Na+.parm7", "coords": "Na+.pdb", "options": opts,
+                                 "sp": parse_breakdown(out)}
     text = open(os.path.join(nab, "txmin.out.check")).read()
     checks["nab_txmin"] = {"prmtop": "gbrna.prmtop", "coords": "gbrna.pdb",
                            "options": "ntpr=1, gb=1, kappa=0.10395, rgbmax=99., cut=99.0, diel=C",

@@ -35,12 +35,12 @@ def gpu_eval(prm, x, opts):
     return out
 
 
-def assert_close(ene, g, reff, ene0, g0, reff0):
+def assert_close(ene, g, reff, ene0, g0, reff0, g_rms=G_RMS):
     assert abs(ene[0] - ene0[0]) <= E_REL * abs(ene0[0]), (ene[0], ene0[0])
     for k in (1, 2, 3, 4, 5, 7, 8, 10):
         assert abs(ene[k] - ene0[k]) <= E_REL * max(abs(ene0[k]), abs(ene0[0])), (k, ene[k], ene0[k])
     rms = np.sqrt(((g - g0) ** 2).mean())
-    assert rms <= G_RMS, rms
+    assert rms <= g_rms, rms
     if reff is not None:
         assert np.max(np.abs(reff / reff0 - 1.0)) <= REFF_REL
 
@@ -120,3 +120,41 @@ def test_deterministic(lib, checks):
         assert np.array_equal(b.energy(0), e1)
         assert np.array_equal(b.grad(0), g1)
     b.close()
+
+
+@pytest.mark.parametrize("gbk", [1, 5, 8])
+def test_single_ion(lib, oracle_mod, checks, gbk):
+    """One atom (Na+): a tile holding a single atom, no pairs at all; the
+    Born self-energy of the compiled reference and the oracle, zero
+    gradient."""
+    c = checks[f"na_gb{gbk}"]
+    prm, x = load_case(c)
+    ene, g, reff, npairs = gpu_eval(prm, x, c["options"])
+    assert npairs == 0
+    assert ene[0] == pytest.approx(c["sp"]["Total"], rel=E_REL)
+    assert ene[10] == pytest.approx(c["sp"]["egb"], rel=E_REL)
+    assert np.all(g == 0.0)
+    o = oracle_mod.Oracle(prm, c["options"])
+    e0, ene0, g0, reff0 = o.mme(x)
+    assert_close(ene, g, reff, ene0, g0, reff0)
+
+
+@pytest.mark.parametrize("natom", [4, 5, 8, 12, 31, 32])
+def test_tiny_molecules(lib, oracle_mod, natom):
+    """Tiny synthetic molecules (one partial or exactly full tile, most
+    pairs excluded as 1-2/1-3 neighbours) for each GB model, against the
+    oracle.  These compact chains have steep repulsive contacts (gradients
+    up to 67 kcal/mol/A for 12 atoms), where FP32 rounding of the r^-12 term
+    is ~5e-7 of the component, so the gradient bar here is the larger of
+    1e-5 kcal/mol/A and 1e-6 of the gradient's RMS (measured worst: 1.0e-5
+    against an RMS gradient of 21)."""
+    from nabc_gb300 import sff
+    prm, x, _ = sff.synth_molecule(natom, 40 + natom)
+    for opts in ("gb=1, cut=999.0, rgbmax=15.0", "gb=5, cut=999.0, rgbmax=15.0, kappa=0.1",
+                 "gb=8, cut=999.0, rgbmax=25.0"):
+        ene, g, reff, npairs = gpu_eval(prm, x, opts)
+        o = oracle_mod.Oracle(prm, opts)
+        e0, ene0, g0, reff0 = o.mme(x)
+        assert npairs == o.npairs()
+        assert_close(ene, g, reff, ene0, g0, reff0, g_rms=max(G_RMS, 1e-6 * np.sqrt((g0 ** 2).mean())))
+    sff.free_prm(prm)
