@@ -246,6 +246,17 @@ int sffg_server_destroy(sffg_server *s);
 int sffg_born_radii_static(int natom, const double *x, const double *rborn, const double *fs, int gb,
                            double rgbmax, double *reff, void *stream);
 
+/* ---- checked build ------------------------------------------------------ */
+
+/* A library built with -DSFFG_CHECKED (for example SFFG_NVCC_EXTRA=
+ * -DSFFG_CHECKED SFFG_BUILD_DIR=<dir> python -m nabc_gb300._build) tests
+ * every indirect index of its kernels against the array's extent and, on a
+ * failure, records a code (1 list entry slot, 2 tile, 3 Lennard-Jones row,
+ * 4 neck table, 5 bonded-term atom) and reads element 0 instead, without
+ * trapping.  Returns the first code recorded, 0 when every check passed,
+ * -1 in the normal build. */
+int sffg_checked_code(void);
+
 #ifdef __cplusplus
 }
 #endif

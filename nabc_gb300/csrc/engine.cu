@@ -808,6 +808,8 @@ DevTables make_tables(DeviceState &d, const ModelParams &mp, double fsmax, int q
   t.sys_ntypes = d.sys_ntypes.p;
   t.lj = d.lj.p;
   t.lj_n = static_cast<int>(d.lj.n);
+  t.nslot = static_cast<int>(d.pos_hi.n);
+  t.ntile = static_cast<int>(d.tile_sys.n);
   t.la.chunk_i = d.chunkA_i.p;
   t.la.slot = d.entA_slot.p;
   t.la.col = d.entA_col.p;
@@ -1161,6 +1163,7 @@ int Batch::run_eval_direct(bool rebuild, void *stream) {
   SFFG_CK(cudaStreamWaitEvent(d.side, d.fork_ev, 0));
   const cudaStream_t bs = d.side;
   BondedArgs ba;
+  ba.natom = natom_total_;
   ba.x = d.x.p;
   ba.atom_slot = d.atom_slot.p;
   ba.atom_sys = d.atom_sys.p;
@@ -1934,3 +1937,18 @@ int Batch::cg(int maxiter, double rmsgrad, double dfpred, bool first_rebuild, st
 }
 
 }  // namespace sffg
+
+// The first failed bounds check of a build with -DSFFG_CHECKED (a
+// CheckCode), 0 when none failed, -1 in the normal build.
+extern "C" int sffg_checked_code(void) {
+#ifdef SFFG_CHECKED
+  int c = 0;
+  cudaMemcpyFromSymbol(&c, sffg::g_check_code, sizeof(int));
+  const int codes[4] = {c, sffg::pass1_check_code(), sffg::pass2_check_code(), sffg::pass3_check_code()};
+  for (int k : codes)
+    if (k) return k;
+  return 0;
+#else
+  return -1;
+#endif
+}

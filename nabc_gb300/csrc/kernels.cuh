@@ -49,6 +49,7 @@ struct DevTables {
   const float2 *lj;       // (A, B) per type pair, per system blocks
   int lj_n;               // entries of lj
   bool lj_shared;         // pass 2 may stage lj in shared memory
+  int nslot, ntile;       // extents, for the checked build
   // lists: la (r < cut) for pass 2; lb and lc (r < rgbmax + Fsmax + skin,
   // lc the pairs within near-field range) for passes 1 and 3
   ChunkList la, lb, lc;
@@ -63,6 +64,29 @@ struct DevTables {
   float neck_scale;
   const float *neck_pos, *neck_val;  // 441 each
 };
+
+// ---- checked build ---------------------------------------------------------
+// With -DSFFG_CHECKED every indirect index of the kernels (list entries,
+// tiles, table rows, atoms of bonded terms) is tested against its array's
+// extent; a failed test records a code in the translation unit's error word
+// (the first failure wins), the access goes to element 0 instead, and the
+// kernel runs on: an out-of-range index is reported, never dereferenced,
+// and nothing traps.  sffg_checked_code() reads the word.  Without the
+// option the checks compile to nothing.
+enum CheckCode { kCheckSlot = 1, kCheckTile = 2, kCheckLj = 3, kCheckNeck = 4, kCheckAtom = 5 };
+#ifdef SFFG_CHECKED
+static __device__ int g_check_code;
+__device__ __forceinline__ int checked_index(int i, int n, int code) {
+  if (static_cast<unsigned>(i) >= static_cast<unsigned>(n)) {
+    atomicCAS(&g_check_code, 0, code);
+    return 0;
+  }
+  return i;
+}
+#define SFFG_IDX(i, n, code) ::sffg::checked_index((i), (n), (code))
+#else
+#define SFFG_IDX(i, n, code) (i)
+#endif
 
 __device__ __forceinline__ long long to_fixed(float v, float scale) {
   return __float2ll_rn(v * scale);
@@ -168,10 +192,10 @@ __device__ __forceinline__ void descreen_pair(const BornConst &c, bool in, float
 // Stages the j-entries of chunk k in shared memory: lane l loads entry l.
 // Returns this lane's j slot (padding entries point at a real slot of the
 // i-tile and have an empty column).
-__device__ __forceinline__ int chunk_entry(const ChunkList &L, int k, int lane, unsigned &col) {
+__device__ __forceinline__ int chunk_entry(const ChunkList &L, int k, int lane, unsigned &col, int nslot) {
   const size_t e = static_cast<size_t>(k) * 32 + lane;
   col = L.col[e];
-  return L.slot[e];
+  return SFFG_IDX(L.slot[e], nslot, kCheckSlot);
 }
 
 // ------------------------------------------------------------ list C chunks
@@ -229,7 +253,7 @@ __device__ __forceinline__ int near_stage(const DevTables &t, int k, int lane, f
                                           bool sda) {
   const size_t e = static_cast<size_t>(k) * 32 + lane;
   col = t.lc.col[e];
-  sj = t.lc.slot[e];
+  sj = SFFG_IDX(t.lc.slot[e], t.nslot, kCheckSlot);
   float4 l = t.pos_lo[sj];
   if (sda) l.w = t.sumda32[sj];
   hj[lane] = t.pos_hi[sj];
@@ -278,7 +302,7 @@ __global__ void __launch_bounds__(256, 3) k_born(const DevTables t) {
   // list B chunk k: lanes hold the i-tile, steps walk the 32 j-entries
   auto far_chunk = [&](int k) {
     unsigned mycol;
-    const int sj = chunk_entry(t.lb, k, lane, mycol);
+    const int sj = chunk_entry(t.lb, k, lane, mycol, t.nslot);
     sm_hi[w][lane] = t.pos_hi[sj];
     sm_lo[w][lane] = t.pos_lo[sj];
     {
@@ -317,8 +341,8 @@ __global__ void __launch_bounds__(256, 3) k_born(const DevTables t) {
           const bool nk = in && dij < rbi + gp.z + 6.8f;
           if (__any_sync(kFull, nk)) {
             const int nkj = (sm_par[w][j] >> 16) & 0xff;
-            const float a = neck_term(dij, s_npos[nki * 21 + nkj], s_nval[nki * 21 + nkj], t.neck_scale);
-            const float b = neck_term(dij, s_npos[nkj * 21 + nki], s_nval[nkj * 21 + nki], t.neck_scale);
+            const float a = neck_term(dij, s_npos[SFFG_IDX(nki * 21 + nkj, 441, kCheckNeck)], s_nval[SFFG_IDX(nki * 21 + nkj, 441, kCheckNeck)], t.neck_scale);
+            const float b = neck_term(dij, s_npos[SFFG_IDX(nkj * 21 + nki, 441, kCheckNeck)], s_nval[SFFG_IDX(nkj * 21 + nki, 441, kCheckNeck)], t.neck_scale);
             ti += nk ? a : 0.0f;
             tj += nk ? b : 0.0f;
           }
@@ -361,8 +385,8 @@ __global__ void __launch_bounds__(256, 3) k_born(const DevTables t) {
           tj = fmaf(tj, gi.w, tj);
           if (NECK && dij < gi.z + gp.z + 6.8f) {
             const int nkp = (si_par[w][il] >> 16) & 0xff, nkj = (sm_par[w][jl] >> 16) & 0xff;
-            ti += neck_term(dij, s_npos[nkp * 21 + nkj], s_nval[nkp * 21 + nkj], t.neck_scale);
-            tj += neck_term(dij, s_npos[nkj * 21 + nkp], s_nval[nkj * 21 + nkp], t.neck_scale);
+            ti += neck_term(dij, s_npos[SFFG_IDX(nkp * 21 + nkj, 441, kCheckNeck)], s_nval[SFFG_IDX(nkp * 21 + nkj, 441, kCheckNeck)], t.neck_scale);
+            tj += neck_term(dij, s_npos[SFFG_IDX(nkj * 21 + nkp, 441, kCheckNeck)], s_nval[SFFG_IDX(nkj * 21 + nkp, 441, kCheckNeck)], t.neck_scale);
           }
         }
       }
@@ -386,7 +410,7 @@ __global__ void __launch_bounds__(256, 3) k_born(const DevTables t) {
     for (int m = base; m < end; m++) {
       int k;
       const bool nr = merged_item(m, nB, nC, k);
-      const int I = nr ? t.lc.chunk_i[k] : t.lb.chunk_i[k];
+      const int I = SFFG_IDX(nr ? t.lc.chunk_i[k] : t.lb.chunk_i[k], t.ntile, kCheckTile);
       if (!t.sys_active[t.tile_sys[I]]) continue;
       if (I != cur_I) {
         if (cur_I >= 0) atomic_add_ll(&t.acc_sumi[cur_I * 32 + lane], sumi64);
@@ -460,7 +484,7 @@ __global__ void __launch_bounds__(256, 3) k_gbpair(const DevTables t) {
     if (base >= nchunk) break;
     const int end = min(base + t.claim, nchunk);
     for (int k = base; k < end; k++) {
-      const int I = t.la.chunk_i[k];
+      const int I = SFFG_IDX(t.la.chunk_i[k], t.ntile, kCheckTile);
       const int sys = t.tile_sys[I];
       if (!t.sys_active[sys]) continue;
       if (sys != cur_sys) {
@@ -481,7 +505,7 @@ __global__ void __launch_bounds__(256, 3) k_gbpair(const DevTables t) {
         ti = t.param[sl] & 0xffff;
       }
       unsigned mycol;
-      const int sj = chunk_entry(t.la, k, lane, mycol);
+      const int sj = chunk_entry(t.la, k, lane, mycol, t.nslot);
       {
         float4 l = t.pos_lo[sj];
         l.w = t.reff32[sj];
@@ -511,7 +535,12 @@ __global__ void __launch_bounds__(256, 3) k_gbpair(const DevTables t) {
           const bool in = (au.z >> lane) & 1u;
           const bool coul = !((au.w >> lane) & 1u);
           // row type_j: the lanes' i types fall in one row of the symmetric table
+#ifdef SFFG_CHECKED
+          const float2 ab = lj_all[SFFG_IDX(static_cast<int>(lj - lj_all) + static_cast<int>(au.y) + ti, t.lj_n,
+                                            kCheckLj)];
+#else
           const float2 ab = lj[au.y + ti];
+#endif
           const PairOut o = gb_pair<KAPPA>(t.pair, r2, qi * h.w, ri, l.w, rvi, __uint_as_float(au.x), coul, ab.x,
                                            ab.y);
           const float de = in ? o.de : 0.0f;
@@ -592,7 +621,7 @@ __global__ void __launch_bounds__(256, 3) k_chain(const DevTables t) {
 
   auto far_chunk = [&](int k) {
     unsigned mycol;
-    const int sj = chunk_entry(t.lb, k, lane, mycol);
+    const int sj = chunk_entry(t.lb, k, lane, mycol, t.nslot);
     {
       float4 l = t.pos_lo[sj];
       l.w = t.sumda32[sj];
@@ -631,8 +660,8 @@ __global__ void __launch_bounds__(256, 3) k_chain(const DevTables t) {
           const bool nk = in && dij < rbi + gp.z + 6.8f;
           if (__any_sync(kFull, nk)) {
             const int nkj = (sm_par[w][j] >> 16) & 0xff;
-            const float a = neck_deriv(dij, s_npos[nki * 21 + nkj], s_nval[nki * 21 + nkj], t.neck_scale);
-            const float b = neck_deriv(dij, s_npos[nkj * 21 + nki], s_nval[nkj * 21 + nki], t.neck_scale);
+            const float a = neck_deriv(dij, s_npos[SFFG_IDX(nki * 21 + nkj, 441, kCheckNeck)], s_nval[SFFG_IDX(nki * 21 + nkj, 441, kCheckNeck)], t.neck_scale);
+            const float b = neck_deriv(dij, s_npos[SFFG_IDX(nkj * 21 + nki, 441, kCheckNeck)], s_nval[SFFG_IDX(nkj * 21 + nki, 441, kCheckNeck)], t.neck_scale);
             di += nk ? a : 0.0f;
             dj += nk ? b : 0.0f;
           }
@@ -683,8 +712,8 @@ __global__ void __launch_bounds__(256, 3) k_chain(const DevTables t) {
           dj = fmaf(dj, gi.w, dj);
           if (NECK && dij < gi.z + gp.z + 6.8f) {
             const int nkp = (si_par[w][il] >> 16) & 0xff, nkj = (sm_par[w][jl] >> 16) & 0xff;
-            di += neck_deriv(dij, s_npos[nkp * 21 + nkj], s_nval[nkp * 21 + nkj], t.neck_scale);
-            dj += neck_deriv(dij, s_npos[nkj * 21 + nkp], s_nval[nkj * 21 + nkp], t.neck_scale);
+            di += neck_deriv(dij, s_npos[SFFG_IDX(nkp * 21 + nkj, 441, kCheckNeck)], s_nval[SFFG_IDX(nkp * 21 + nkj, 441, kCheckNeck)], t.neck_scale);
+            dj += neck_deriv(dij, s_npos[SFFG_IDX(nkj * 21 + nkp, 441, kCheckNeck)], s_nval[SFFG_IDX(nkj * 21 + nkp, 441, kCheckNeck)], t.neck_scale);
           }
           const float gg = fmaf(li.w, di, l.w * dj);
           gx = gg * dx;
@@ -720,7 +749,7 @@ __global__ void __launch_bounds__(256, 3) k_chain(const DevTables t) {
     for (int m = base; m < end; m++) {
       int k;
       const bool nr = merged_item(m, nB, nC, k);
-      const int I = nr ? t.lc.chunk_i[k] : t.lb.chunk_i[k];
+      const int I = SFFG_IDX(nr ? t.lc.chunk_i[k] : t.lb.chunk_i[k], t.ntile, kCheckTile);
       if (!t.sys_active[t.tile_sys[I]]) continue;
       if (I != cur_I) {
         if (cur_I >= 0) flush_i();

@@ -163,6 +163,7 @@ __global__ void k_chain_prep(const long long *acc_sd, const double *chainfac, co
 // FP64, one thread per term, forces scattered in fixed point.  Terms are
 // stored with batch-global atom indices, grouped by system.
 struct BondedArgs {
+  int natom;  // atoms of the batch, for the checked build
   const double *x;
   const int *atom_slot;
   const int *atom_sys;
@@ -198,7 +199,7 @@ __global__ void k_bonds(const BondedArgs a, const int2 *atoms, const double2 *pa
   int sys = -1;
   double e = 0.0;
   if (i < n) {
-    const int p = atoms[i].x, q = atoms[i].y;
+    const int p = SFFG_IDX(atoms[i].x, a.natom, kCheckAtom), q = SFFG_IDX(atoms[i].y, a.natom, kCheckAtom);
     sys = a.atom_sys[p];
     if (!a.sys_active[sys]) {
       sys = -1;
@@ -223,7 +224,8 @@ __global__ void k_angles(const BondedArgs a, const int4 *atoms, const double2 *p
   int sys = -1;
   double e = 0.0;
   if (i < n) {
-    const int p = atoms[i].x, q = atoms[i].y, r = atoms[i].z;
+    const int p = SFFG_IDX(atoms[i].x, a.natom, kCheckAtom), q = SFFG_IDX(atoms[i].y, a.natom, kCheckAtom),
+              r = SFFG_IDX(atoms[i].z, a.natom, kCheckAtom);
     sys = a.atom_sys[p];
     if (!a.sys_active[sys]) {
       sys = -1;
@@ -261,7 +263,8 @@ __global__ void k_dihedrals(const BondedArgs a, const int4 *atoms, const double4
   int sys = -1;
   double e = 0.0;
   if (i < n) {
-    const int p = atoms[i].x, q = atoms[i].y, r = atoms[i].z, w = atoms[i].w;
+    const int p = SFFG_IDX(atoms[i].x, a.natom, kCheckAtom), q = SFFG_IDX(atoms[i].y, a.natom, kCheckAtom),
+              r = SFFG_IDX(atoms[i].z, a.natom, kCheckAtom), w = SFFG_IDX(atoms[i].w, a.natom, kCheckAtom);
     sys = a.atom_sys[p];
     if (!a.sys_active[sys]) {
       sys = -1;
@@ -329,7 +332,7 @@ __global__ void k_pairs14(const BondedArgs a, const int4 *atoms, const double4_3
   int sys = -1;
   double eel = 0.0, evdw = 0.0;
   if (i < n) {
-    const int p = atoms[i].x, q = atoms[i].y;
+    const int p = SFFG_IDX(atoms[i].x, a.natom, kCheckAtom), q = SFFG_IDX(atoms[i].y, a.natom, kCheckAtom);
     sys = a.atom_sys[p];
     if (!a.sys_active[sys]) {
       sys = -1;

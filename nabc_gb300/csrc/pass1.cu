@@ -15,4 +15,14 @@ int born_blocks_per_sm(bool neck) {
   return occ > 0 ? occ : 1;
 }
 
+int pass1_check_code() {
+#ifdef SFFG_CHECKED
+  int c = 0;
+  cudaMemcpyFromSymbol(&c, g_check_code, sizeof(int));
+  return c;
+#else
+  return 0;
+#endif
+}
+
 }  // namespace sffg

@@ -23,4 +23,14 @@ int gbpair_blocks_per_sm(bool kappa) {
   return occ > 0 ? occ : 1;
 }
 
+int pass2_check_code() {
+#ifdef SFFG_CHECKED
+  int c = 0;
+  cudaMemcpyFromSymbol(&c, g_check_code, sizeof(int));
+  return c;
+#else
+  return 0;
+#endif
+}
+
 }  // namespace sffg

@@ -36,5 +36,10 @@ void launch_chain(bool neck, int grid, cudaStream_t st, const DevTables &t);
 int born_blocks_per_sm(bool neck);
 int gbpair_blocks_per_sm(bool kappa);
 int chain_blocks_per_sm(bool neck);
+// The checked build's error word of each pass's translation unit (0 when
+// no check failed, and always 0 in the normal build).
+int pass1_check_code();
+int pass2_check_code();
+int pass3_check_code();
 
 }  // namespace sffg

@@ -135,6 +135,8 @@ def lib():
         L.sffg_batch_cg.argtypes = [vp, C.c_int, C.c_double, C.c_double, INT_P, REAL_P, vp]
         L.sffg_batch_xmin.argtypes = [vp, C.POINTER(XMIN_OPT_T), INT_P, INT_P, REAL_P, vp]
         L.sffg_batch_status.argtypes = [vp, INT_P, vp]
+        L.sffg_checked_code.argtypes = []
+        L.sffg_checked_code.restype = C.c_int
         L.sffg_batch_save.argtypes = [vp, C.c_char_p, vp]
         L.sffg_batch_load.argtypes = [vp, C.c_char_p, vp]
         L.mm_set_checkpoint.argtypes = [C.POINTER(C.c_char_p)]
