@@ -8,6 +8,8 @@
 #include <map>
 #include <numeric>
 
+#include <nvtx3/nvToolsExt.h>
+
 #include "engine.h"
 #include "gbneck_tables.h"
 #include "kernels_aux.cuh"
@@ -36,6 +38,14 @@ struct DBuf {
   size_t bytes() const { return n * sizeof(T); }
 };
 
+
+// NVTX range over a host-side scope: evaluations, list builds, md and
+// minimiser turns show as named ranges in Nsight Systems or under ncu
+// --nvtx (free when no tool is attached).
+struct Range {
+  explicit Range(const char *name) { nvtxRangePushA(name); }
+  ~Range() { nvtxRangePop(); }
+};
 
 }  // namespace
 
@@ -930,6 +940,7 @@ double Batch::fsmax_all() const {
 // Both pair lists from the current coordinates (lists.cuh, stages 1-6).
 // The host reads two counts back (candidates, chunks) to size the stores.
 int Batch::build_lists(void *stream) {
+  Range range("sffg list build");
   DeviceState &d = *d_;
   cudaStream_t st = pick(d, stream);
   const double fsmax = fsmax_all();
@@ -1130,6 +1141,7 @@ int Batch::tuned_split(int pass, int *claim, int *blocks) const {
 // One evaluation; without a list rebuild it replays a captured graph (one
 // launch instead of ~20) unless graphs are off or pass timing is on.
 int Batch::run_eval(bool rebuild, void *stream) {
+  Range range("sffg evaluation");
   DeviceState &d = *d_;
   cudaStream_t st = pick(d, stream);
   if (!rebuild) {
@@ -1202,7 +1214,10 @@ int Batch::run_eval_direct(bool rebuild, void *stream) {
     DevTables t = make_tables(d, mp_, fsmax, 5);
     t.claim = cfg_[0].claim;
     if (tuning_) SFFG_CK(cudaEventRecord(d.tune_ev[0][0], st));
-    launch_born(neck, cfg_[0].blocks, st, t);
+    {
+      Range range("pass 1 Born radii");
+      launch_born(neck, cfg_[0].blocks, st, t);
+    }
     if (tuning_) SFFG_CK(cudaEventRecord(d.tune_ev[0][1], st));
     SFFG_CK(cudaGetLastError());
   }
@@ -1242,7 +1257,10 @@ int Batch::run_eval_direct(bool rebuild, void *stream) {
     t.claim = cfg_[1].claim;
     t.lj_shared = opts_.sffg_lj_shared != 0;
     if (tuning_) SFFG_CK(cudaEventRecord(d.tune_ev[1][0], st));
-    launch_gbpair(mp_.kappa != 0.0, cfg_[1].blocks, st, t);
+    {
+      Range range("pass 2 GB Coulomb LJ");
+      launch_gbpair(mp_.kappa != 0.0, cfg_[1].blocks, st, t);
+    }
     if (tuning_) SFFG_CK(cudaEventRecord(d.tune_ev[1][1], st));
     SFFG_CK(cudaGetLastError());
   }
@@ -1255,7 +1273,10 @@ int Batch::run_eval_direct(bool rebuild, void *stream) {
     DevTables t = make_tables(d, mp_, fsmax, 7);
     t.claim = cfg_[2].claim;
     if (tuning_) SFFG_CK(cudaEventRecord(d.tune_ev[2][0], st));
-    launch_chain(neck, cfg_[2].blocks, st, t);
+    {
+      Range range("pass 3 chain rule");
+      launch_chain(neck, cfg_[2].blocks, st, t);
+    }
     if (tuning_) SFFG_CK(cudaEventRecord(d.tune_ev[2][1], st));
     SFFG_CK(cudaGetLastError());
   }
@@ -1460,6 +1481,7 @@ int Batch::md_com_remove(void *stream) {
 }
 
 int Batch::md_steps(int step0, int k, NoiseFn noise, void *noise_ctx, void *stream, bool com_at_end) {
+  Range range("sffg md steps");
   if (!finalized_) return SFFG_ESTATE;
   DeviceState &d = *d_;
   cudaStream_t st = pick(d, stream);
@@ -1825,6 +1847,7 @@ int Batch::cg_begin(const std::vector<int> &maxiter, const std::vector<double> &
 }
 
 int Batch::cg_turns(int n, bool first_rebuild, void *stream, const std::function<int(int)> &after_eval) {
+  Range range("sffg conjgrad turns");
   DeviceState &d = *d_;
   cudaStream_t st = pick(d, stream);
   CgArgs a;
