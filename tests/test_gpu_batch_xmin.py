@@ -113,15 +113,25 @@ def test_reactivated_systems_get_their_lists(lib):
     plain evaluation equals a rebuilt one for every system."""
     from nabc_gb300 import sff
     from nabc_gb300.batch import Batch
-    b = Batch("gb=5, cut=12.0, rgbmax=10.0")
+    opts = "gb=5, cut=12.0, rgbmax=10.0"
     prms = []
-    for natom, seed in ((200, 1), (1500, 2)):
-        prm, x, _ = sff.synth_molecule(natom, seed)
-        prms.append(prm)
-        b.add(prm, x)
+    small, xs, _ = sff.synth_molecule(200, 1)
+    big, xb, _ = sff.synth_molecule(1500, 2)
+    prms += [small, big]
+    # the small molecule first minimised alone, so it ends at once below
+    b = Batch(opts)
+    b.add(small, xs)
     b.finalize()
-    st, it, en = b.xmin(method=2, maxiter=60, grms_tol=0.5)
-    assert it[0] != it[1]  # one system ended while the other went on
+    st, it, en = b.xmin(method=2, maxiter=3000, grms_tol=0.05)
+    xs = b.coords(0)
+    tol = 2.0 * np.sqrt((b.grad(0) ** 2).mean())  # above the small one's end, far below the big one's start
+    b.close()
+    b = Batch(opts)
+    b.add(small, xs)
+    b.add(big, xb)
+    b.finalize()
+    st, it, en = b.xmin(method=2, maxiter=30, grms_tol=tol)
+    assert it[0] < it[1]  # one system ended while the other went on
     b.eval(rebuild=False)
     e0 = [b.energy(s) for s in range(2)]
     b.eval(rebuild=True)
