@@ -533,7 +533,7 @@ __global__ void __launch_bounds__(256, 3) k_gbpair(const DevTables t) {
           const float dz = (zi - h.z) + (zli - l.z);
           const float r2 = fmaf(dx, dx, fmaf(dy, dy, dz * dz));
           const bool in = (au.z >> lane) & 1u;
-          const bool coul = !((au.w >> lane) & 1u);
+          const bool coul = in && !((au.w >> lane) & 1u);
           // row type_j: the lanes' i types fall in one row of the symmetric table
 #ifdef SFFG_CHECKED
           const float2 ab = lj_all[SFFG_IDX(static_cast<int>(lj - lj_all) + static_cast<int>(au.y) + ti, t.lj_n,
@@ -541,20 +541,23 @@ __global__ void __launch_bounds__(256, 3) k_gbpair(const DevTables t) {
 #else
           const float2 ab = lj[au.y + ti];
 #endif
-          const PairOut o = gb_pair<KAPPA>(t.pair, r2, qi * h.w, ri, l.w, rvi, __uint_as_float(au.x), coul, ab.x,
-                                           ab.y);
-          const float de = in ? o.de : 0.0f;
+          // a lane off the list gets zero charge and coefficients (and r2 = 1:
+          // the self pair of a diagonal tile has r2 = 0), hence zero terms
+          const float qq = in ? qi * h.w : 0.0f;
+          const PairOut o = gb_pair<KAPPA>(t.pair, in ? r2 : 1.0f, qq, coul ? qq : 0.0f, ri, l.w, rvi,
+                                           __uint_as_float(au.x), coul ? ab.x : 0.0f, coul ? ab.y : 0.0f);
+          const float de = o.de;
           fix = fmaf(de, dx, fix);
           fiy = fmaf(de, dy, fiy);
           fiz = fmaf(de, dz, fiz);
           ax[s] = -de * dx;
           ay[s] = -de * dy;
           az[s] = -de * dz;
-          sdi += in ? o.sd_i : 0.0f;
-          as[s] = in ? o.sd_j : 0.0f;
-          ep += in ? o.epol : 0.0f;
-          ee += in ? o.eel : 0.0f;
-          ev += in ? o.evdw : 0.0f;
+          sdi += o.sd_i;
+          as[s] = o.sd_j;
+          ep += o.epol;
+          ee += o.eel;
+          ev += o.evdw;
         }
         jx += reduce_to_lane(ax, g, lane);
         jy += reduce_to_lane(ay, g, lane);
