@@ -178,6 +178,86 @@ REAL_T xminC(INT_T *xyz_min, INT_T *minim_method, INT_T *maxiter,
              REAL_T *ftol_wolfe, REAL_T *gtol_wolfe, INT_T *return_flag,
              INT_T *label);
 
+/* Options of the LMOD low-mode search (src/sff/sff.h:86-113, the
+ * reference's layout and meaning): niter iterations over nmod low modes,
+ * kmod of them explored per iteration after the first nrotran_dof; nconf
+ * structures kept within energy_window of the lowest and
+ * conf_separation_rms apart; modes recomputed every eig_recalc iterations
+ * in a Krylov basis of ndim_arnoldi (+ nrotran_dof) vectors (0: all);
+ * restart from one of the n_best_struct best every lmod_restart
+ * iterations; mc_option 1 Metropolis at rtemp, 2 total, 3 quick quenching;
+ * steps between lmod_step_size_min and _max, nof_lmod_steps zig-zag steps
+ * (0: up to 20, stopping at a barrier), relaxed to lmod_relax_grms and
+ * minimised to minim_grms; nlig ligands moved every apply_rigdock
+ * iterations in nof_poses_to_try tries; random_seed (0: from the clock);
+ * print_level 0-5.  lmod_time, aux_time and error_flag are outputs. */
+typedef struct lmod_opt {
+  INT_T niter;
+  INT_T nmod;
+  INT_T kmod;
+  INT_T nrotran_dof;
+  INT_T nconf;
+  REAL_T minim_grms;
+  REAL_T energy_window;
+  REAL_T conf_separation_rms;
+  INT_T eig_recalc;
+  INT_T ndim_arnoldi;
+  INT_T lmod_restart;
+  INT_T n_best_struct;
+  INT_T mc_option;
+  REAL_T rtemp;
+  REAL_T lmod_step_size_min;
+  REAL_T lmod_step_size_max;
+  INT_T nof_lmod_steps;
+  REAL_T lmod_relax_grms;
+  INT_T nlig;
+  INT_T apply_rigdock;
+  INT_T nof_poses_to_try;
+  INT_T random_seed;
+  INT_T print_level;
+  REAL_T lmod_time;
+  REAL_T aux_time;
+  INT_T error_flag;
+} LMOD_OPT_T;
+
+/* Defaults of the LMOD and its minimiser's options (src/sff/sff.h:135,
+ * lmodC.c:3064). */
+INT_T lmod_opt_init(struct lmod_opt *lo, struct xmin_opt *xo);
+
+/* LMOD search driving mme() and xmin() (src/sff/sff.h:130-134,
+ * lmodC.c:3108): natm atoms from xyz (atoms whose gradient in grad is
+ * exactly zero stay fixed); conflib receives up to lo->nconf structures
+ * (3 natm each, lowest energy first), lmod_trajectory the niter + 1
+ * structures visited; lig_* / tr_* / rot_* describe the ligands (1-based
+ * atom numbers, translation in A, rotation in degrees).  Writes
+ * conflib.dat in the working directory and reads one left there.  Returns
+ * the lowest energy found, its structure in xyz; 0 with lo->error_flag < 0
+ * on an error. */
+REAL_T lmod(INT_T *natm, REAL_T *xyz, REAL_T *grad, REAL_T *energy,
+            REAL_T *conflib, REAL_T *lmod_trajectory, INT_T *lig_start,
+            INT_T *lig_end, INT_T *lig_cent, REAL_T *tr_min, REAL_T *tr_max,
+            REAL_T *rot_min, REAL_T *rot_max, struct xmin_opt *xo,
+            struct lmod_opt *lo);
+
+/* LMOD's reverse-communication form (lmodC.c:1686): call with *label = 0;
+ * while it returns *return_flag > 0, act on the request -- 1/2 energy and
+ * gradient with a new pair list, 3/4 with the old one, 5 minimise, 6 relax,
+ * 7 minimise the start structure, each at xyz_ext -- and call again with
+ * the *label it returned; *return_flag = 0 means done (*label < 0: an
+ * error). */
+REAL_T lmodC(INT_T *nlmodit, INT_T *nmod, INT_T *kmod, INT_T *rotran,
+             INT_T *natm_ext, REAL_T *xyz_ext, REAL_T *enrg, REAL_T *grad_ext,
+             INT_T *nconf, REAL_T *enrg_win, REAL_T *separ_rms,
+             REAL_T *conflib, REAL_T *trajectory, INT_T *arpk_recalc,
+             INT_T *arpk_dim, INT_T *lmod_restart, INT_T *topten,
+             INT_T *mc_option, REAL_T *rtemp, REAL_T *lmod_step_min,
+             REAL_T *lmod_step_max, INT_T *nof_lmod_step, INT_T *nligs,
+             INT_T *lig_start, INT_T *lig_end, INT_T *try_now, INT_T *ntry,
+             REAL_T *trmin, REAL_T *trmax, INT_T *lig_rot_cent,
+             REAL_T *angmin, REAL_T *angmax, INT_T *seed,
+             INT_T *print_level, REAL_T *lmod_time, REAL_T *extn_time,
+             INT_T *return_flag, INT_T *label);
+
 /* parm7 reader, writer and release (src/sff/sff.h:178-180, prm.c:584,
  * prm.c:1997, prm.c:2810). */
 PARMSTRUCT_T *rdparm(STRING_T *name);

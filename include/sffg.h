@@ -145,6 +145,26 @@ int sffg_batch_cg(sffg_batch *b, int maxiter, double rmsgrad, double dfpred, int
  * (sffg_batch_get_coords). */
 int sffg_batch_xmin(sffg_batch *b, const XMIN_OPT_T *xo, int *status, int *iters, double *energy, void *stream);
 
+/* LMOD over any energy function: the reference's lmod() driver
+ * (src/sff/lmodC.c:3108-3462, which hard-wires mme()) with func in mme()'s
+ * place, for its energies and for the xmin() minimisations.  Arguments and
+ * result as lmod() (include/sff.h).  No reference counterpart. */
+REAL_T sffg_lmod_func(REAL_T (*func)(REAL_T *, REAL_T *, INT_T *), INT_T *natm, REAL_T *xyz, REAL_T *grad,
+                      REAL_T *energy, REAL_T *conflib, REAL_T *lmod_trajectory, INT_T *lig_start, INT_T *lig_end,
+                      INT_T *lig_cent, REAL_T *tr_min, REAL_T *tr_max, REAL_T *rot_min, REAL_T *rot_max,
+                      XMIN_OPT_T *xo, LMOD_OPT_T *lo);
+
+/* The nev eigenpairs of smallest magnitude of a symmetric n x n operator
+ * (thick-restart Lanczos, the solver LMOD takes its low modes from, in place
+ * of the reference's ARPACK dsaupd/dseupd with which = "SM"): matvec(x, y,
+ * ctx) stores y = A x; nev < ncv <= n basis vectors, relative residual bound
+ * tol, at most max_restarts restarts.  values[nev] receives the converged
+ * eigenvalues in ascending order, vectors[nev * n] the eigenvectors one
+ * after another.  Returns the number converged, or -1. */
+int sffg_low_modes(int n, int nev, int ncv, double tol, int max_restarts,
+                   void (*matvec)(const double *x, double *y, void *ctx), void *ctx, double *values,
+                   double *vectors);
+
 /* Kernel launches issued by this batch since it was created. */
 long long sffg_batch_launch_count(const sffg_batch *b);
 /* With profiling on, the three pair passes of every evaluation are

@@ -25,8 +25,12 @@ NVCC_FLAGS = ["-O3", "-std=c++17", "-lineinfo", "-Xcompiler", "-fPIC", "-Xptxas"
 CXX_FLAGS = ["-O2", "-std=c++17", "-fPIC", "-Wall", "-Wno-unused-function"]
 # Host files whose arithmetic must match the reference's bit for bit on any
 # host: no floating-point contraction (FMA) and the C++20 coroutines the
-# minimiser is written with.
-CXX_FILE_FLAGS = {"xmin.cpp": ["-std=c++20", "-ffp-contract=off"]}
+# minimiser and the low-mode search are written with.
+CXX_FILE_FLAGS = {
+    "xmin.cpp": ["-std=c++20", "-ffp-contract=off"],
+    "lmod.cpp": ["-std=c++20", "-ffp-contract=off"],
+    "lowmodes.cpp": ["-ffp-contract=off"],
+}
 
 
 def library_path():

@@ -34,7 +34,6 @@
 // One minimisation runs at a time per process, as in the reference.
 #include <cfloat>
 #include <cmath>
-#include <coroutine>
 #include <cstdio>
 #include <cstring>
 #include <ctime>
@@ -42,9 +41,12 @@
 #include <memory>
 #include <vector>
 
+#include "coro.h"
 #include "sffg_internal.h"
 
 namespace {
+
+using sffg::Gen;
 
 // Request codes a run hands back (xminC.c:57-66): evaluate energy and
 // gradient, with a forced (4-6), prevented (7-9) or free (1-3) pair-list
@@ -63,46 +65,7 @@ inline double lo(double a, double b) { return a < b ? a : b; }
 inline double hi(double a, double b) { return a > b ? a : b; }
 inline double sq(double a) { return a * a; }
 
-// A resumable computation that yields request codes and ends with a status.
-struct Gen {
-  struct promise_type {
-    int request = 0, status = 0;
-    Gen get_return_object() { return Gen(std::coroutine_handle<promise_type>::from_promise(*this)); }
-    std::suspend_always initial_suspend() noexcept { return {}; }
-    std::suspend_always final_suspend() noexcept { return {}; }
-    std::suspend_always yield_value(int r) noexcept {
-      request = r;
-      return {};
-    }
-    void return_value(int s) noexcept { status = s; }
-    void unhandled_exception() { std::terminate(); }
-  };
-  explicit Gen(std::coroutine_handle<promise_type> h) : h_(h) {}
-  Gen(Gen &&o) noexcept : h_(o.h_) { o.h_ = nullptr; }
-  Gen(const Gen &) = delete;
-  ~Gen() {
-    if (h_) h_.destroy();
-  }
-  // Runs to the next request (true) or to the end (false).
-  bool next() {
-    h_.resume();
-    return !h_.done();
-  }
-  int request() const { return h_.promise().request; }
-  int status() const { return h_.promise().status; }
-
- private:
-  std::coroutine_handle<promise_type> h_;
-};
-
-// Passes every request of a sub-computation out and stores its status.
-#define XMIN_RUN(gen, status_out)                           \
-  {                                                         \
-    Gen sub_ = (gen);                                       \
-    while (sub_.next()) co_yield sub_.request();            \
-    (status_out) = sub_.status();                           \
-    (void)(status_out);                                     \
-  }
+#define XMIN_RUN CORO_RUN
 
 // Verbosity shared by all runs, as the reference's file-scope flags
 // (print_level 0: none; 1: every iteration; 2: also line-search and CG

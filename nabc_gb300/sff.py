@@ -63,6 +63,24 @@ class XMIN_OPT_T(C.Structure):
         ("ls_iter", C.c_int), ("print_level", C.c_int), ("error_flag", C.c_int),
     ]
 
+
+
+class LMOD_OPT_T(C.Structure):
+    """Same field order and types as the reference's struct lmod_opt
+    (src/sff/sff.h:86-113)."""
+
+    _fields_ = [
+        ("niter", C.c_int), ("nmod", C.c_int), ("kmod", C.c_int), ("nrotran_dof", C.c_int),
+        ("nconf", C.c_int), ("minim_grms", C.c_double), ("energy_window", C.c_double),
+        ("conf_separation_rms", C.c_double), ("eig_recalc", C.c_int), ("ndim_arnoldi", C.c_int),
+        ("lmod_restart", C.c_int), ("n_best_struct", C.c_int), ("mc_option", C.c_int),
+        ("rtemp", C.c_double), ("lmod_step_size_min", C.c_double), ("lmod_step_size_max", C.c_double),
+        ("nof_lmod_steps", C.c_int), ("lmod_relax_grms", C.c_double), ("nlig", C.c_int),
+        ("apply_rigdock", C.c_int), ("nof_poses_to_try", C.c_int), ("random_seed", C.c_int),
+        ("print_level", C.c_int), ("lmod_time", C.c_double), ("aux_time", C.c_double),
+        ("error_flag", C.c_int),
+    ]
+
 _lib = None
 
 
@@ -100,6 +118,17 @@ def lib():
                         REAL_P, INT_P, REAL_P, INT_P, INT_P, INT_P, INT_P, REAL_P, REAL_P, REAL_P,
                         REAL_P, REAL_P, REAL_P, INT_P, INT_P]
     L.xminC.restype = C.c_double
+    L.lmod_opt_init.argtypes = [C.POINTER(LMOD_OPT_T), C.POINTER(XMIN_OPT_T)]
+    L.lmod_opt_init.restype = C.c_int
+    lmod_args = [INT_P, REAL_P, REAL_P, REAL_P, REAL_P, REAL_P, INT_P, INT_P, INT_P, REAL_P, REAL_P,
+                 REAL_P, REAL_P, C.POINTER(XMIN_OPT_T), C.POINTER(LMOD_OPT_T)]
+    L.lmod.argtypes = lmod_args
+    L.lmod.restype = C.c_double
+    L.sffg_lmod_func.argtypes = [C.c_void_p] + lmod_args
+    L.sffg_lmod_func.restype = C.c_double
+    L.sffg_low_modes.argtypes = [C.c_int, C.c_int, C.c_int, C.c_double, C.c_int, C.c_void_p, C.c_void_p, REAL_P,
+                                 REAL_P]
+    L.sffg_low_modes.restype = C.c_int
     if hasattr(L, "mme_init_sff"):
         L.mme_init_sff.argtypes = [PRM_P, INT_P, INT_P, REAL_P, C.c_char_p]
         L.mme_init_sff.restype = C.c_int
@@ -166,6 +195,17 @@ def set_output(path):
     old = var.value
     var.value = fp
     return old
+
+
+def restore_output(previous):
+    """Close the file set_output opened and point nabout back at previous."""
+    libc = C.CDLL(None)
+    libc.fclose.argtypes = [C.c_void_p]
+    var = C.c_void_p.in_dll(lib(), "nabout")
+    fp = var.value
+    var.value = previous
+    if fp and fp != previous:
+        libc.fclose(fp)
 
 
 def flush_output():

@@ -21,6 +21,16 @@
  *                                     xmin(func) with print_level 10, func(x, g, -1),
  *                                     func = mme_rattle (rattle=1) or mme;
  *                                     trace.bin: every energy xmin asked for (f64)
+ *   lmod <niter> <nmod> <kmod> <mc_option> <nof_lmod_steps> <seed> <grms_tol>
+ *        <maxiter> <out.bin>        the reference's test/tlmod.c with these
+ *                                     options (print_level 2, xmin
+ *                                     ls_maxatmov 0.15, the first
+ *                                     minimisation to grms_tol in maxiter
+ *                                     steps); ARPACK replaced by
+ *                                     ref_shim/arpack_standin.cpp; run in an
+ *                                     empty directory (conflib.dat);
+ *                                     out.bin: natom, nconf (int32), the
+ *                                     return value (f64), x, conflib (f64)
  *
  * Coordinates come from a PDB (columns 31-54 of ATOM/HETATM records, the
  * order the prmtop uses) or an Amber ASCII restart read with getxv().
@@ -155,6 +165,40 @@ int main(int argc, char **argv)
     fp = fopen(argv[11], "wb");
     if (!fp) { perror(argv[11]); return 2; }
     fwrite(trace, sizeof(double), (size_t)(ntraced < 100000 ? ntraced : 100000), fp);
+    fclose(fp);
+    return 0;
+  }
+  if (strcmp(mode, "lmod") == 0) {
+    struct xmin_opt xo;
+    struct lmod_opt lo;
+    double *conflib, *traj, ret;
+    int none = 0;
+    double zero = 0.0;
+    FILE *fp;
+    lmod_opt_init(&lo, &xo);
+    lo.niter = atoi(argv[5]);
+    lo.nmod = atoi(argv[6]);
+    lo.kmod = atoi(argv[7]);
+    lo.mc_option = atoi(argv[8]);
+    lo.nof_lmod_steps = atoi(argv[9]);
+    lo.random_seed = atoi(argv[10]);
+    lo.print_level = 2;
+    xo.grms_tol = atof(argv[11]);
+    xo.maxiter = atoi(argv[12]);
+    xo.ls_maxatmov = 0.15;
+    conflib = calloc((size_t)n3 * (size_t)lo.nconf, sizeof(double));
+    traj = calloc((size_t)n3 * (size_t)(lo.niter + 1), sizeof(double));
+    iter = -1;
+    e = mme(x, g, &iter);
+    ret = lmod(&natom, x, g, &e, conflib, traj, &none, &none, &none, &zero, &zero, &zero, &zero, &xo, &lo);
+    printf("lmod returns %.17g error %d nconf %d\n", ret, lo.error_flag, lo.nconf);
+    fp = fopen(argv[13], "wb");
+    if (!fp) { perror(argv[13]); return 2; }
+    fwrite(&natom, sizeof(int), 1, fp);
+    fwrite(&lo.nconf, sizeof(int), 1, fp);
+    fwrite(&ret, sizeof(double), 1, fp);
+    fwrite(x, sizeof(double), (size_t)n3, fp);
+    fwrite(conflib, sizeof(double), (size_t)n3 * (size_t)lo.nconf, fp);
     fclose(fp);
     return 0;
   }

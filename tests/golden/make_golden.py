@@ -19,7 +19,10 @@ It produces
                 Langevin trajectories, XMIN minimisations of xfin (the
                 reference's test/txmin.c) and of the test functions of
                 oracle/xmin_funcs.c (oracle/_ref/xminref), each with every
-                function value XMIN asked for.
+                function value XMIN asked for, and LMOD searches on the
+                bead chain of oracle/xmin_funcs.c (oracle/_ref/lmodref: the
+                reference's lmodC.c with the ARPACK stand-in) -- final
+                structure, conflib, trajectory, conflib.dat and printout.
 """
 import json
 import os
@@ -36,6 +39,24 @@ sys.path.insert(0, ROOT)
 
 SFFREF = os.path.join(ROOT, "oracle", "_ref", "sffref")
 XMINREF = os.path.join(ROOT, "oracle", "_ref", "xminref")
+LMODREF = os.path.join(ROOT, "oracle", "_ref", "lmodref")
+
+# LMOD on the bead chain (oracle/xmin_funcs.c), the lmodref arguments
+# (ref_shim/lmod_driver.c): natom, frozen atom (-1: none), niter, nmod, kmod,
+# mc_option, nof_lmod_steps, eig_recalc, ndim_arnoldi, lmod_restart,
+# n_best_struct, energy_window, conf_separation_rms, nlig, lig_start,
+# lig_end, lig_cent, print_level, random_seed
+LMOD_CASES = [
+    ("metropolis", [14, -1, 6, 5, 3, 1, 0, 5, 0, 10, 10, 50.0, 2.0, 0, 0, 0, 0, 2, 314159]),
+    ("total_quench_restarted_krylov", [14, -1, 8, 5, 3, 2, 3, 2, 6, 3, 3, 50.0, 0.5, 0, 0, 0, 0, 2, 99]),
+    ("quick_quench_frozen", [14, 4, 8, 4, 2, 3, 0, 1, 0, 4, 2, 5.0, 0.5, 0, 0, 0, 0, 1, 7]),
+    ("docking_centroid", [14, -1, 6, 5, 3, 1, 0, 3, 0, 10, 10, 50.0, 0.5, 1, 11, 14, 0, 2, 314159]),
+    ("docking_atom_centre", [14, -1, 6, 5, 3, 2, 2, 3, 0, 10, 10, 50.0, 0.5, 1, 11, 14, 12, 2, 5]),
+    ("zigzag_movie", [14, -1, 2, 4, 2, 1, 2, 1, 0, 10, 10, 50.0, 0.5, 0, 0, 0, 0, 5, 11]),
+    ("quiet_long", [14, -1, 12, 5, 3, 1, 0, 5, 8, 4, 3, 20.0, 0.7, 0, 0, 0, 0, 0, 271]),
+]
+# run twice in one directory: the second search starts from conflib.dat
+LMOD_RESTART_CASE = ("conflib_restart", [14, -1, 4, 5, 3, 1, 0, 2, 0, 10, 10, 50.0, 0.5, 0, 0, 0, 0, 2, 42])
 
 # XMIN on the test functions of oracle/xmin_funcs.c: (function, method,
 # ls_method, numdiff, m_lbfgs, maxiter, grms_tol, ls_maxatmov)
@@ -342,6 +363,49 @@ def main():
         arrays[f"xmin{k}_g"] = rest[2 * ndim:3 * ndim]
         arrays[f"xmin{k}_trace"] = rest[3 * ndim:3 * ndim + ncalls]
     checks["xmin_functions"] = {"frozen_chain_atom": 4, "cases": xcases}
+    # LMOD on the bead chain (bit-for-bit cases)
+    lcases = []
+    for name, largs in LMOD_CASES + [LMOD_RESTART_CASE]:
+        work = os.path.join(HERE, "_lmod_tmp")
+        shutil.rmtree(work, ignore_errors=True)
+        os.makedirs(work)
+        runs = 2 if name == LMOD_RESTART_CASE[0] else 1
+        for _ in range(runs):
+            out = run([LMODREF] + [repr(a) if isinstance(a, float) else str(a) for a in largs] + ["out.bin"], cwd=work)
+        with open(os.path.join(work, "out.bin"), "rb") as f:
+            n, nconf, err, narn = np.frombuffer(f.read(16), np.int32)
+            ret, e = np.frombuffer(f.read(16), np.float64)
+            rest = np.frombuffer(f.read(), np.float64)
+        k = len(lcases)
+        d = 3 * int(n)
+        arrays[f"lmod{k}_scalars"] = np.array([ret, e])
+        arrays[f"lmod{k}_start"] = rest[:d]
+        arrays[f"lmod{k}_x"] = rest[d:2 * d]
+        arrays[f"lmod{k}_conflib"] = rest[2 * d:2 * d + d * int(nconf)]
+        arrays[f"lmod{k}_traj"] = rest[2 * d + d * int(nconf):]
+        with open(os.path.join(work, "conflib.dat"), "rb") as f:
+            arrays[f"lmod{k}_conflib_dat"] = np.frombuffer(f.read(), np.uint8)
+        lcases.append({"name": name, "args": largs, "runs": runs, "nconf": int(nconf), "error_flag": int(err),
+                       "ndim_arnoldi": int(narn), "log": out.split("lmod returns")[0]})
+        shutil.rmtree(work)
+    checks["lmod_chain"] = {"cases": lcases}
+    # LMOD through the reference's mme() on asp (GB 1): the test/tlmod.c
+    # driver with GB in place of its distance-dependent dielectric
+    work = os.path.join(HERE, "_lmod_tmp")
+    shutil.rmtree(work, ignore_errors=True)
+    os.makedirs(work)
+    opts = "ntpr=99999, gb=1, cut=99.0, rgbmax=99.0, nsnb=9999"
+    largs = [3, 5, 3, 2, 5, 99, 1e-4, 2000]
+    out = run([SFFREF, os.path.join(HERE, "ref", "asp.top"), os.path.join(HERE, "ref", "asp.pdb"), "lmod", opts] +
+              [str(a) for a in largs] + ["out.bin"], cwd=work)
+    m = re.search(r"lmod returns (\S+) error (-?\d+) nconf (\d+)", out)
+    iters = [float(v) for v in re.findall(r"^ +\d+ +E = +(-?[0-9.]+) \(", out, re.M)]
+    checks["lmod_asp"] = {"prmtop": "asp.top", "coords": "asp.pdb", "options": opts,
+                          "niter": 3, "nmod": 5, "kmod": 3, "mc_option": 2, "nof_lmod_steps": 5, "seed": 99,
+                          "grms_tol": 1e-4, "maxiter": 2000, "glob_min": float(m.group(1)),
+                          "error_flag": int(m.group(2)), "nconf": int(m.group(3)), "iteration_energies": iters,
+                          "log": out.split("lmod returns")[0]}
+    shutil.rmtree(work)
     os.remove(tmp)
     with open(os.path.join(HERE, "checks.json"), "w") as f:
         json.dump(checks, f, indent=1)
