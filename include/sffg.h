@@ -145,6 +145,23 @@ int sffg_batch_cg(sffg_batch *b, int maxiter, double rmsgrad, double dfpred, int
  * (sffg_batch_get_coords). */
 int sffg_batch_xmin(sffg_batch *b, const XMIN_OPT_T *xo, int *status, int *iters, double *energy, void *stream);
 
+/* LMOD searches on every system of the batch at once: each system runs the
+ * reference's search (lmod(), include/sff.h) with the options lo -- its
+ * minimisations by XMIN with xo, the tolerances set as lmod() sets them --
+ * and its own random stream seeded lo->random_seed + s; ligand moves
+ * (nlig), printout and conflib.dat are not used.  All systems' evaluations
+ * of a turn run as one pass over the batch.  status[s]: 0, a negative LMOD
+ * status, or -8 if the system's energy turned non-finite; glob_min[s] its
+ * lowest energy; nconf[s] the structures returned.  conflib (may be NULL)
+ * receives system s's structures, lowest first, at offset
+ * lo->nconf * 3 * (atom offset of s), room for lo->nconf * 3 * natom(s)
+ * doubles each.  Each system's lowest structure is left in the batch
+ * (sffg_batch_get_coords).  A one-system batch takes lmod()'s path bit for
+ * bit; in a larger batch pair-list rebuilds one search asks for change the
+ * others' FP32 rounding.  No reference counterpart. */
+int sffg_batch_lmod(sffg_batch *b, const LMOD_OPT_T *lo, const XMIN_OPT_T *xo, int *status, double *glob_min,
+                    int *nconf, double *conflib, void *stream);
+
 /* LMOD over any energy function: the reference's lmod() driver
  * (src/sff/lmodC.c:3108-3462, which hard-wires mme()) with func in mme()'s
  * place, for its energies and for the xmin() minimisations.  Arguments and

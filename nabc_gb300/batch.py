@@ -127,6 +127,34 @@ class Batch:
         _check(L.sffg_batch_xmin(self.h, C.byref(xo), sff.iptr(st), sff.iptr(it), sff.dptr(en), stream), "xmin")
         return st, it, en
 
+    def lmod(self, xmin_opts=None, stream=None, **opts):
+        """LMOD searches on every system (sffg_batch_lmod); opts set fields
+        of LMOD_OPT_T over lmod_opt_init's defaults (niter, nmod, kmod,
+        mc_option, random_seed, ...), xmin_opts fields of the XMIN_OPT_T the
+        minimisations use.  Returns (status, lowest energy, number of
+        structures, conflib) per system, conflib[s] an (nconf, natom, 3)
+        array; the lowest structures stay in the batch."""
+        L = sff.lib()
+        lo, xo = sff.LMOD_OPT_T(), sff.XMIN_OPT_T()
+        L.lmod_opt_init(C.byref(lo), C.byref(xo))
+        for k, v in opts.items():
+            setattr(lo, k, v)
+        for k, v in (xmin_opts or {}).items():
+            setattr(xo, k, v)
+        n = len(self.natoms)
+        st = np.zeros(n, np.int32)
+        gm = np.zeros(n)
+        nc = np.zeros(n, np.int32)
+        flat = np.zeros(3 * int(np.sum(self.natoms)) * lo.nconf)
+        _check(L.sffg_batch_lmod(self.h, C.byref(lo), C.byref(xo), sff.iptr(st), sff.dptr(gm), sff.iptr(nc),
+                                 sff.dptr(flat), stream), "lmod")
+        out, off = [], 0
+        for s, na in enumerate(self.natoms):
+            blk = flat[3 * off * lo.nconf:3 * (off + na) * lo.nconf].reshape(lo.nconf, na, 3)
+            out.append(blk[:nc[s]].copy())
+            off += na
+        return st, gm, nc, out
+
     def md_begin(self, stream=None):
         _check(sff.lib().sffg_batch_md_begin(self.h, stream), "md_begin")
 

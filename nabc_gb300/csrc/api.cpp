@@ -153,6 +153,21 @@ extern "C" int sffg_batch_xmin(sffg_batch *b, const XMIN_OPT_T *xo, int *status,
   return SFFG_OK;
 }
 
+extern "C" int sffg_batch_lmod(sffg_batch *b, const LMOD_OPT_T *lo, const XMIN_OPT_T *xo, int *status,
+                               double *glob_min, int *nconf, double *conflib, void *stream) {
+  if (!b || !lo || !xo) return fail(SFFG_EINVAL, "null batch or options");
+  std::vector<int> st, nc;
+  std::vector<double> gm;
+  const int rc = b->impl->lmod(*lo, *xo, st, gm, nc, conflib, stream);
+  if (rc) return pass(b->impl, rc);
+  for (size_t s = 0; s < st.size(); s++) {
+    if (status) status[s] = st[s];
+    if (glob_min) glob_min[s] = gm[s];
+    if (nconf) nconf[s] = nc[s];
+  }
+  return SFFG_OK;
+}
+
 extern "C" int sffg_batch_md_begin(sffg_batch *b, void *stream) {
   SFFG_WRAP(b->impl->md_begin(false, nullptr, nullptr, stream));
 }

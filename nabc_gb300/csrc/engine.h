@@ -108,6 +108,10 @@ class Batch {
   // count and final energy per system.
   int xmin(const XMIN_OPT_T &xo, std::vector<int> &status, std::vector<int> &iters, std::vector<double> &energy,
            void *stream);
+  // LMOD searches on every system (csrc/batch_lmod.cpp); conflib: per
+  // system lo.nconf structures at lo.nconf * 3 * atom offset (may be null)
+  int lmod(const LMOD_OPT_T &lo, const XMIN_OPT_T &xo, std::vector<int> &status, std::vector<double> &glob_min,
+           std::vector<int> &nconf, double *conflib, void *stream);
 
   // One energy+gradient evaluation of every active system.  rebuild
   // requests a pair-list rebuild first (always done on the first call).

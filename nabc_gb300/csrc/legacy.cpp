@@ -51,52 +51,7 @@ void check(int rc, const char *what) {
   }
 }
 
-// ------------------------------------------------ the reference's RNG
-// L'Ecuyer combined generator with Bays-Durham shuffle and polar
-// Box-Muller Gaussians, as published in src/sff/rand2.c:51-128, with the
-// same process-global state and default seed (-1).
-struct Rand2 {
-  int seed3 = -1, seed2 = 0, iy = 0, iv[32] = {0};
-  double uniform() {
-    const int IM1 = 2147483563, IM2 = 2147483399, IA1 = 40014, IA2 = 40692, IQ1 = 53668, IQ2 = 52774,
-              IR1 = 12211, IR2 = 3791, NTAB = 32, IMM1 = IM1 - 1, NDIV = 1 + IMM1 / NTAB;
-    const double AM = 1.0 / IM1, RNMX = 1.0 - 1.2e-13;
-    int k;
-    if (seed3 <= 0) {
-      seed3 = (-seed3 < 1) ? 1 : -seed3;
-      seed2 = seed3;
-      for (int j = NTAB + 7; j >= 0; j--) {
-        k = seed3 / IQ1;
-        seed3 = IA1 * (seed3 - k * IQ1) - k * IR1;
-        if (seed3 < 0) seed3 += IM1;
-        if (j < NTAB) iv[j] = seed3;
-      }
-      iy = iv[0];
-    }
-    k = seed3 / IQ1;
-    seed3 = IA1 * (seed3 - k * IQ1) - k * IR1;
-    if (seed3 < 0) seed3 += IM1;
-    k = seed2 / IQ2;
-    seed2 = IA2 * (seed2 - k * IQ2) - k * IR2;
-    if (seed2 < 0) seed2 += IM2;
-    const int j = iy / NDIV;
-    iy = iv[j] - seed2;
-    iv[j] = seed3;
-    if (iy < 1) iy += IMM1;
-    const double t = AM * iy;
-    return t > RNMX ? RNMX : t;
-  }
-  double gauss(double mean, double sd) {
-    double s1, s2, rsq;
-    do {
-      s1 = 2. * uniform() - 1.;
-      s2 = 2. * uniform() - 1.;
-      rsq = s1 * s1 + s2 * s2;
-    } while (rsq >= 1. || rsq == 0.0);
-    return sd * (s1 * std::sqrt(-2. * std::log(rsq) / rsq)) + mean;
-  }
-};
-
+// the reference's RNG (Rand2, sffg_internal.h): one process-global stream
 Rand2 &rng() {
   static Rand2 r;
   return r;

@@ -239,10 +239,11 @@ class Archive {
     return ok;
   }
 
-  // One of the nmax lowest structures, chosen by one rand2() draw.
-  void restart(int ndim, int nmax, double *xyz) const {
+  // One of the nmax lowest structures, chosen by one uniform draw.
+  template <class Draw>
+  void restart(int ndim, int nmax, double *xyz, Draw draw) const {
     if (e.empty()) return;
-    const int nrand = 1 + static_cast<int>(nmax * rand2());
+    const int nrand = 1 + static_cast<int>(nmax * draw());
     size_t n = 0;
     for (const Entry &x : e) {
       std::memcpy(xyz, x.xyz.data(), ndim * sizeof(double));
@@ -406,6 +407,11 @@ class Search {
   double hess_eps = 2.2204460492503131e-16;  // relative gradient precision for the Hessian products
   double glob_min = 0.0;
   clock_t lmod_stamp = 0, extn_stamp = 0;
+  // a search of its own stream (batched searches) or the process-global
+  // rand2() stream (lmod(), lmodC(), as the reference)
+  sffg::Rand2 *own_rng = nullptr;
+  // conflib.dat read at the start and written as the reference does
+  bool use_files = true;
 
   Gen run() {
     const int pl = *a.print_level;
@@ -443,10 +449,13 @@ class Search {
       seed3 = -static_cast<int>(tv.tv_sec ^ tv.tv_usec);
       if (seed3 == 0) seed3 = -1;
     }
-    setseed(&seed3);
+    if (own_rng)
+      own_rng->seed3 = seed3;
+    else
+      setseed(&seed3);
 
     // a conflib.dat from an earlier search seeds this one
-    if (FILE *f = std::fopen("conflib.dat", "rb")) {
+    if (FILE *f = use_files ? std::fopen("conflib.dat", "rb") : nullptr) {
       std::fclose(f);
       std::fprintf(out, "\n*****  W A R N I N G  *****\n\n");
       std::fprintf(out, "It appears that results from a previous LMOD search were found\n");
@@ -457,7 +466,7 @@ class Search {
       std::fprintf(out, "If conflib.dat is incompatible with the current search, *KILL*\n");
       std::fprintf(out, "this LMOD job, remove conflib.dat, and restart LMOD.\n\n");
       if (!arch_.read_and_sort("conflib.dat", next_)) co_return kFileError;
-      arch_.restart(next_, 1, a.xyz_ext);
+      arch_.restart(next_, 1, a.xyz_ext, [this] { return draw(); });
       gather_x();
     }
     // minimise the start structure
@@ -533,7 +542,7 @@ class Search {
         std::fflush(out);
       }
       // a random sign for each mode of the mixed mode
-      for (int i = 0; i < ncm; i++) sign[i] = rand2() < 0.5 ? 1 : -1;
+      for (int i = 0; i < ncm; i++) sign[i] = draw() < 0.5 ? 1 : -1;
       const int rotran = *a.rotran, kmod = *a.kmod;
       double min_energy = kBig;
       int kk = 0, cnt = 0;
@@ -542,7 +551,7 @@ class Search {
         // kmod of the modes at random, then the mixed mode
         if (cnt == kmod) k = ncm;
         if (kmod < (ncm - rotran) && (kmod - cnt) < (ncm - k) &&
-            rand2() >= (static_cast<double>(kmod) / static_cast<double>(ncm - rotran)))
+            draw() >= (static_cast<double>(kmod) / static_cast<double>(ncm - rotran)))
           continue;
         cnt++;
         for (int i = 0; i < nd_; i++) {
@@ -569,7 +578,7 @@ class Search {
             if (s > max_atmov) max_atmov = s;
           }
           max_atmov = std::sqrt(max_atmov);
-          const double step = *a.lmod_step_min + (*a.lmod_step_max - *a.lmod_step_min) * rand2();
+          const double step = *a.lmod_step_min + (*a.lmod_step_max - *a.lmod_step_min) * draw();
           const double scale = step / max_atmov;
           double energy_old = ref_energy, rms_old = 0.0;
           int zz;
@@ -637,8 +646,8 @@ class Search {
       if (!quenched && *a.mc_option == kMetropolis) {
         int tries = 0;
         do {
-          n = static_cast<int>(kk * rand2());
-        } while (rand2() > pboltz[n] && ++tries < kMaxMcTry);
+          n = static_cast<int>(kk * draw());
+        } while (draw() > pboltz[n] && ++tries < kMaxMcTry);
       }
       for (int i = 0; i < nd_; i++) x_[i] = cent[i] + moves[static_cast<size_t>(n) * nd_ + i];
       scatter_x();
@@ -647,7 +656,7 @@ class Search {
       // prune and save the archive; restart from one of its best
       if ((it % *a.lmod_restart == *a.lmod_restart - 1) || (it % kConflibUpdate == kConflibUpdate - 1)) {
         size = arch_.update(next_, nd_, *a.enrg_win, *a.separ_rms);
-        if (!arch_.write("conflib.dat", next_)) co_return kFileError;
+        if (use_files && !arch_.write("conflib.dat", next_)) co_return kFileError;
         if (print_) {
           std::fprintf(out, "__________________________________________________\n");
           std::fprintf(out, " Top Ten:\n");
@@ -662,7 +671,7 @@ class Search {
           std::fflush(out);
         }
         if (it % *a.lmod_restart == *a.lmod_restart - 1) {
-          arch_.restart(next_, std::min(*a.topten, size), a.xyz_ext);
+          arch_.restart(next_, std::min(*a.topten, size), a.xyz_ext, [this] { return draw(); });
           gather_x();
         }
       }
@@ -675,11 +684,11 @@ class Search {
           for (int l = 0; l < *a.nligs; l++) {
             double tx, ty, tz, tn;
             do {
-              tx = 2 * rand2() - 1;
-              ty = 2 * rand2() - 1;
-              tz = 2 * rand2() - 1;
+              tx = 2 * draw() - 1;
+              ty = 2 * draw() - 1;
+              tz = 2 * draw() - 1;
             } while ((tn = std::sqrt(sq(tx) + sq(ty) + sq(tz))) < kTiny);
-            const double ts = a.trmin[l] + (a.trmax[l] - a.trmin[l]) * rand2();
+            const double ts = a.trmin[l] + (a.trmax[l] - a.trmin[l]) * draw();
             tx *= ts / tn;
             ty *= ts / tn;
             tz *= ts / tn;
@@ -692,14 +701,14 @@ class Search {
             }
             double rx, ry, rz, rn;
             do {
-              rx = 2 * rand2() - 1;
-              ry = 2 * rand2() - 1;
-              rz = 2 * rand2() - 1;
+              rx = 2 * draw() - 1;
+              ry = 2 * draw() - 1;
+              rz = 2 * draw() - 1;
             } while ((rn = std::sqrt(sq(rx) + sq(ry) + sq(rz))) < kTiny);
             rx /= rn;
             ry /= rn;
             rz /= rn;
-            const double ang = a.angmin[l] + (a.angmax[l] - a.angmin[l]) * rand2();
+            const double ang = a.angmin[l] + (a.angmax[l] - a.angmin[l]) * draw();
             double m[3][3];
             rot_matrix((kPi / 180.) * ang, rx, ry, rz, m);
             double c[3] = {0.0, 0.0, 0.0};
@@ -738,7 +747,7 @@ class Search {
     }
     // final pruning; the archive goes to conflib.dat and conflib[]
     size = arch_.update(next_, nd_, *a.enrg_win, *a.separ_rms);
-    if (!arch_.write("conflib.dat", next_)) co_return kFileError;
+    if (use_files && !arch_.write("conflib.dat", next_)) co_return kFileError;
     if (print_ || debug_) {
       std::fprintf(out, "__________________________________________________\n");
       std::fprintf(out, debug_ ? " Full list:\n" : " Top Ten:\n");
@@ -783,6 +792,7 @@ class Search {
   }
 
  private:
+  double draw() { return own_rng ? own_rng->uniform() : rand2(); }
   void gather_x() {
     for (int i = 0; i < natm_; i++)
       for (int k = 0; k < 3; k++) x_[3 * i + k] = a.xyz_ext[3 * idx_[i] + k];
@@ -832,6 +842,59 @@ Active &active() {
 double g_next_hess_eps = 2.2204460492503131e-16;
 
 }  // namespace
+
+namespace sffg {
+
+struct LmodJob::Impl {
+  LMOD_OPT_T lo{};
+  int natm = 0, zero_i = 0, return_flag = 0;
+  double zero_d = 0.0, lmod_time = 0.0, extn_time = 0.0;
+  Rand2 rng;
+  Search search;
+  std::unique_ptr<Gen> gen;
+  int step() {
+    if (gen->next()) return gen->request() / 16;
+    const int status = gen->status();
+    gen.reset();
+    return status;
+  }
+};
+
+LmodJob::LmodJob() : impl_(new Impl) {}
+LmodJob::~LmodJob() = default;
+
+int LmodJob::start(const LMOD_OPT_T &lo, int natm, double *xyz, double *grad, double *energy, double *conflib,
+                   double *trajectory, int seed, double hess_eps) {
+  Impl &m = *impl_;
+  m.lo = lo;
+  m.lo.print_level = 0;
+  m.lo.nlig = 0;
+  m.lo.random_seed = seed;
+  m.natm = natm;
+  LMOD_OPT_T &o = m.lo;
+  m.search.a = Args{&o.niter, &o.nmod, &o.kmod, &o.nrotran_dof, &m.natm, xyz, energy, grad, &o.nconf,
+                    &o.energy_window, &o.conf_separation_rms, conflib, trajectory, &o.eig_recalc,
+                    &o.ndim_arnoldi, &o.lmod_restart, &o.n_best_struct, &o.mc_option, &o.rtemp,
+                    &o.lmod_step_size_min, &o.lmod_step_size_max, &o.nof_lmod_steps, &o.nlig, &m.zero_i,
+                    &m.zero_i, &o.apply_rigdock, &o.nof_poses_to_try, &m.zero_d, &m.zero_d, &m.zero_i, &m.zero_d,
+                    &m.zero_d, &o.random_seed, &o.print_level, &m.lmod_time, &m.extn_time, &m.return_flag};
+  if (!check_params(m.search.a)) return kParamsError;
+  m.search.own_rng = &m.rng;
+  m.search.use_files = false;
+  m.search.hess_eps = hess_eps;
+  m.gen.reset(new Gen(m.search.run()));
+  return m.step();
+}
+
+int LmodJob::resume() {
+  if (!impl_->gen) return -2;
+  return impl_->step();
+}
+
+double LmodJob::glob_min() const { return impl_->search.glob_min; }
+int LmodJob::nconf() const { return impl_->lo.nconf; }
+
+}  // namespace sffg
 
 extern "C" {
 

@@ -3,6 +3,7 @@
 // include/sffg.h).
 #pragma once
 
+#include <cmath>
 #include <cstdint>
 #include <cstdio>
 #include <memory>
@@ -92,6 +93,75 @@ class XminJob {
   std::unique_ptr<Impl> impl_;
   int iter_ = 0, ls_iter_ = 0;
   double grms_ = 0.0, time_ = 0.0;
+};
+
+// ------------------------------------------------ the reference's RNG
+// L'Ecuyer combined generator with Bays-Durham shuffle and polar
+// Box-Muller Gaussians, as published in src/sff/rand2.c:51-128, with the
+// same default seed (-1).  md(), rand2() and lmod() share one process-
+// global stream as in the reference; batched LMOD searches own one each.
+struct Rand2 {
+  int seed3 = -1, seed2 = 0, iy = 0, iv[32] = {0};
+  double uniform() {
+    const int IM1 = 2147483563, IM2 = 2147483399, IA1 = 40014, IA2 = 40692, IQ1 = 53668, IQ2 = 52774,
+              IR1 = 12211, IR2 = 3791, NTAB = 32, IMM1 = IM1 - 1, NDIV = 1 + IMM1 / NTAB;
+    const double AM = 1.0 / IM1, RNMX = 1.0 - 1.2e-13;
+    int k;
+    if (seed3 <= 0) {
+      seed3 = (-seed3 < 1) ? 1 : -seed3;
+      seed2 = seed3;
+      for (int j = NTAB + 7; j >= 0; j--) {
+        k = seed3 / IQ1;
+        seed3 = IA1 * (seed3 - k * IQ1) - k * IR1;
+        if (seed3 < 0) seed3 += IM1;
+        if (j < NTAB) iv[j] = seed3;
+      }
+      iy = iv[0];
+    }
+    k = seed3 / IQ1;
+    seed3 = IA1 * (seed3 - k * IQ1) - k * IR1;
+    if (seed3 < 0) seed3 += IM1;
+    k = seed2 / IQ2;
+    seed2 = IA2 * (seed2 - k * IQ2) - k * IR2;
+    if (seed2 < 0) seed2 += IM2;
+    const int j = iy / NDIV;
+    iy = iv[j] - seed2;
+    iv[j] = seed3;
+    if (iy < 1) iy += IMM1;
+    const double t = AM * iy;
+    return t > RNMX ? RNMX : t;
+  }
+  double gauss(double mean, double sd) {
+    double s1, s2, rsq;
+    do {
+      s1 = 2. * uniform() - 1.;
+      s2 = 2. * uniform() - 1.;
+      rsq = s1 * s1 + s2 * s2;
+    } while (rsq >= 1. || rsq == 0.0);
+    return sd * (s1 * std::sqrt(-2. * std::log(rsq) / rsq)) + mean;
+  }
+};
+
+// One LMOD search driven by its caller (the batched searches of
+// sffg_batch_lmod): lmodC()'s search with its own random stream, no printout
+// and no conflib.dat.  start() and resume() return the next request -- 1-7,
+// lmodC()'s return_flag codes, acted on at xyz/grad/energy, which the
+// caller updates in place before resuming -- or, when the search ends, 0 or
+// a negative status.  conflib holds nconf * 3 natm, trajectory
+// (niter + 1) * 3 natm doubles.
+class LmodJob {
+ public:
+  LmodJob();
+  ~LmodJob();
+  int start(const LMOD_OPT_T &lo, int natm, double *xyz, double *grad, double *energy, double *conflib,
+            double *trajectory, int seed, double hess_eps);
+  int resume();
+  double glob_min() const;
+  int nconf() const;
+
+ private:
+  struct Impl;
+  std::unique_ptr<Impl> impl_;
 };
 
 // ---------------------------------------------------------------- model

@@ -70,9 +70,11 @@ inline double sq(double a) { return a * a; }
 // Verbosity shared by all runs, as the reference's file-scope flags
 // (print_level 0: none; 1: every iteration; 2: also line-search and CG
 // details; n > 2: every n-th iteration).
-int g_print = 0;
-bool g_debug = false;
-int g_nfunc = 0;  // evaluations made by xmin() in the current call
+// (per thread: batched runs start and resume on the host's worker threads,
+// always quietly)
+thread_local int g_print = 0;
+thread_local bool g_debug = false;
+thread_local int g_nfunc = 0;  // evaluations made by xmin() in the current call
 
 struct Pair {
   double rho = 0.0, gamma = 0.0;

@@ -163,6 +163,8 @@ def lib():
         L.sffg_batch_md.argtypes = [vp, C.c_int, vp]
         L.sffg_batch_cg.argtypes = [vp, C.c_int, C.c_double, C.c_double, INT_P, REAL_P, vp]
         L.sffg_batch_xmin.argtypes = [vp, C.POINTER(XMIN_OPT_T), INT_P, INT_P, REAL_P, vp]
+        L.sffg_batch_lmod.argtypes = [vp, C.POINTER(LMOD_OPT_T), C.POINTER(XMIN_OPT_T), INT_P, REAL_P, INT_P,
+                                      REAL_P, vp]
         L.sffg_batch_status.argtypes = [vp, INT_P, vp]
         L.sffg_checked_code.argtypes = []
         L.sffg_checked_code.restype = C.c_int
