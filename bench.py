@@ -231,6 +231,63 @@ def bench_batched(args, stream, sp, flush):
     res["xmin_conformer_iterations_per_s"] = float(np.sum(it)) / xs
     res["xmin_seconds"] = xs
     out["conformers"] = res
+
+    # LMOD searches: small molecules, each searched by the reference's
+    # low-mode algorithm; batched (sffg_batch_lmod) against lmod() one
+    # molecule after another (timed on a sample, per search)
+    if args.lmod_systems > 0:
+        import tempfile
+        sizes = np.full(args.lmod_systems, 60)
+        lm_mols = make_molecules(sizes, 31000)
+        lopts = dict(niter=2, nmod=3, kmod=2, mc_option=2, nof_lmod_steps=2, random_seed=11)
+        xopts = dict(grms_tol=0.05, maxiter=200, ls_maxatmov=0.15)
+        bl = Batch(CONFORMER_OPTS)
+        for prm_l, x_l, _ in lm_mols:
+            bl.add(prm_l, x_l)
+        bl.finalize()
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        st, gm, nc, _ = bl.lmod(xmin_opts=xopts, **lopts)
+        tb = time.perf_counter() - t0
+        bl.close()
+        L = sff.lib()
+        nplain = min(2, len(lm_mols))
+        t_plain = 0.0
+        with tempfile.TemporaryDirectory() as d:
+            cwd = os.getcwd()
+            os.chdir(d)
+            try:
+                for prm_l, x_l, _ in lm_mols[:nplain]:
+                    session = sff.Session(prm_l, CONFORMER_OPTS)
+                    na = sff.natom(prm_l)
+                    xl = x_l.copy()
+                    gl = np.zeros(3 * na)
+                    it = C.c_int(-1)
+                    t1 = time.perf_counter()
+                    e = C.c_double(L.mme(sff.dptr(xl), sff.dptr(gl), C.byref(it)))
+                    lo, xo = sff.LMOD_OPT_T(), sff.XMIN_OPT_T()
+                    L.lmod_opt_init(C.byref(lo), C.byref(xo))
+                    for k, v in lopts.items():
+                        setattr(lo, k, v)
+                    for k, v in xopts.items():
+                        setattr(xo, k, v)
+                    conf = np.zeros(3 * na * lo.nconf)
+                    traj = np.zeros(3 * na * (lo.niter + 1))
+                    zi, zd, nn = C.c_int(0), C.c_double(0.0), C.c_int(na)
+                    L.lmod(C.byref(nn), sff.dptr(xl), sff.dptr(gl), C.byref(e), sff.dptr(conf), sff.dptr(traj),
+                           C.byref(zi), C.byref(zi), C.byref(zi), C.byref(zd), C.byref(zd), C.byref(zd),
+                           C.byref(zd), C.byref(xo), C.byref(lo))
+                    t_plain += time.perf_counter() - t1
+                    os.remove("conflib.dat")
+                    del session
+            finally:
+                os.chdir(cwd)
+        out["lmod"] = {"systems": len(lm_mols), "atoms_each": 60, "options": CONFORMER_OPTS,
+                       "lmod_options": lopts, "xmin_options": xopts,
+                       "all_ok": bool(np.all(st == 0)),
+                       "batched_searches_per_s": len(lm_mols) / tb, "batched_seconds": tb,
+                       "plain_searches_per_s": nplain / t_plain, "plain_sample": nplain,
+                       "speedup": (len(lm_mols) / tb) / (nplain / t_plain)}
     return out
 
 
@@ -328,6 +385,7 @@ def main():
     ap.add_argument("--conformers", type=int, default=512, help="conformers in the conformer batch")
     ap.add_argument("--cg-steps", type=int, default=200, help="batched conjgrad steps on the conformers")
     ap.add_argument("--xmin-iters", type=int, default=50, help="batched L-BFGS iterations on the conformers")
+    ap.add_argument("--lmod-systems", type=int, default=32, help="molecules in the batched LMOD search (0: skip)")
     ap.add_argument("--no-batched", action="store_true", help="skip the batched-versus-plain measurements")
     ap.add_argument("--no-tune", action="store_true",
                     help="default work split instead of the autotuned one (for profiler runs, whose timing the "

@@ -155,7 +155,10 @@ int Batch::lmod(const LMOD_OPT_T &lo, const XMIN_OPT_T &xo_in, std::vector<int> 
         advance(s, y.search.resume());
       }
     };
-    const int nthr = std::min<int>(std::max(1u, std::thread::hardware_concurrency()), (nsys + 1) / 2);
+    // host threads pay for themselves only on large systems: a thread is
+    // started per turn, about the cost of resuming 10,000 atoms' minimiser
+    const int nthr = std::min<int>(std::min<int>(std::max(1u, std::thread::hardware_concurrency()), (nsys + 1) / 2),
+                                   std::max(1, natom_total_ / 10000));
     if (nthr <= 1) {
       resume_range(0, nsys);
     } else {

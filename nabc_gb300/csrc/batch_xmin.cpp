@@ -106,7 +106,10 @@ int Batch::xmin(const XMIN_OPT_T &xo_in, std::vector<int> &status, std::vector<i
         settle(s, jobs[s].resume(ene[13 * s], g.data() + o, x.data() + o, &request[s]));
       }
     };
-    const int nthr = std::min<int>(std::max(1u, std::thread::hardware_concurrency()), (nsys + 3) / 4);
+    // host threads pay for themselves only on large systems: a thread is
+    // started per turn, about the cost of resuming 10,000 atoms' minimiser
+    const int nthr = std::min<int>(std::min<int>(std::max(1u, std::thread::hardware_concurrency()), (nsys + 3) / 4),
+                                   std::max(1, natom_total_ / 10000));
     if (nthr <= 1) {
       resume_range(0, nsys);
     } else {
