@@ -40,7 +40,8 @@ int Batch::lmod(const LMOD_OPT_T &lo, const XMIN_OPT_T &xo_in, std::vector<int> 
   }
   const int nsys = num_systems();
   const size_t n3 = 3 * static_cast<size_t>(natom_total_);
-  std::vector<double> x(n3), g(n3), ene, energy(nsys, 0.0);
+  HostDoubles x(n3), g(n3);
+  std::vector<double> ene, energy(nsys, 0.0);
   for (int s = 0; s < nsys; s++) {
     int rc = get_coords(s, x.data() + 3 * static_cast<size_t>(sys_[s].atom_off), stream);
     if (rc) return rc;
@@ -131,8 +132,7 @@ int Batch::lmod(const LMOD_OPT_T &lo, const XMIN_OPT_T &xo_in, std::vector<int> 
     if ((rc = set_all_active(on, stream))) return rc;
     if ((rc = set_all_coords(x.data(), stream))) return rc;
     if ((rc = eval(rebuild, stream))) return rc;
-    if ((rc = get_all_energy_grad(ene, g.data(), stream))) return rc;
-    if ((rc = system_status(health, stream))) return rc;
+    if ((rc = get_all_energy_grad(ene, g.data(), stream, &health))) return rc;
     auto resume_range = [&](int s0, int s1) {
       for (int s = s0; s < s1; s++) {
         Sys &y = sys[s];

@@ -41,7 +41,8 @@ int Batch::xmin(const XMIN_OPT_T &xo_in, std::vector<int> &status, std::vector<i
   const int nsys = num_systems();
   XMIN_OPT_T xo = xo_in;
   xo.print_level = 0;  // no per-system progress lines
-  std::vector<double> x(3 * static_cast<size_t>(natom_total_)), g(x.size()), ene;
+  HostDoubles x(3 * static_cast<size_t>(natom_total_)), g(3 * static_cast<size_t>(natom_total_));
+  std::vector<double> ene;
   for (int s = 0; s < nsys; s++) {
     int rc = get_coords(s, x.data() + 3 * static_cast<size_t>(sys_[s].atom_off), stream);
     if (rc) return rc;
@@ -88,8 +89,7 @@ int Batch::xmin(const XMIN_OPT_T &xo_in, std::vector<int> &status, std::vector<i
     if ((rc = set_all_active(on, stream))) return rc;
     if ((rc = set_all_coords(x.data(), stream))) return rc;
     if ((rc = eval(rebuild, stream))) return rc;
-    if ((rc = get_all_energy_grad(ene, g.data(), stream))) return rc;
-    if ((rc = system_status(health, stream))) return rc;
+    if ((rc = get_all_energy_grad(ene, g.data(), stream, &health))) return rc;
     // the minimisers are independent: resume them on the host's cores
     // (each system's arithmetic is the same on any thread)
     auto resume_range = [&](int s0, int s1) {

@@ -778,16 +778,23 @@ int Batch::set_all_active(const std::vector<int> &on, void *stream) {
   return SFFG_OK;
 }
 
-int Batch::get_all_energy_grad(std::vector<double> &out, double *grad, void *stream) {
+int Batch::get_all_energy_grad(std::vector<double> &out, double *grad, void *stream, std::vector<int> *status) {
   if (!finalized_) return SFFG_ESTATE;
   const int nsys = num_systems();
   std::vector<long long> e(kEnergySlots * static_cast<size_t>(nsys));
+  std::vector<int> bad(status ? nsys : 0);
   cudaStream_t st = pick(*d_, stream);
   SFFG_CK(cudaMemcpyAsync(grad, d_->grad.p, 3 * sizeof(double) * natom_total_, cudaMemcpyDeviceToHost, st));
   SFFG_CK(cudaMemcpyAsync(e.data(), d_->energy.p, e.size() * sizeof(long long), cudaMemcpyDeviceToHost, st));
+  if (status)
+    SFFG_CK(cudaMemcpyAsync(bad.data(), d_->nonfinite.p, nsys * sizeof(int), cudaMemcpyDeviceToHost, st));
   SFFG_CK(cudaStreamSynchronize(st));
   out.resize(13 * static_cast<size_t>(nsys));
   for (int s = 0; s < nsys; s++) ene_from_fixed(&e[kEnergySlots * s], &out[13 * s]);
+  if (status) {
+    status->resize(nsys);
+    for (int s = 0; s < nsys; s++) (*status)[s] = bad[s] ? SFFG_ENONFINITE : SFFG_OK;
+  }
   return SFFG_OK;
 }
 

@@ -23,6 +23,34 @@
 namespace sffg {
 
 struct DeviceState;  // defined in engine.cu
+
+// Page-locked host doubles for the per-turn coordinate uploads and gradient
+// reads of the batched minimisers (pageable copies go through a staging
+// buffer); falls back to pageable memory if pinning fails.
+class HostDoubles {
+ public:
+  explicit HostDoubles(size_t n) : n_(n) {
+    if (cudaMallocHost(reinterpret_cast<void **>(&p_), n * sizeof(double) + 8) != cudaSuccess) {
+      (void)cudaGetLastError();
+      p_ = nullptr;
+      fallback_.assign(n, 0.0);
+    } else {
+      for (size_t i = 0; i < n; i++) p_[i] = 0.0;
+    }
+  }
+  ~HostDoubles() {
+    if (p_) cudaFreeHost(p_);
+  }
+  HostDoubles(const HostDoubles &) = delete;
+  HostDoubles &operator=(const HostDoubles &) = delete;
+  double *data() { return p_ ? p_ : fallback_.data(); }
+  size_t size() const { return n_; }
+
+ private:
+  double *p_ = nullptr;
+  size_t n_;
+  std::vector<double> fallback_;
+};
 struct ListArgs;     // defined in lists.cuh
 
 // State of one system's conjugate-gradient run (the locals of the
@@ -103,7 +131,9 @@ class Batch {
   int save_state(const char *path, void *stream);
   int load_state(const char *path, void *stream);
   int set_all_active(const std::vector<int> &on, void *stream);
-  int get_all_energy_grad(std::vector<double> &ene13, double *grad, void *stream);
+  // status (optional): each system's non-finite flag, read with the same wait
+  int get_all_energy_grad(std::vector<double> &ene13, double *grad, void *stream,
+                          std::vector<int> *status = nullptr);
   // XMIN on every system at once (csrc/batch_xmin.cpp): status, iteration
   // count and final energy per system.
   int xmin(const XMIN_OPT_T &xo, std::vector<int> &status, std::vector<int> &iters, std::vector<double> &energy,
