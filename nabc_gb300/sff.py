@@ -126,6 +126,7 @@ def lib():
     L.lmod.restype = C.c_double
     L.sffg_lmod_func.argtypes = [C.c_void_p] + lmod_args
     L.sffg_lmod_func.restype = C.c_double
+    L.lmodC.restype = C.c_double  # 38 pointer arguments, passed as given
     L.sffg_low_modes.argtypes = [C.c_int, C.c_int, C.c_int, C.c_double, C.c_int, C.c_void_p, C.c_void_p, REAL_P,
                                  REAL_P]
     L.sffg_low_modes.restype = C.c_int

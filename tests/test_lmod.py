@@ -161,3 +161,77 @@ def test_low_modes_against_dense_eigensolver(lib, n, nev, ncv):
         assert np.linalg.norm(A @ v - lam * v) <= 2 * tol * max(abs(lam), 2.31e-11) + 1e-12 * np.abs(ev).max()
     if ncv == n:
         assert len(products) == n  # one sweep spans the space
+
+
+def test_lmodC_reverse_communication(lib, funcs, checks, refrun, tmp_path, monkeypatch):
+    """lmodC() driven directly, with the reference's lmod() driver loop
+    (lmodC.c:3366-3462) written out here over the chain function and this
+    library's xmin(): the first golden search again, bit for bit, and the
+    reference's labels (2-7 while running, 0 at the end)."""
+    monkeypatch.chdir(tmp_path)
+    case = checks["lmod_chain"]["cases"][0]
+    (n, frozen, niter, nmod, kmod, mc, nsteps, recalc, narn, restart, nbest, window, sep, nlig, ls, le, lc, pl,
+     seed) = case["args"]
+    F = funcs
+    C.c_int.in_dll(F, "xf_natom").value = n
+    fr = (C.c_int * 64).in_dll(F, "xf_frozen")
+    for i in range(64):
+        fr[i] = 0
+    lo, xo = sff.LMOD_OPT_T(), sff.XMIN_OPT_T()
+    lib.lmod_opt_init(C.byref(lo), C.byref(xo))
+    lo.niter, lo.nmod, lo.kmod, lo.mc_option = niter, nmod, kmod, mc
+    lo.nof_lmod_steps, lo.eig_recalc, lo.ndim_arnoldi = nsteps, recalc, narn
+    lo.lmod_restart, lo.n_best_struct = restart, nbest
+    lo.energy_window, lo.conf_separation_rms = window, sep
+    lo.random_seed = seed
+    lo.apply_rigdock, lo.nof_poses_to_try = 2, 3
+    xo.ls_maxatmov = 0.15
+    fn = C.cast(F.xf_chain, C.c_void_p)
+    raw = sff.FUNC_T(fn.value)
+    x = refrun["lmod0_start"].copy()
+    g = np.zeros_like(x)
+    conflib = np.zeros(3 * n * lo.nconf)
+    traj = np.zeros(3 * n * (niter + 1))
+    it = C.c_int(0)
+    e = C.c_double(raw(sff.dptr(x), sff.dptr(g), C.byref(it)))
+    nn = C.c_int(n)
+    zi = C.c_int(0)
+    zd = C.c_double(0.0)
+    rf, label = C.c_int(0), C.c_int(0)
+    grms = C.c_double(0.0)
+    labels = set()
+    for _ in range(100000):
+        ret = lib.lmodC(C.byref(lo, type(lo).niter.offset), C.byref(lo, type(lo).nmod.offset),
+                        C.byref(lo, type(lo).kmod.offset), C.byref(lo, type(lo).nrotran_dof.offset), C.byref(nn),
+                        sff.dptr(x), C.byref(e), sff.dptr(g), C.byref(lo, type(lo).nconf.offset),
+                        C.byref(lo, type(lo).energy_window.offset), C.byref(lo, type(lo).conf_separation_rms.offset),
+                        sff.dptr(conflib), sff.dptr(traj), C.byref(lo, type(lo).eig_recalc.offset),
+                        C.byref(lo, type(lo).ndim_arnoldi.offset), C.byref(lo, type(lo).lmod_restart.offset),
+                        C.byref(lo, type(lo).n_best_struct.offset), C.byref(lo, type(lo).mc_option.offset),
+                        C.byref(lo, type(lo).rtemp.offset), C.byref(lo, type(lo).lmod_step_size_min.offset),
+                        C.byref(lo, type(lo).lmod_step_size_max.offset), C.byref(lo, type(lo).nof_lmod_steps.offset),
+                        C.byref(lo, type(lo).nlig.offset), C.byref(zi), C.byref(zi),
+                        C.byref(lo, type(lo).apply_rigdock.offset), C.byref(lo, type(lo).nof_poses_to_try.offset),
+                        C.byref(zd), C.byref(zd), C.byref(zi), C.byref(zd), C.byref(zd),
+                        C.byref(lo, type(lo).random_seed.offset), C.byref(lo, type(lo).print_level.offset),
+                        C.byref(lo, type(lo).lmod_time.offset), C.byref(lo, type(lo).aux_time.offset), C.byref(rf),
+                        C.byref(label))
+        if rf.value == 0:
+            break
+        labels.add(label.value)
+        if rf.value in (1, 2, 3, 4):
+            it.value = -4 if rf.value <= 2 else -2
+            e.value = raw(sff.dptr(x), sff.dptr(g), C.byref(it))
+        else:
+            if rf.value == 5:
+                xo.grms_tol = lo.minim_grms
+            elif rf.value == 6:
+                xo.grms_tol = lo.lmod_relax_grms
+            ev = np.array([e.value])
+            e.value = lib.xmin(fn, C.byref(nn), sff.dptr(x), sff.dptr(g), sff.dptr(ev), C.byref(grms), C.byref(xo))
+    assert label.value == 0 and rf.value == 0
+    assert labels == {2, 3, 4, 5, 6}  # 7: the ligand minimisations, not used here
+    assert ret == refrun["lmod0_scalars"][0]
+    np.testing.assert_array_equal(x, refrun["lmod0_x"])
+    np.testing.assert_array_equal(conflib[:3 * n * lo.nconf], refrun["lmod0_conflib"])
+    np.testing.assert_array_equal(traj, refrun["lmod0_traj"])
