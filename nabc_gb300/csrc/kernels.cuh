@@ -653,7 +653,9 @@ __global__ void __launch_bounds__(256, 3) k_chain(const DevTables t) {
         const float r2 = fmaf(dx, dx, fmaf(dy, dy, dz * dz));
         const bool in = ((__float_as_uint(gp.x) >> lane) & 1u) && r2 <= t.born.cutoff2;
         if (!__any_sync(kFull, in)) continue;
-        const float dij1i = rsqrt_nr(r2);
+        // the hardware rsqrt alone: pass 3 only shapes the forces, whose RMS
+        // error against FP64 it leaves at 4.70e-6 (to 3 digits) for -2% time
+        const float dij1i = rsqrt_fast(r2);
         const float dij = r2 * dij1i;
         float di, dj;
         descreen_pair<true>(t.born, in, dij, dij1i, si, gp.y, di, dj);
