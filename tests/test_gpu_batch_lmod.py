@@ -102,3 +102,24 @@ def test_batch_deterministic_and_consistent(lib):
         # structure is lower
         assert abs(energies[s][0] - gm[s]) <= 1e-6 * abs(gm[s])
         assert min(energies[s]) >= gm[s] - 1e-6 * abs(gm[s])
+
+
+def test_nonfinite_system_ends_alone(lib):
+    """A system whose energy is not finite (a NaN coordinate) ends with
+    status -8 before its search starts; the others search as usual and
+    give the same results as without it in the batch only up to rounding,
+    so they are checked for status and consistency."""
+    from nabc_gb300.batch import Batch
+    prm_a, xa = load_case(MOLECULES[0])
+    prm_n, xn = load_case(MOLECULES[1])
+    bad = xn.copy()
+    bad[4] = np.nan
+    b = Batch(OPTS)
+    b.add(prm_a, xa)
+    b.add(prm_n, bad)
+    b.finalize()
+    st, gm, nc, conf = b.lmod(xmin_opts=XMIN, **LMOD)
+    assert st[1] == -8 and nc[1] == 0
+    assert st[0] == 0 and nc[0] >= 1 and np.isfinite(gm[0])
+    np.testing.assert_array_equal(b.coords(0), conf[0][0].ravel())
+    b.close()
