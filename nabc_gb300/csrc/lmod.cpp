@@ -913,6 +913,9 @@ REAL_T lmodC(INT_T *nlmodit, INT_T *nmod, INT_T *kmod, INT_T *rotran, INT_T *nat
                   trmax,      lig_rot_cent, angmin,     angmax,        seed,          print_level,   lmod_time,
                   extn_time,  return_flag};
   if (*label == 0) {
+    // the step for this search only, whether or not it starts
+    const double hess_eps = g_next_hess_eps;
+    g_next_hess_eps = 2.2204460492503131e-16;
     *lmod_time = 0.0;
     *extn_time = 0.0;
     act.gen.reset();
@@ -923,8 +926,7 @@ REAL_T lmodC(INT_T *nlmodit, INT_T *nmod, INT_T *kmod, INT_T *rotran, INT_T *nat
     }
     act.search.reset(new Search);
     act.search->a = args;
-    act.search->hess_eps = g_next_hess_eps;
-    g_next_hess_eps = 2.2204460492503131e-16;
+    act.search->hess_eps = hess_eps;
     act.search->lmod_stamp = clock();
     act.gen.reset(new Gen(act.search->run()));
   } else {
