@@ -235,3 +235,18 @@ def test_lmodC_reverse_communication(lib, funcs, checks, refrun, tmp_path, monke
     np.testing.assert_array_equal(x, refrun["lmod0_x"])
     np.testing.assert_array_equal(conflib[:3 * n * lo.nconf], refrun["lmod0_conflib"])
     np.testing.assert_array_equal(traj, refrun["lmod0_traj"])
+
+
+def test_low_modes_rejects_inconsistent_sizes(lib):
+    """nev < ncv <= n is required (ARPACK's dsaupd rule); anything else
+    returns -1 without calling the operator."""
+    calls = []
+
+    @C.CFUNCTYPE(None, C.POINTER(C.c_double), C.POINTER(C.c_double), C.c_void_p)
+    def matvec(xp, yp, ctx):
+        calls.append(1)
+
+    vals, vecs = np.zeros(8), np.zeros(64)
+    for n, nev, ncv in ((8, 4, 4), (8, 0, 4), (8, 4, 9), (0, 1, 2)):
+        assert lib.sffg_low_modes(n, nev, ncv, 1e-4, 10, matvec, None, sff.dptr(vals), sff.dptr(vecs)) == -1
+    assert not calls
