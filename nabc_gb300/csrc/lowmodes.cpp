@@ -134,7 +134,7 @@ int LowModes::init(int n, int nev, int ncv, double tol, int max_restarts) {
   h_.assign(2 * static_cast<size_t>(ncv), 0.0);
   val_.clear();
   vec_.clear();
-  j_ = kept_ = restarts_ = products_ = nconv_ = 0;
+  j_ = restarts_ = products_ = nconv_ = 0;
   state_ = 0;
   rng_ = 0x2545F4914F6CDD1DULL;
   return 0;
@@ -172,7 +172,7 @@ void LowModes::orthogonalise(double *w, int ncols, double *h) {
 int LowModes::iterate() {
   if (state_ == 0) {
     random_unit(V_.data());
-    j_ = kept_ = 0;
+    j_ = 0;
     state_ = 1;
   } else if (state_ == 1) {
     // column j_'s product is in y_: extend the basis
@@ -289,7 +289,6 @@ int LowModes::finish_sweep() {
   orthogonalise(next, keep, h_.data());
   const double s = std::sqrt(dot(n_, next, next));
   for (int t = 0; t < n_; t++) next[t] /= s;
-  kept_ = keep;
   j_ = keep;
   restarts_++;
   return 1;

@@ -60,7 +60,7 @@ class LowModes {
   int n_ = 0, nev_ = 0, ncv_ = 0, max_restarts_ = 0;
   double tol_ = 0.0;
   std::vector<double> V_, H_, x_, y_, r_, h_, val_, vec_;
-  int j_ = 0, kept_ = 0, restarts_ = 0, products_ = 0, nconv_ = 0, state_ = 0;
+  int j_ = 0, restarts_ = 0, products_ = 0, nconv_ = 0, state_ = 0;
   unsigned long long rng_ = 0;
 };
 
