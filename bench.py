@@ -16,8 +16,13 @@ evaluation plus the integrator update, device-resident.
           the md rate)
   reference arm (--impl reference): the same workload on the host CPU
           cores through the FP64 CPU restatement of the reference's egb()/
-          mme(), all cores (the reference itself does not build on the
-          Arm GPU host without its source tree)
+          mme() (oracle/sffo.c), with its input made by oracle/synth.c, the
+          restatement of the library's generator: that process loads no
+          library of the product (the reference itself cannot be built on
+          the GPU host, which has no copy of its source tree)
+
+Both arms print the same "config": the workload, its options, the
+generator's realised radius and density and the pair counts.
 
 Multi-GPU (--gpus N under torchrun): independent replicas (the path has
 no data exchange between systems), value = total evaluations/s; scaling
@@ -40,17 +45,24 @@ ROOT = os.path.dirname(os.path.abspath(__file__))
 sys.path.insert(0, ROOT)
 
 METRIC = "GB energy+force evals/s & pairs/s, batched vs plain at fixed err; p50/p99 ms"
-WORKLOAD = "single 25,000-atom synthetic molecule, gb=5 (OBC II), rgbmax 15, cut 25, Langevin MD dt 2 fs"
+WORKLOAD = "single {natom:,}-atom synthetic molecule, gb=5 (OBC II), rgbmax 15, cut 25, Langevin MD dt 2 fs"
 OPTS = "gb=5, rgbmax=15.0, cut=25.0, nsnb=10, dt=0.002, gamma_ln=5.0, temp0=300.0, kappa=0.0"
 # Algorithmic work per unordered in-list pair (FP32 flops counted FADD/FMUL
 # = 1, FFMA = 2) for the three passes, from the reference formulas at
 # kappa = 0 with the far-field Born branch.
 FLOPS_PASS = (36.0, 60.0, 62.0)
+# MUFU (special-function unit) operations per unordered in-list pair of each
+# pass (reciprocal square roots and the exponential of the GB kernel).
+MUFU_PASS = (1.0, 4.0, 1.0)
 # DRAM bytes (read + write) per launch of each pass on this workload, from
 # one ncu capture (dram__bytes_read.sum + dram__bytes_write.sum): the inputs
 # (~1.6 MB of per-atom data, the lists) stay in L2, so traffic is far below
 # what the FP32 work would allow.
 TRAFFIC_PASS = (6.77e6, 17.87e6, 7.28e6)
+PASS_NAMES = ("k_born (pass 1, Born radii)", "k_gbpair (pass 2, GB+Coulomb+LJ)", "k_chain (pass 3, chain rule)")
+# Per SM and clock: FP32 lanes (an FFMA counts 2 flops) and MUFU results.
+FP32_LANES_PER_SM, MUFU_PER_SM = 128, 16
+CUT, RGBMAX, NSNB = 25.0, 15.0, 10
 
 
 def rank_info():
@@ -186,16 +198,23 @@ def bench_batched(args, stream, sp, flush):
     sizes = np.floor(np.exp(rng.uniform(np.log(200), np.log(20000), args.uneven))).astype(int)
     mols = make_molecules(sizes, 9000)
     b, plain, res = compare(UNEVEN_OPTS, [(prm, x) for prm, x, _ in mols], 3, "uneven")
-    # accuracy of three of the smaller molecules against the FP64 oracle
+    # accuracy of the smallest, the median and the largest molecule against
+    # the FP64 oracle
     errs = []
-    for k in np.argsort(sizes)[:: max(1, len(sizes) // 3)][:3]:
+    order = np.argsort(sizes)
+    checked = [int(order[0]), int(order[len(order) // 2]), int(order[-1])]
+    for k in checked:
         prm, x, _ = mols[k]
         o = oracle.Oracle(prm, UNEVEN_OPTS)
         e0, _, g0, _ = o.mme(x)
         errs.append((abs(b.energy(int(k))[0] - e0) / abs(e0), float(np.sqrt(((b.grad(int(k)) - g0) ** 2).mean()))))
     res["energy_rel_max"] = max(e for e, _ in errs)
     res["force_rms_max"] = max(f for _, f in errs)
-    res["checked_vs_fp64"] = "3 molecules of the batch"
+    res["checked_vs_fp64"] = {"atoms": [int(sizes[k]) for k in checked],
+                              "which": "smallest, median and largest molecule of the batch"}
+    res["pairs_in_cut"] = int(sum(b.num_pairs(k) for k in range(len(sizes))))
+    res["batched_pairs_per_s"] = res["pairs_in_cut"] * res["batched_evals_per_s"] / len(sizes)
+    res["plain_pairs_per_s"] = res["pairs_in_cut"] * res["plain_evals_per_s"] / len(sizes)
     b.close()
     for p in plain:
         p.close()
@@ -230,6 +249,13 @@ def bench_batched(args, stream, sp, flush):
     res["xmin_lbfgs_iterations"] = args.xmin_iters
     res["xmin_conformer_iterations_per_s"] = float(np.sum(it)) / xs
     res["xmin_seconds"] = xs
+    # per-conformer outcome: XMIN's status (0 ended normally: converged or
+    # the iteration limit; negative: an error such as y.s = 0)
+    codes, counts = np.unique(np.asarray(st), return_counts=True)
+    res["xmin_status_counts"] = {str(int(c)): int(k) for c, k in zip(codes, counts)}
+    res["xmin_converged"] = int(np.sum((np.asarray(st) == 0) & (np.asarray(it) < args.xmin_iters)))
+    res["xmin_at_iteration_limit"] = int(np.sum((np.asarray(st) == 0) & (np.asarray(it) >= args.xmin_iters)))
+    res["xmin_errored"] = int(np.sum(np.asarray(st) != 0))
     out["conformers"] = res
 
     # LMOD searches: small molecules, each searched by the reference's
@@ -344,32 +370,153 @@ def bench_serving(args):
 
 
 def count_pairs(x, cut, rcut_gb):
-    """Unordered pairs within cut and within rgbmax + Fsmax (cell grid)."""
+    """Unordered pairs within cut and within rgbmax + Fsmax (k-d tree)."""
     from scipy.spatial import cKDTree
     t = cKDTree(x.reshape(-1, 3))
     return int(t.count_neighbors(t, cut) - len(x) // 3) // 2, int(t.count_neighbors(t, rcut_gb) - len(x) // 3) // 2
 
 
-def make_system(natom, seed):
-    from nabc_gb300 import sff
-    prm, x, radius = sff.synth_molecule(natom, seed)
-    return prm, x, radius
+def cpu_model():
+    """The host CPU's model name."""
+    try:
+        out = subprocess.run(["lscpu"], capture_output=True, text=True, timeout=10).stdout
+        for line in out.splitlines():
+            if line.startswith("Model name:"):
+                return line.split(":", 1)[1].strip()
+    except (OSError, subprocess.SubprocessError):
+        pass
+    try:
+        with open("/proc/cpuinfo") as f:
+            for line in f:
+                if line.lower().startswith(("model name", "cpu model")):
+                    return line.split(":", 1)[1].strip()
+    except OSError:
+        pass
+    return "unknown"
 
 
-def run_cpu_reference(args, natom, seed, steps, warmup):
-    """The reference algorithm on the host cores (FP64 oracle port, OpenMP
-    over all cores): evaluations per second, list rebuilt every nsnb."""
+def workload(natom, seed, world):
+    """(config, molecule): the workload's description, the same in both
+    arms, from oracle/synth.c's molecule (the library generator's molecule
+    bit for bit, made without loading the library)."""
     from oracle import oracle
     oracle.build()
-    prm, x, radius = make_system(natom, seed)
-    o = oracle.Oracle(prm, OPTS)
-    for k in range(warmup):
-        o.mme(x, rebuild=(k == 0))
+    m = oracle.SynthMolecule(natom, seed)
+    npairs, npairs_gb = count_pairs(m.x, CUT, RGBMAX + m.fsmax)
+    cfg = {"workload": WORKLOAD.format(natom=natom), "natom": natom, "seed": seed, "options": OPTS,
+           "generator": "compact self-avoiding chain (bond 1.53 A, angle 111 deg, no non-bonded atom within "
+                        "2.5 A), C/N/O/H 0.32/0.09/0.09/0.50, charges N(0, 0.4^2) neutralised",
+           "specified_density_per_A3": 0.09,
+           "realised_radius_A": m.radius,
+           "realised_density_per_A3": natom / (4.0 / 3.0 * math.pi * m.radius ** 3),
+           "pairs_in_cut": npairs, "pairs_in_rgbmax_fsmax": npairs_gb,
+           "l2": "inputs (~1.6 MB per-atom data + lists) fit L2; a 256 MiB buffer is written between timed "
+                 "GPU steps (outside the timed events)",
+           "parallelism": f"{world} independent replica(s), one per GPU"}
+    return cfg, m
+
+
+def time_oracle(o, x, n):
+    """Seconds for n oracle evaluations at the nsnb cadence (the pair list
+    rebuilt on the first and every tenth)."""
     t0 = time.perf_counter()
-    for k in range(steps):
-        o.mme(x, rebuild=(k % 10 == 0))
-    dt = time.perf_counter() - t0
-    return steps / dt, dt, o
+    for k in range(n):
+        o.mme(x, rebuild=(k % NSNB == 0))
+    return time.perf_counter() - t0
+
+
+def cpu_baseline(m, cores, n_all, n_warm=1):
+    """The FP64 restatement of the reference's egb()/mme34() on this host:
+    n_all evaluations on all threads, and the 1-thread rate from one
+    evaluation with a list rebuild and two without, weighted to the
+    cadence of one rebuild per nsnb evaluations."""
+    from oracle import oracle
+    o = oracle.Oracle(m, OPTS)
+    oracle.set_threads(cores)
+    for _ in range(n_warm):
+        o.mme(m.x)
+    dt_all = time_oracle(o, m.x, n_all)
+    oracle.set_threads(1)
+    t0 = time.perf_counter()
+    o.mme(m.x, rebuild=True)
+    t_rebuild = time.perf_counter() - t0
+    t0 = time.perf_counter()
+    o.mme(m.x, rebuild=False)
+    o.mme(m.x, rebuild=False)
+    t_eval = (time.perf_counter() - t0) / 2
+    oracle.set_threads(cores)
+    o.close()
+    return {"value": n_all / dt_all, "unit": "evals/s", "cores": cores, "kind": "port",
+            "sample": f"{n_all} mme() evaluations of the workload, pair list rebuilt every {NSNB} "
+                      "(FP64 CPU restatement of the reference egb()/mme34() in oracle/sffo.c, OpenMP, "
+                      "brute-force pair list)",
+            "cpu_model": cpu_model(), "nproc": os.cpu_count(),
+            "one_thread_value": NSNB / (t_rebuild + (NSNB - 1) * t_eval),
+            "one_thread_sample": "1 thread: one evaluation with a list rebuild and two without, weighted "
+                                 f"1:{NSNB - 1}"}
+
+
+C1_OPTS = "gb=1, cut=999.0, rgbmax=15.0, dt=0.001, gamma_ln=5.0, temp0=300.0, tempi=0.0"
+
+
+def bench_small_md(args, stream, sp, cores):
+    """The small all-pairs case: 2,000 atoms, gb=1 (HCT), cut 999, one
+    mme() then 1,000 Langevin md() steps at dt 1 fs, 300 K, gamma 5/ps, from
+    zero velocities; on the GPU (device-resident batch md, CUDA events) and
+    through the FP64 restatement on all host cores (the full run)."""
+    import torch
+    from nabc_gb300 import sff
+    from nabc_gb300.batch import Batch
+    from oracle import oracle
+    n, seed, nsteps = 2000, 2000, args.c1_steps
+    prm, x, _ = sff.synth_molecule(n, seed)
+    b = Batch(C1_OPTS)
+    b.add(prm, x)
+    b.finalize()
+    e0, e1, e2 = (torch.cuda.Event(enable_timing=True) for _ in range(3))
+    torch.cuda.synchronize()
+    e0.record(stream)
+    b.eval(rebuild=True, stream=sp)
+    e1.record(stream)
+    b.md_begin(stream=sp)
+    b.md_steps(0, nsteps, stream=sp)
+    e2.record(stream)
+    torch.cuda.synchronize()
+    sp_ms, md_ms = e0.elapsed_time(e1), e1.elapsed_time(e2)
+    b.close()
+    sff.free_prm(prm)
+    m = oracle.SynthMolecule(n, seed)
+    o = oracle.Oracle(m, C1_OPTS + ", ntpr_md=1000000")
+    oracle.set_threads(cores)
+    t0 = time.perf_counter()
+    o.mme(m.x)
+    cpu_sp = time.perf_counter() - t0
+    t0 = time.perf_counter()
+    o.md(m.x, np.zeros_like(m.x), nsteps)
+    cpu_md = time.perf_counter() - t0
+    o.close()
+    return {"natom": n, "options": C1_OPTS, "md_steps": nsteps,
+            "gpu_single_point_ms": sp_ms, "gpu_md_ms": md_ms, "gpu_md_steps_per_s": nsteps / (md_ms * 1e-3),
+            "gpu_ns_per_day": nsteps * 0.001e-3 / (md_ms * 1e-3) * 86400,
+            "cpu_single_point_ms": cpu_sp * 1e3, "cpu_md_s": cpu_md, "cpu_md_steps_per_s": nsteps / cpu_md,
+            "cpu_cores": cores, "cpu_kind": "port (FP64 restatement, OpenMP)",
+            "gpu_over_cpu_md": (nsteps / (md_ms * 1e-3)) / (nsteps / cpu_md)}
+
+
+def reference_arm(args, cores):
+    """--impl reference: the workload through the FP64 CPU restatement on
+    all host cores, with its 1-thread rate; rank 0 only."""
+    os.environ.setdefault("OMP_NUM_THREADS", str(cores))
+    steps, warmup = max(1, args.steps), max(0, args.warmup)
+    cfg, m = workload(args.natom, args.seed, args.gpus)
+    cb = cpu_baseline(m, cores, steps, n_warm=warmup)
+    rate = cb["value"]
+    line = {"metric": METRIC, "value": rate, "unit": "evals/s", "n_gpus": args.gpus, "steps": steps,
+            "warmup": warmup, "ms_per_step": 1e3 / rate, "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+            "impl": "reference", "config": cfg, "cpu_baseline": cb,
+            "e2e": {"value": rate, "unit": "evals/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+    print(json.dumps(line))
 
 
 def main():
@@ -380,8 +527,10 @@ def main():
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
     ap.add_argument("--natom", type=int, default=25000)
     ap.add_argument("--seed", type=int, default=2025)
-    ap.add_argument("--cpu-sample", type=int, default=6, help="evaluations in the CPU-baseline sample")
-    ap.add_argument("--uneven", type=int, default=512, help="molecules in the uneven-size batch (2048: full size)")
+    ap.add_argument("--cpu-sample", type=int, default=10, help="evaluations in the CPU-baseline sample")
+    ap.add_argument("--md-long", type=int, default=10000, help="steps of the long md run (ns/day)")
+    ap.add_argument("--c1-steps", type=int, default=1000, help="md steps of the 2,000-atom all-pairs case")
+    ap.add_argument("--uneven", type=int, default=2048, help="molecules in the uneven-size batch")
     ap.add_argument("--conformers", type=int, default=512, help="conformers in the conformer batch")
     ap.add_argument("--cg-steps", type=int, default=200, help="batched conjgrad steps on the conformers")
     ap.add_argument("--xmin-iters", type=int, default=50, help="batched L-BFGS iterations on the conformers")
@@ -399,23 +548,8 @@ def main():
     cores = os.cpu_count() or 1
 
     if args.impl == "reference":
-        if rank != 0:
-            return
-        os.environ.setdefault("OMP_NUM_THREADS", str(cores))
-        # one step is one evaluation of the workload (~0.1 s on 16 Arm cores),
-        # so the requested steps and warm-up run in full within minutes
-        steps, warmup = max(1, args.steps), max(0, args.warmup)
-        rate, dt, o = run_cpu_reference(args, args.natom, args.seed, steps, warmup)
-        line = {"metric": METRIC, "value": rate, "unit": "evals/s", "n_gpus": args.gpus, "steps": steps,
-                "warmup": warmup, "ms_per_step": 1e3 * dt / steps, "higher_is_better": True,
-                "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
-                "impl": "reference",
-                "config": {"workload": WORKLOAD, "natom": args.natom, "options": OPTS},
-                "cpu_baseline": {"value": rate, "unit": "evals/s", "cores": cores, "kind": "port",
-                                 "sample": f"{steps} mme() evaluations of the workload (FP64 CPU restatement of "
-                                           "the reference egb()/mme34(), OpenMP over all host cores)"},
-                "e2e": {"value": rate, "unit": "evals/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
-        print(json.dumps(line))
+        if rank == 0:
+            reference_arm(args, cores)
         return
 
     import torch
@@ -429,10 +563,13 @@ def main():
     sff.lib()
     sff.set_output(os.devnull)
     seed = args.seed + rank  # each replica its own molecule
-    prm, x, radius = make_system(args.natom, seed)
+    cfg, mol = workload(args.natom, seed, world)
+    prm, x, _ = sff.synth_molecule(args.natom, seed)
+    assert np.array_equal(x, mol.x), "library and oracle generators disagree"
     n = args.natom
-    cut, rgbmax = 25.0, 15.0
-    npairs, npairs_gb = count_pairs(x, cut, rgbmax + prm.contents.Fsmax)
+    npairs, npairs_gb = cfg["pairs_in_cut"], cfg["pairs_in_rgbmax_fsmax"]
+    props = torch.cuda.get_device_properties(local)
+    nsm = props.multi_processor_count
 
     opts = OPTS + (", sffg_tune=0" if args.no_tune else "")
     b = Batch(opts)
@@ -449,12 +586,12 @@ def main():
     err = None
     if rank == 0:
         from oracle import oracle
-        oracle.build()
         b.eval(rebuild=True, stream=sp)
         torch.cuda.synchronize()
         e_gpu, g_gpu = b.energy(0), b.grad(0)
-        o = oracle.Oracle(prm, OPTS)
+        o = oracle.Oracle(mol, OPTS)
         e0, ene0, g0, _ = o.mme(x)
+        o.close()
         err = {"energy_rel": abs(e_gpu[0] - e0) / abs(e0), "force_rms": float(np.sqrt(((g_gpu - g0) ** 2).mean())),
                "oracle": "FP64 CPU restatement of egb()/mme34()"}
 
@@ -495,6 +632,21 @@ def main():
     pass_ms, nev = b.kernel_times()
     b.set_profiling(False)
 
+    # the long md run: md_long steps back to back (one call), ns/day
+    md_long = None
+    if args.md_long > 0:
+        a0, a1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        torch.cuda.synchronize()
+        a0.record(stream)
+        b.md_steps(step, args.md_long, stream=sp)
+        a1.record(stream)
+        torch.cuda.synchronize()
+        step += args.md_long
+        long_ms = a0.elapsed_time(a1)
+        md_long = {"steps": args.md_long, "dt_fs": 2.0, "seconds": long_ms * 1e-3,
+                   "steps_per_s": args.md_long / (long_ms * 1e-3),
+                   "ns_per_day": args.md_long * 2e-6 / (long_ms * 1e-3) * 86400}
+
     # e2e through the reference-facing C ABI with pinned host buffers
     L = sff.lib()
     L.sffg_options_reset()
@@ -530,20 +682,30 @@ def main():
         return
 
     clocks = clk.summary()
-    pass_avg = [m / max(nev, 1) for m in pass_ms]
-    flops = [FLOPS_PASS[0] * npairs_gb, FLOPS_PASS[1] * npairs, FLOPS_PASS[2] * npairs_gb]
-    dom = int(np.argmax(pass_avg))
-    names = ["k_born (pass 1, Born radii)", "k_gbpair (pass 2, GB+Coulomb+LJ)", "k_chain (pass 3, chain rule)"]
     sm_mhz = clocks["sm_mhz"] or 2070.0
-    fp32_peak = 152 * 128 * 2 * sm_mhz * 1e6 / 1e12
-    achieved = flops[dom] / (pass_avg[dom] * 1e-3) / 1e12
+    fp32_peak = nsm * FP32_LANES_PER_SM * 2 * sm_mhz * 1e6 / 1e12
+    mufu_peak = nsm * MUFU_PER_SM * sm_mhz * 1e6 / 1e12
+    pass_avg = [m_ / max(nev, 1) for m_ in pass_ms]
+    pairs_pass = (npairs_gb, npairs, npairs_gb)
+    passes = []
+    for k in range(3):
+        fl = FLOPS_PASS[k] * pairs_pass[k] / (pass_avg[k] * 1e-3) / 1e12
+        mu = MUFU_PASS[k] * pairs_pass[k] / (pass_avg[k] * 1e-3) / 1e12
+        passes.append({"kernel": PASS_NAMES[k], "avg_launch_ms": pass_avg[k], "pairs": pairs_pass[k],
+                       "flops_per_pair": FLOPS_PASS[k], "mufu_per_pair": MUFU_PASS[k],
+                       "fp32_tflops": fl, "fp32_frac": fl / fp32_peak,
+                       "mufu_tops": mu, "mufu_frac": mu / mufu_peak,
+                       "pairs_per_s": pairs_pass[k] / (pass_avg[k] * 1e-3)})
+    dom = int(np.argmax(pass_avg))
+    flops_dom = FLOPS_PASS[dom] * pairs_pass[dom]
 
+    c1 = None if args.c1_steps <= 0 else bench_small_md(args, stream, sp, cores)
     batched = None if args.no_batched else bench_batched(args, stream, sp, flush)
     serving = None if args.no_batched else bench_serving(args)
 
-    # CPU baseline: the oracle port on all host cores, bounded sample
+    # CPU baseline: the oracle port on the host cores, bounded sample
     os.environ.setdefault("OMP_NUM_THREADS", str(cores))
-    cpu_rate, cpu_dt, _ = run_cpu_reference(args, n, seed, args.cpu_sample, 1)
+    cb = cpu_baseline(mol, cores, args.cpu_sample)
 
     ms_sorted = sorted(step_ms)
     line = {
@@ -551,29 +713,29 @@ def main():
         "warmup": max(3, args.warmup), "ms_per_step": total_ms / args.steps, "higher_is_better": True,
         "scaling": "weak", "vs_baseline": None, "dtype": "f32 pair arithmetic, 64-bit fixed-point sums, f64 state",
         "data": "synthetic",
-        "config": {"workload": WORKLOAD, "natom": n, "options": OPTS, "realised_radius_A": radius,
-                   "pairs_in_cut": npairs, "pairs_in_rgbmax_fsmax": npairs_gb,
-                   "pairs_per_s": npairs * value, "ns_per_day": value * 0.002 * 86400 * 1e-3 / world,
-                   "p50_ms": ms_sorted[len(ms_sorted) // 2], "p99_ms": ms_sorted[min(len(ms_sorted) - 1,
-                                                                                      int(0.99 * len(ms_sorted)))],
-                   "l2": "256 MiB buffer written between timed steps (outside the timed events)",
-                   "parallelism": f"{world} independent replica(s), one per GPU",
-                   "accuracy_vs_fp64": err,
-                   "tuned_split_claim_blocks": split},
-        "roofline": {"bound": "fp32", "kernel": names[dom], "achieved": achieved, "peak": fp32_peak,
-                     "unit": "TFLOP/s", "frac": achieved / fp32_peak, "traffic": TRAFFIC_PASS[dom],
-                     "peak_source": f"nominal FP32 FMA rate (152 SMs x 128 lanes x 2) at the sampled median SM clock "
-                                    f"{sm_mhz:.0f} MHz; no tensor cores or HBM bound apply to this pass",
-                     "algorithmic_flops_per_launch": flops[dom], "avg_launch_ms": pass_avg[dom],
-                     "pass_avg_ms": pass_avg},
-        "cpu_baseline": {"value": cpu_rate, "unit": "evals/s", "cores": cores, "kind": "port",
-                         "sample": f"{args.cpu_sample} mme() evaluations of the same molecule (FP64 CPU restatement "
-                                   "of the reference egb()/mme34(), OpenMP over all host cores)"},
+        "config": cfg,
+        "pairs_per_s": npairs * value,
+        "ns_per_day": value * 0.002 * 86400 * 1e-3 / world,
+        "latency_ms": {"p50": ms_sorted[len(ms_sorted) // 2],
+                       "p99": ms_sorted[min(len(ms_sorted) - 1, int(0.99 * len(ms_sorted)))]},
+        "accuracy_vs_fp64": err,
+        "tuned_split_claim_blocks": split,
+        "md_long": md_long,
+        "roofline": {"bound": "fp32", "kernel": PASS_NAMES[dom], "achieved": passes[dom]["fp32_tflops"],
+                     "peak": fp32_peak, "unit": "TFLOP/s", "frac": passes[dom]["fp32_frac"],
+                     "traffic": TRAFFIC_PASS[dom],
+                     "peak_source": f"nominal FP32 rate ({nsm} SMs x {FP32_LANES_PER_SM} lanes x 2 flops) at the "
+                                    f"sampled median SM clock {sm_mhz:.0f} MHz; MUFU peak {nsm} SMs x "
+                                    f"{MUFU_PER_SM}/clock; no tensor core or HBM bound applies to the pair passes",
+                     "algorithmic_flops_per_launch": flops_dom, "avg_launch_ms": pass_avg[dom],
+                     "mufu_peak_tops": mufu_peak, "passes": passes},
+        "cpu_baseline": cb,
         "e2e": {"value": e2e, "unit": "evals/s", "h2d_bytes_per_step": 3 * n * 8,
                 "d2h_bytes_per_step": 3 * n * 8 + 8 * 8,
                 "path": "mme(x, f, &iter) of the C ABI, pinned host buffers"},
         "gpu_launches": launches,
         "clocks": clocks,
+        "small_md": c1,
         "batched": batched,
         "serving": serving,
     }

@@ -267,9 +267,12 @@ int sffg_server_destroy(sffg_server *s);
  * arrays.  The call is ordered on stream (NULL: the legacy default stream)
  * and returns once reff is written.
  *
- * The first call on a device does a one-time set-up with that device
- * current: it looks up the device address of the static array.  Make that
- * first call before any stream capture begins on the device.
+ * Every call looks up the static array's device address for the device
+ * current at the call (cudaGetSymbolAddress, which allocates nothing); the
+ * first call on a device also loads this library's device code there.
+ * The call copies through pageable host memory and waits for its stream,
+ * so it must not be made on a stream that is being captured: it returns
+ * SFFG_EINVAL there and leaves the capture intact.
  *
  * All calls on one device share the one array: calls whose GPU work
  * overlaps (different streams or threads) race and corrupt each other's
@@ -277,8 +280,11 @@ int sffg_server_destroy(sffg_server *s);
  *
  * Returns SFFG_OK; SFFG_ENOMEM when natom > SFFG_STATIC_MAX_ATOMS (the
  * molecule does not fit the static scratch); SFFG_EINVAL for natom < 1, a
- * NULL array, another gb or rgbmax <= 0; SFFG_ENODEV / SFFG_ECUDA when no
- * device is current or a CUDA call fails.  It does not update
+ * NULL array, another gb, rgbmax <= 0 or a capturing stream; SFFG_ENODEV /
+ * SFFG_ECUDA when no device is current or a CUDA call fails (after waiting
+ * for any of its work already queued).  On entry it clears the CUDA
+ * runtime's last-error state, so an earlier unrelated launch failure is not
+ * reported as its own.  It does not update
  * sffg_last_error(), which would need a host allocation. */
 int sffg_born_radii_static(int natom, const double *x, const double *rborn, const double *fs, int gb,
                            double rgbmax, double *reff, void *stream);

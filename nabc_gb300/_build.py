@@ -30,6 +30,10 @@ CXX_FILE_FLAGS = {
     "xmin.cpp": ["-std=c++20", "-ffp-contract=off"],
     "lmod.cpp": ["-std=c++20", "-ffp-contract=off"],
     "lowmodes.cpp": ["-ffp-contract=off"],
+    # the synthetic-molecule generator: the same molecules on every host, and
+    # the same bits as its C restatement under oracle/ (which the CPU
+    # baseline generates its inputs with)
+    "synth.cpp": ["-ffp-contract=off"],
 }
 
 

@@ -19,13 +19,14 @@
 // scale, same offset and OBC constants (src/sff/sff.c:1186-1333).
 //
 // Scratch: one file-scope __device__ array per device, kStaticMaxAtoms
-// atoms x 104 bytes (about 0.85 MB).  Its device address is looked up once
-// per device with cudaGetSymbolAddress (the set-up of the first call on
-// that device) and only that address is handed to the kernels.
+// atoms x 104 bytes (about 0.85 MB).  Every call looks up its device
+// address for the current device with cudaGetSymbolAddress (a lookup that
+// allocates nothing; the first call on a device also loads this file's
+// device code there) and only that address is handed to the kernels, so a
+// context that was reset and recreated is picked up.
 #include <cuda_runtime.h>
 
 #include <cstdint>
-#include <mutex>
 
 #include "gbmath.cuh"
 #include "../../include/sffg.h"
@@ -181,25 +182,23 @@ __global__ void k_static_finish(const StaticArgs a) {
   region<double>(a, kOffReff)[i] = reff;
 }
 
-constexpr int kMaxDevices = 64;
-std::mutex g_setup_mu;
-void *g_scratch_ptr[kMaxDevices];  // device address of g_scratch, per device ordinal
-
-// The set-up: once per device, with that device current, look up the
-// scratch array's device address.
+// The device address of g_scratch in the current device's context.  Host
+// code must not use the symbol itself: in host code it names a host-side
+// stand-in, not device memory.
 int scratch_for_current_device(unsigned char **out) {
   int dev = -1;
-  if (cudaGetDevice(&dev) != cudaSuccess) return SFFG_ENODEV;
-  if (dev < 0 || dev >= kMaxDevices) return SFFG_ENODEV;
-  std::lock_guard<std::mutex> lock(g_setup_mu);
-  if (!g_scratch_ptr[dev]) {
-    void *p = nullptr;
-    const cudaError_t e = cudaGetSymbolAddress(&p, g_scratch);
-    if (e != cudaSuccess || !p) return SFFG_ECUDA;
-    g_scratch_ptr[dev] = p;
-  }
-  *out = static_cast<unsigned char *>(g_scratch_ptr[dev]);
+  if (cudaGetDevice(&dev) != cudaSuccess || dev < 0) return SFFG_ENODEV;
+  void *p = nullptr;
+  if (cudaGetSymbolAddress(&p, g_scratch) != cudaSuccess || !p) return SFFG_ECUDA;
+  *out = static_cast<unsigned char *>(p);
   return SFFG_OK;
+}
+
+// A failure after work was queued: wait for that work (it may still read the
+// caller's host arrays or write reff) before reporting the error.
+int fail_after_queue(cudaStream_t st) {
+  cudaStreamSynchronize(st);
+  return SFFG_ECUDA;
 }
 
 }  // namespace
@@ -211,10 +210,22 @@ extern "C" int sffg_born_radii_static(int natom, const double *x, const double *
   if (natom > kStaticMaxAtoms) return SFFG_ENOMEM;  // does not fit the static scratch
   if (natom < 1 || !x || !rborn || !fs || !reff) return SFFG_EINVAL;
   if (!(gb == 1 || gb == 2 || gb == 5) || !(rgbmax > 0.0)) return SFFG_EINVAL;
+  cudaStream_t st = stream ? static_cast<cudaStream_t>(stream) : cudaStreamLegacy;
+  // copies from pageable host memory and the final wait are illegal on a
+  // capturing stream and would invalidate the caller's capture: refuse
+  cudaStreamCaptureStatus cap = cudaStreamCaptureStatusNone;
+  if (cudaStreamIsCapturing(st, &cap) != cudaSuccess) return SFFG_ECUDA;
+  if (cap != cudaStreamCaptureStatusNone) return SFFG_EINVAL;
+  // an error left by an earlier, unrelated call would otherwise be reported
+  // as this call's launch failure
+  (void)cudaGetLastError();
   unsigned char *base = nullptr;
   const int rc = scratch_for_current_device(&base);
   if (rc != SFFG_OK) return rc;
-  cudaStream_t st = stream ? static_cast<cudaStream_t>(stream) : cudaStreamLegacy;
+  int dev = 0, nsm = 0;
+  if (cudaGetDevice(&dev) != cudaSuccess ||
+      cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess || nsm < 1)
+    return SFFG_ECUDA;
 
   // Largest screened radius: bounds the pair distance that descreens at all.
   double smax = 0.0;
@@ -238,15 +249,17 @@ extern "C" int sffg_born_radii_static(int natom, const double *x, const double *
   if (cudaMemcpyAsync(base + kOffX, x, 3 * n * sizeof(double), cudaMemcpyHostToDevice, st) != cudaSuccess ||
       cudaMemcpyAsync(base + kOffRb, rborn, n * sizeof(double), cudaMemcpyHostToDevice, st) != cudaSuccess ||
       cudaMemcpyAsync(base + kOffFs, fs, n * sizeof(double), cudaMemcpyHostToDevice, st) != cudaSuccess)
-    return SFFG_ECUDA;
+    return fail_after_queue(st);
   k_static_pack<<<a.ntile, 32, 0, st>>>(a);
+  // eight warps per block, eight resident blocks per SM at most
   const long long warps = static_cast<long long>(a.ntile) * a.ntile;
-  const int blocks = static_cast<int>(warps / 8 + 1 < 152 * 8 ? warps / 8 + 1 : 152 * 8);
+  const long long cap_blocks = 8LL * nsm;
+  const int blocks = static_cast<int>(warps / 8 + 1 < cap_blocks ? warps / 8 + 1 : cap_blocks);
   k_static_born<<<blocks, 256, 0, st>>>(a);
   k_static_finish<<<(natom + 127) / 128, 128, 0, st>>>(a);
-  if (cudaGetLastError() != cudaSuccess) return SFFG_ECUDA;
+  if (cudaGetLastError() != cudaSuccess) return fail_after_queue(st);
   if (cudaMemcpyAsync(reff, base + kOffReff, n * sizeof(double), cudaMemcpyDeviceToHost, st) != cudaSuccess)
-    return SFFG_ECUDA;
+    return fail_after_queue(st);
   if (cudaStreamSynchronize(st) != cudaSuccess) return SFFG_ECUDA;
   return SFFG_OK;
 }

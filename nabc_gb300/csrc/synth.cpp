@@ -127,7 +127,10 @@ double synth_chain(int n, uint64_t seed, std::vector<V3> &pos) {
   auto inside = [&](V3 p) { return dot(p, p) <= radius * radius; };
   // first three atoms
   for (;;) {
-    V3 p0 = (0.3 * radius * std::cbrt(rng.uniform())) * random_unit(rng);
+    // the direction is drawn before the distance (an explicit order: the
+    // two draws must not depend on the compiler's choice of operand order)
+    const V3 dir = random_unit(rng);
+    V3 p0 = (0.3 * radius * std::cbrt(rng.uniform())) * dir;
     V3 p1 = p0 + bond * random_unit(rng);
     V3 u = unit(p1 - p0), w = random_unit(rng);
     V3 perp = unit(w - dot(w, u) * u);

@@ -48,6 +48,15 @@ def lib():
                                     REAL_P, INT_P]
         L.sffo_gauss_stream.argtypes = [INT_P, C.c_int, C.c_double, REAL_P, REAL_P]
         L.sffo_set_restraints.argtypes = [C.c_void_p, INT_P, REAL_P]
+        L.sffo_set_threads.argtypes = [C.c_int]
+        L.sffo_set_threads.restype = C.c_int
+        L.sffo_synth_molecule.argtypes = [C.c_int, C.c_ulonglong, REAL_P, REAL_P]
+        L.sffo_synth_molecule.restype = C.c_void_p
+        L.sffo_synth_free.argtypes = [C.c_void_p]
+        L.sffo_prm_natom.argtypes = [C.c_void_p]
+        L.sffo_prm_natom.restype = C.c_int
+        L.sffo_prm_fsmax.argtypes = [C.c_void_p]
+        L.sffo_prm_fsmax.restype = C.c_double
         _lib = L
     return _lib
 
@@ -94,14 +103,43 @@ def parse_opts(text):
     return o
 
 
+class SynthMolecule:
+    """A synthetic molecule made by oracle/synth.c, the C restatement of the
+    library's generator (sffg_synth_molecule): the same coordinates and
+    topology, made without loading the library.  .ptr is its PARMSTRUCT_T
+    (only the fields the oracle reads are filled)."""
+
+    def __init__(self, natom, seed):
+        self.x = np.zeros(3 * natom)
+        r = C.c_double(0.0)
+        self.ptr = lib().sffo_synth_molecule(natom, seed, _p(self.x), C.byref(r))
+        if not self.ptr:
+            raise ValueError("synthetic molecule generation failed")
+        self.radius = r.value
+        self.natom = lib().sffo_prm_natom(self.ptr)
+        self.fsmax = lib().sffo_prm_fsmax(self.ptr)
+
+    def close(self):
+        if self.ptr:
+            lib().sffo_synth_free(self.ptr)
+            self.ptr = None
+
+    def __del__(self):
+        self.close()
+
+
 class Oracle:
-    """One FP64 oracle session on a PARMSTRUCT_T pointer (ctypes)."""
+    """One FP64 oracle session on a PARMSTRUCT_T pointer (ctypes) or a
+    SynthMolecule."""
 
     def __init__(self, prm, opts, frozen=None):
         self.o = parse_opts(opts) if isinstance(opts, str) else opts
-        self.n = prm.contents.Natom
+        if isinstance(prm, SynthMolecule):
+            self.n, ptr = prm.natom, C.c_void_p(prm.ptr)
+        else:
+            self.n, ptr = prm.contents.Natom, C.cast(prm, C.c_void_p)
         self.frozen = None if frozen is None else np.ascontiguousarray(frozen, np.int32)
-        self.h = lib().sffo_create(C.cast(prm, C.c_void_p), C.byref(self.o),
+        self.h = lib().sffo_create(ptr, C.byref(self.o),
                                    None if self.frozen is None else self.frozen.ctypes.data_as(INT_P))
 
     def close(self):
@@ -146,6 +184,12 @@ class Oracle:
         trace = np.zeros(2 * nsteps)
         lib().sffo_md(self.h, nsteps, _p(x), _p(f), _p(v), C.byref(s), _p(trace))
         return x, v, trace.reshape(-1, 2)
+
+
+def set_threads(n):
+    """Threads of the oracle's OpenMP loops (n > 0 sets it); the count in
+    effect."""
+    return lib().sffo_set_threads(int(n))
 
 
 def gauss_stream(n, sd, seed=-1):

@@ -9,6 +9,10 @@
  *   cg  <maxiter> <dfpred> <rmsgrad> [out.bin]   conjgrad() driven by mme
  *   md  <nsteps> [out.bin]            md() driven by mme
  *   time <nevals>                     repeated quiet mme() evaluations
+ *   timei <nevals>                    mme() at iter = 0, 1, ..., nevals - 1 after
+ *                                     one untimed call: the normal cadence
+ *                                     (list rebuilt when iter % nsnb == 0),
+ *                                     printing suppressed by a large ntpr
  *   spr <out.bin>                     mme_rattle() at iter=-1 on the input
  *                                     positions shifted by 0.02 ((k mod 3) - 1) A
  *                                     per coordinate k (bond lengths off)
@@ -236,6 +240,18 @@ int main(int argc, char **argv)
     t0 = now_s();
     for (k = 0; k < nevals; k++) {
       iter = -2;
+      e = mme(x, g, &iter);
+    }
+    t1 = now_s();
+    printf("oracle_time: %d evals %.6f s total %.17g\n", nevals, t1 - t0, e);
+  } else if (strcmp(mode, "timei") == 0) {
+    int nevals = atoi(argv[5]), k;
+    double t0, t1;
+    iter = -2;
+    e = mme(x, g, &iter);
+    t0 = now_s();
+    for (k = 0; k < nevals; k++) {
+      iter = k;
       e = mme(x, g, &iter);
     }
     t1 = now_s();

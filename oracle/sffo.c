@@ -361,6 +361,18 @@ static int nthreads(void)
 #endif
 }
 
+/* Threads of the parallel loops (the CPU baseline times 1 thread and all
+ * host threads); buffers are sized per call, so this may change between
+ * calls.  Returns the count now in effect. */
+int sffo_set_threads(int n)
+{
+#ifdef _OPENMP
+  if (n > 0) omp_set_num_threads(n);
+#endif
+  (void)n;
+  return nthreads();
+}
+
 static int thread_id(void)
 {
 #ifdef _OPENMP

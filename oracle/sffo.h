@@ -71,6 +71,16 @@ int sffo_conjgrad(sffo_session *s, double *x, double *fret, double rmsgrad, doub
  * N(mean, sd) continuing from *seed. */
 void sffo_gauss_stream(int *seed, int n, double mean, const double *sd, double *out);
 
+/* Threads of the OpenMP loops (n > 0 sets it); returns the count in effect. */
+int sffo_set_threads(int n);
+
+/* oracle/synth.c: the library generator's molecule (sffg_synth_molecule),
+ * made without the library; free with sffo_synth_free. */
+PARMSTRUCT_T *sffo_synth_molecule(int natom, unsigned long long seed, double *x, double *radius_out);
+void sffo_synth_free(PARMSTRUCT_T *prm);
+int sffo_prm_natom(const PARMSTRUCT_T *prm);
+double sffo_prm_fsmax(const PARMSTRUCT_T *prm);
+
 #ifdef __cplusplus
 }
 #endif

@@ -145,3 +145,46 @@ def test_mm_options_ntpr_zero_is_refused():
     """ntpr takes [1-9][0-9]* in the reference's grammar (mm_options.l:32)."""
     r = run_py("from nabc_gb300 import sff\nsff.mm_options('ntpr=0')\nprint('not reached')")
     assert r.returncode == 1 and "ntpr=0" in r.stderr
+
+
+@pytest.mark.parametrize("natom,seed", [(4, 1), (37, 5), (600, 7), (3000, 777), (25000, 2025)])
+def test_oracle_generator_matches_library(lib, oracle_mod, natom, seed):
+    """oracle/synth.c, which the CPU baseline and the reference arm of
+    bench.py make their inputs with (without loading libsffg), gives the
+    library generator's molecule bit for bit: coordinates, radius, and
+    every topology array the oracle reads."""
+    from nabc_gb300 import sff
+    prm, x, radius = sff.synth_molecule(natom, seed)
+    m = oracle_mod.SynthMolecule(natom, seed)
+    assert np.array_equal(m.x, x)
+    assert m.radius == radius and m.natom == natom and m.fsmax == prm.contents.Fsmax
+    P = C.POINTER(sff.PARMSTRUCT_T)
+    q = C.cast(C.c_void_p(m.ptr), P).contents
+    p = prm.contents
+    for name in ("Natom", "Ntypes", "Nbonh", "Mbona", "Ntheth", "Mtheta", "Ntheta", "Nphih", "Mphia", "Nnb"):
+        assert getattr(q, name) == getattr(p, name), name
+    ln = {"Charges": natom, "Masses": natom, "Rborn": natom, "Fs": natom, "Cn1": 10, "Cn2": 10,
+          "Rk": 1, "Req": 1, "Tk": 1, "Teq": 1, "Pk": 1, "Pn": 1, "Phase": 1}
+    for name, n in ln.items():
+        assert np.array_equal(np.ctypeslib.as_array(getattr(q, name), (n,)),
+                              np.ctypeslib.as_array(getattr(p, name), (n,))), name
+    for name in INT_ARRAYS + ["AtomicNum"]:
+        if name == "Ipres":
+            continue
+        n = natom if name == "AtomicNum" else int_len(p, name)
+        if n:
+            assert np.array_equal(np.ctypeslib.as_array(getattr(q, name), (n,)),
+                                  np.ctypeslib.as_array(getattr(p, name), (n,))), name
+    n14 = int(np.ctypeslib.as_array(p.N14pairs, (natom,)).sum())
+    assert np.array_equal(np.ctypeslib.as_array(q.N14pairs, (natom,)), np.ctypeslib.as_array(p.N14pairs, (natom,)))
+    for name in ("N14pairlist", "N14sceelist", "N14scnblist"):
+        assert np.array_equal(np.ctypeslib.as_array(getattr(q, name), (n14,)),
+                              np.ctypeslib.as_array(getattr(p, name), (n14,))), name
+    # the oracle gives the same energy on both (to the rounding of its
+    # OpenMP reduction, whose order varies from run to run)
+    o1 = oracle_mod.Oracle(prm, "gb=5, cut=12.0")
+    o2 = oracle_mod.Oracle(m, "gb=5, cut=12.0")
+    if natom <= 3000:
+        assert o1.mme(x)[0] == pytest.approx(o2.mme(m.x)[0], rel=1e-12)
+    m.close()
+    sff.free_prm(prm)
