@@ -73,6 +73,7 @@ struct DeviceState {
   DBuf<int> sys_active, sys_lj_off, sys_ntypes, sys_tile_end, sys_has_frozen, nonfinite;
   DBuf<int> sys_natom, sys_atom_off;
   DBuf<float2> lj;
+  DBuf<double2> lj64;  // the same table in FP64 (close pairs)
   DBuf<long long> energy;
   DBuf<double> etot;
   // per atom
@@ -88,10 +89,10 @@ struct DeviceState {
   // C, 5..7 queues of passes 1, 2 and 3, 10 chunks of list C
   DBuf<int2> cand;
   DBuf<int4> cand_n, cand_off;
-  DBuf<unsigned> colA, colB, colC, colE;
+  DBuf<unsigned> colA, colB, colC, colE, colK;
   DBuf<int> cand_start, cand_count, chunksA, chunksB, chunksC, chunk0A, chunk0B, chunk0C;
   DBuf<int> chunkA_i, entA_slot, chunkB_i, entB_slot, chunkC_i, entC_slot;
-  DBuf<unsigned> entA_col, entA_exc, entB_col, entC_col;
+  DBuf<unsigned> entA_col, entA_exc, entA_close, entB_col, entC_col;
   DBuf<float4> xb;
   DBuf<int> counters;
   DBuf<unsigned> step;  // md step number (the Philox counter of the noise)
@@ -142,13 +143,14 @@ struct DeviceState {
     rel(acc_fz); rel(tile_valid); rel(tile_sys); rel(box_lo); rel(box_hi); rel(excl_tile_start);
     rel(excl_tile_j); rel(excl_tile_idx); rel(excl_masks); rel(sys_active); rel(sys_lj_off);
     rel(sys_ntypes); rel(sys_tile_end); rel(sys_has_frozen); rel(nonfinite); rel(sys_natom);
-    rel(sys_atom_off); rel(lj); rel(energy); rel(etot); rel(x); rel(grad); rel(v); rel(accel);
+    rel(sys_atom_off); rel(lj); rel(lj64); rel(energy); rel(etot); rel(x); rel(grad); rel(v); rel(accel);
     rel(minv); rel(sqrmass); rel(atom_slot); rel(atom_sys); rel(atom_frozen); rel(bond_atoms);
     rel(bond_par); rel(angle_par); rel(angle_atoms); rel(dih_atoms); rel(p14_atoms); rel(dih_par);
     rel(p14_par); rel(cand); rel(cand_n); rel(cand_off); rel(colA); rel(colB); rel(colC); rel(colE);
     rel(cand_start); rel(cand_count); rel(chunksA); rel(chunksB); rel(chunksC); rel(chunk0A);
     rel(chunk0B); rel(chunk0C); rel(chunkA_i); rel(entA_slot); rel(chunkB_i); rel(entB_slot);
     rel(chunkC_i); rel(entC_slot); rel(entA_col); rel(entA_exc); rel(entB_col); rel(entC_col);
+    rel(colK); rel(entA_close);
     rel(xb); rel(counters); rel(step); rel(cg_nactive); rel(sys_key); rel(tile_flagB); rel(cons_w); rel(cons_x0); rel(neck_pos); rel(neck_val); rel(tscal);
     rel(noise); rel(rndf); rel(ekin); rel(ekin_last); rel(cg_w); rel(cg_state);
   }
@@ -295,7 +297,8 @@ int Batch::upload() {
   std::vector<int> sys_tile_end(nsys), sys_has_frozen(nsys), sys_ntypes(nsys), sys_lj_off(nsys),
       sys_natom(nsys), sys_atom_off(nsys);
   std::vector<float2> lj;
-  std::map<std::vector<float>, int> lj_dedupe;
+  std::vector<double2> lj64;
+  std::map<std::vector<double>, int> lj_dedupe;
   std::vector<int> excl_tile_start(ntile_ + 1, 0);
   std::vector<std::vector<std::pair<int, int>>> excl_by_tile(ntile_);
   std::vector<unsigned> excl_masks;
@@ -352,13 +355,16 @@ int Batch::upload() {
     sys_natom[s] = n;
     sys_atom_off[s] = si.atom_off;
     {
-      std::vector<float> keyv(hs.lj_a);
-      keyv.insert(keyv.end(), hs.lj_b.begin(), hs.lj_b.end());
-      keyv.push_back(static_cast<float>(hs.ntypes));
+      std::vector<double> keyv(hs.lj_a64);
+      keyv.insert(keyv.end(), hs.lj_b64.begin(), hs.lj_b64.end());
+      keyv.push_back(static_cast<double>(hs.ntypes));
       auto it = lj_dedupe.find(keyv);
       if (it == lj_dedupe.end()) {
         const int o = static_cast<int>(lj.size());
-        for (size_t k = 0; k < hs.lj_a.size(); k++) lj.push_back(make_float2(hs.lj_a[k], hs.lj_b[k]));
+        for (size_t k = 0; k < hs.lj_a.size(); k++) {
+          lj.push_back(make_float2(hs.lj_a[k], hs.lj_b[k]));
+          lj64.push_back(make_double2(hs.lj_a64[k], hs.lj_b64[k]));
+        }
         it = lj_dedupe.emplace(keyv, o).first;
       }
       sys_lj_off[s] = it->second;
@@ -440,6 +446,7 @@ int Batch::upload() {
   SFFG_CK(up(d.sys_natom, sys_natom));
   SFFG_CK(up(d.sys_atom_off, sys_atom_off));
   SFFG_CK(up(d.lj, lj));
+  SFFG_CK(up(d.lj64, lj64));
   SFFG_CK(up(d.excl_tile_start, excl_tile_start));
   SFFG_CK(up(d.excl_tile_j, excl_tile_j));
   SFFG_CK(up(d.excl_tile_idx, excl_tile_idx));
@@ -573,6 +580,7 @@ size_t Batch::device_bytes() const {
   b += d.chunkA_i.bytes() + d.entA_slot.bytes() + d.entA_col.bytes() + d.entA_exc.bytes();
   b += d.chunkB_i.bytes() + d.entB_slot.bytes() + d.entB_col.bytes() + d.xb.bytes();
   b += d.chunkC_i.bytes() + d.entC_slot.bytes() + d.entC_col.bytes();
+  b += d.colK.bytes() + d.entA_close.bytes();
   b += d.grad.bytes() + d.v.bytes() + d.accel.bytes() + d.minv.bytes() + d.sqrmass.bytes();
   b += d.excl_masks.bytes() + d.cg_w.bytes() + d.noise.bytes();
   b += d.bond_par.bytes() + d.angle_par.bytes() + d.dih_par.bytes() + d.p14_par.bytes();
@@ -820,10 +828,13 @@ DevTables make_tables(DeviceState &d, const ModelParams &mp, double fsmax, int q
   t.rinv2 = d.rinv2.p;
   t.sumda32 = d.sumda32.p;
   t.tile_sys = d.tile_sys.p;
+  t.box_lo = d.box_lo.p;
+  t.box_hi = d.box_hi.p;
   t.sys_active = d.sys_active.p;
   t.sys_lj_off = d.sys_lj_off.p;
   t.sys_ntypes = d.sys_ntypes.p;
   t.lj = d.lj.p;
+  t.lj64 = d.lj64.p;
   t.lj_n = static_cast<int>(d.lj.n);
   t.nslot = static_cast<int>(d.pos_hi.n);
   t.ntile = static_cast<int>(d.tile_sys.n);
@@ -831,16 +842,19 @@ DevTables make_tables(DeviceState &d, const ModelParams &mp, double fsmax, int q
   t.la.slot = d.entA_slot.p;
   t.la.col = d.entA_col.p;
   t.la.exc = d.entA_exc.p;
+  t.la.close = d.entA_close.p;
   t.la.nchunk = d.counters.p + 2;
   t.lb.chunk_i = d.chunkB_i.p;
   t.lb.slot = d.entB_slot.p;
   t.lb.col = d.entB_col.p;
   t.lb.exc = nullptr;
+  t.lb.close = nullptr;
   t.lb.nchunk = d.counters.p + 3;
   t.lc.chunk_i = d.chunkC_i.p;
   t.lc.slot = d.entC_slot.p;
   t.lc.col = d.entC_col.p;
   t.lc.exc = nullptr;
+  t.lc.close = nullptr;
   t.lc.nchunk = d.counters.p + 10;
   t.counter = d.counters.p + queue;
   t.acc_sumi = d.acc_sumi.p;
@@ -909,6 +923,7 @@ ListArgs Batch::list_args(double fsmax) {
   a.colA = d.colA.p;
   a.colB = d.colB.p;
   a.colC = d.colC.p;
+  a.colK = d.colK.p;
   a.colE = d.colE.p;
   a.gbpar = d.gbpar.p;
   a.cand_n = d.cand_n.p;
@@ -926,6 +941,8 @@ ListArgs Batch::list_args(double fsmax) {
   a.entA_slot = d.entA_slot.p;
   a.entA_col = d.entA_col.p;
   a.entA_exc = d.entA_exc.p;
+  a.entA_close = d.entA_close.p;
+  a.close2f = (kClose + 1.0f) * (kClose + 1.0f);
   a.chunkB_i = d.chunkB_i.p;
   a.entB_slot = d.entB_slot.p;
   a.entB_col = d.entB_col.p;
@@ -973,6 +990,7 @@ int Batch::build_lists(void *stream) {
   SFFG_CK(ensure(d.colA, nc * 32));
   SFFG_CK(ensure(d.colB, nc * 32));
   SFFG_CK(ensure(d.colC, nc * 32));
+  SFFG_CK(ensure(d.colK, nc * 32));
   SFFG_CK(ensure(d.colE, nc * 32));
   SFFG_CK(ensure(d.cand_n, nc));
   SFFG_CK(ensure(d.cand_off, nc));
@@ -994,6 +1012,7 @@ int Batch::build_lists(void *stream) {
   SFFG_CK(ensure(d.entA_slot, ne));
   SFFG_CK(ensure(d.entA_col, ne));
   SFFG_CK(ensure(d.entA_exc, ne));
+  SFFG_CK(ensure(d.entA_close, ne));
   SFFG_CK(ensure(d.entB_slot, ne));
   SFFG_CK(ensure(d.entB_col, ne));
   SFFG_CK(ensure(d.chunkA_i, ne / 32));
@@ -1043,8 +1062,9 @@ int Batch::eval(bool rebuild, void *stream) {
 // outgrows its store).
 std::vector<const void *> Batch::list_sig() const {
   const DeviceState &d = *d_;
-  return {d.cand.p, d.cand_n.p, d.cand_off.p, d.colA.p, d.colB.p, d.colC.p, d.colE.p, d.chunkA_i.p, d.entA_slot.p,
-          d.entA_col.p, d.entA_exc.p, d.chunkB_i.p, d.entB_slot.p, d.entB_col.p, d.chunkC_i.p, d.entC_slot.p,
+  return {d.cand.p, d.cand_n.p, d.cand_off.p, d.colA.p, d.colB.p, d.colC.p, d.colE.p, d.chunkA_i.p,
+          d.entA_slot.p, d.entA_col.p, d.entA_exc.p, d.chunkB_i.p, d.entB_slot.p, d.entB_col.p, d.chunkC_i.p,
+          d.colK.p, d.entA_close.p, d.entC_slot.p,
           d.entC_col.p};
 }
 

@@ -14,6 +14,7 @@
 #pragma once
 
 #include <cstdint>
+#include <type_traits>
 
 #include "gbmath.cuh"
 
@@ -21,6 +22,10 @@ namespace sffg {
 
 constexpr unsigned kFull = 0xffffffffu;
 constexpr int kEnergySlots = 9;  // fixed-point energy terms per system (EnergySlot)
+// Non-excluded pairs closer than this (in A, at the list build) take their
+// Coulomb and Lennard-Jones terms in FP64: their forces reach 1e3-1e5
+// kcal/mol/A, where FP32 rounding alone is ~1e-7 of them.
+constexpr float kClose = 2.5f;
 
 // One compacted pair list (built by lists.cuh).
 struct ChunkList {
@@ -28,6 +33,7 @@ struct ChunkList {
   const int *slot;      // 32 j slots per chunk
   const unsigned *col;  // per entry, bit i: the pair with lane i of the i-tile is listed
   const unsigned *exc;  // per entry, bit i: the pair is excluded from Coulomb/LJ (cutoff list)
+  const unsigned *close;  // per entry, bit i: a close pair, Coulomb/LJ in FP64 (cutoff list)
   const int *nchunk;
 };
 
@@ -42,11 +48,13 @@ struct DevTables {
   const float *sumda32;   // chain-rule weight (pass 3)
   // per tile
   const int *tile_sys;
+  const float4 *box_lo, *box_hi;  // bounding boxes (their centres are the tiles' reference points)
   // per system
   const int *sys_active;
   const int *sys_lj_off;
   const int *sys_ntypes;
   const float2 *lj;       // (A, B) per type pair, per system blocks
+  const double2 *lj64;    // the same table in FP64 (close pairs)
   int lj_n;               // entries of lj
   bool lj_shared;         // pass 2 may stage lj in shared memory
   int nslot, ntile;       // extents, for the checked build
@@ -198,6 +206,73 @@ __device__ __forceinline__ int chunk_entry(const ChunkList &L, int k, int lane, 
   return SFFG_IDX(L.slot[e], nslot, kCheckSlot);
 }
 
+// ------------------------------------------------------ rotation schedule
+// Far-field chunks (lists A, B and T) are walked in a rotation: lane l holds
+// i-atom l of the chunk's i-tile; at step s (0..31) it takes j-entry
+// (l + s) mod 32, so every step the warp evaluates 32 different pairs and
+// each entry meets each lane once.  The entry data sit twice in shared
+// memory (entries 0..31, then again), so lane l's read at step s is element
+// l + s with the step as an immediate offset.  An entry's j-side sums travel
+// with it: after each step every lane hands them to lane l - 1, which meets
+// that entry next; after 32 steps lane e holds entry e's sums.  The column
+// masks are transposed once per chunk so that bit s of a lane's mask word is
+// its pair at step s.  Coordinates are taken relative to a reference point
+// of the i-tile: the i-atom's exactly (high + low parts), the entry's as one
+// FP32 value.
+
+// 32 x 32 bit-matrix transpose over the warp: lane l returns the word whose
+// bit e is bit l of lane e's x.
+__device__ __forceinline__ unsigned warp_transpose_bits(unsigned x, int lane) {
+  unsigned m = 0x0000ffffu;
+#pragma unroll
+  for (int j = 16; j != 0; j >>= 1, m ^= m << j) {
+    const unsigned y = __shfl_xor_sync(kFull, x, j);
+    x = (lane & j) ? ((x & ~m) | ((y >> j) & m)) : ((x & m) | ((y << j) & ~m));
+  }
+  return x;
+}
+
+// Lane l's pair at step s of the rotation schedule: bit s of the result is
+// bit l of entry (l + s) mod 32's column word col (held by that lane).
+__device__ __forceinline__ unsigned rotation_mask(unsigned col, int lane) {
+  const unsigned t = warp_transpose_bits(col, lane);
+  return __funnelshift_r(t, t, lane);
+}
+
+// (hi + lo) - c for coordinates split into FP32 high and low parts and a
+// reference point c: the exact difference hi - c (two-sum) plus lo.  d gets
+// the rounded value; e the remainder (|e| <= half an ulp of d).
+__device__ __forceinline__ void rel_coord(float hi, float lo, float c, float &d, float &e) {
+  const float s = hi - c;
+  const float hv = s + c;
+  const float err = (hi - hv) + ((hv - s) - c);  // hi - c = s + err exactly
+  const float t = err + lo;
+  d = s + t;
+  e = (s - d) + t;
+}
+
+// Reference point of tile I: its bounding box's centre rounded to 1/256 A.
+__device__ __forceinline__ float3 tile_ref(const float4 *box_lo, const float4 *box_hi, int I) {
+  const float4 a = box_lo[I], b = box_hi[I];
+  const float cx = rintf((a.x + b.x) * 128.0f) * (1.0f / 256.0f);
+  const float cy = rintf((a.y + b.y) * 128.0f) * (1.0f / 256.0f);
+  const float cz = rintf((a.z + b.z) * 128.0f) * (1.0f / 256.0f);
+  // a tile without a finite atom has an empty (inverted) box: centre 0
+  return make_float3(isfinite(cx) ? cx : 0.0f, isfinite(cy) ? cy : 0.0f, isfinite(cz) ? cz : 0.0f);
+}
+
+__device__ __forceinline__ float ex2_ftz(float x) {
+  float y;
+  asm("ex2.approx.ftz.f32 %0, %1;" : "=f"(y) : "f"(x));
+  return y;
+}
+
+__device__ __forceinline__ float rsqrt_ftz(float x) {
+  float y;
+  asm("rsqrt.approx.ftz.f32 %0, %1;" : "=f"(y) : "f"(x));
+  return y;
+}
+
 // ------------------------------------------------------------ list C chunks
 // List C holds the pairs close enough for the near-field forms; its chunks
 // are sparse (~13% of the 32 x 32 bits set), so a warp walks the set bits
@@ -212,7 +287,7 @@ __device__ __forceinline__ int chunk_entry(const ChunkList &L, int k, int lane, 
 // throughput-bound, and mixing them keeps every SM issuing.
 
 // Work item m of the merged queue: true and the list C chunk k, or false
-// and the list B chunk k.
+// and the list B chunk k (the list C chunks spread evenly among the others).
 __device__ __forceinline__ bool merged_item(int m, int nB, int nC, int &k) {
   const long long n = static_cast<long long>(nB) + nC;
   const int c0 = static_cast<int>(static_cast<long long>(m) * nC / n);
@@ -220,8 +295,6 @@ __device__ __forceinline__ bool merged_item(int m, int nB, int nC, int &k) {
   k = c1 > c0 ? c0 : m - c0;
   return c1 > c0;
 }
-
-
 
 // Pair p of the chunk (0 <= p < total): its j-entry and i-lane, from the
 // exclusive prefix counts s_pre of set bits per entry.
@@ -276,8 +349,34 @@ __device__ __forceinline__ int near_stage(const DevTables &t, int k, int lane, f
 // ------------------------------------------------------------------ pass 1
 // Born-radius descreening sums (src/sff/eff.c:1566-1709): both directions
 // of every pair within rgbmax + Fsmax, over lists B and C.
+
+// Far-field descreening term of a sphere of radius s (s2 = s^2) at
+// 1/dij^2 = d2i (the Taylor form of eff.c:1674-1681), and its derivative
+// over dij (eff.c:2299-2307): far_term / far_deriv with s^2 and 1/dij^2
+// supplied.
+__device__ __forceinline__ float far_term2(float d2i, float s, float s2) {
+  const float tmpsd = s2 * d2i;
+  const float dumbo = fmaf(tmpsd, fmaf(tmpsd, fmaf(tmpsd, fmaf(tmpsd, kTDD, kTD), kTC), kTB), kTA) + kTAlo;
+  return s * tmpsd * d2i * dumbo;
+}
+
+__device__ __forceinline__ float far_deriv2(float d2i, float s, float s2) {
+  const float tmpsd = s2 * d2i;
+  const float dumbo = fmaf(tmpsd, fmaf(tmpsd, fmaf(tmpsd, fmaf(tmpsd, kTHH, kTH), kTG), kTF), kTE) + kTElo;
+  return tmpsd * s * d2i * d2i * dumbo;
+}
+
+// r^2 given to a lane whose pair is not on the list: every far-field,
+// tail and neck term of it is an exact zero.
+constexpr float kOffList = 1.0e30f;
+
 template <bool NECK>
 __global__ void __launch_bounds__(256, 3) k_born(const DevTables t) {
+  // far-field chunks (list B): per warp the entries twice, (x, y, z
+  // relative to the i-tile's reference point, s) and (s correction, s^2,
+  // rborn, neck index)
+  __shared__ float4 sm_a[8][64], sm_b[8][64];
+  // near-field chunks (list C)
   __shared__ float4 sm_hi[8][32], sm_lo[8][32], sm_gb[8][32];  // j entries of the chunk
   __shared__ float4 si_hi[8][32], si_lo[8][32], si_gb[8][32];  // the i-tile
   __shared__ unsigned sm_col[8][32];
@@ -294,66 +393,90 @@ __global__ void __launch_bounds__(256, 3) k_born(const DevTables t) {
   const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
   const int nB = *t.lb.nchunk, nC = *t.lc.nchunk, nitem = nB + nC;
   const float FB = 1099511627776.0f;
+  const float rgbmax = t.born.rgbmax;
+  const int next = (lane + 1) & 31;
   int cur_I = -1;
-  float xi = 0, yi = 0, zi = 0, xli = 0, yli = 0, zli = 0, si = 0, rbi = 0, sci = 0;
+  float3 cref = make_float3(0.f, 0.f, 0.f);
+  float xi = 0, yi = 0, zi = 0, xil = 0, yil = 0, zil = 0, si = 0, si2 = 0, rbi = 0, sci = 0;
   int nki = 0;
   long long sumi64 = 0;
 
-  // list B chunk k: lanes hold the i-tile, steps walk the 32 j-entries
+  // list B chunk k, rotation schedule
   auto far_chunk = [&](int k) {
-    unsigned mycol;
-    const int sj = chunk_entry(t.lb, k, lane, mycol, t.nslot);
-    sm_hi[w][lane] = t.pos_hi[sj];
-    sm_lo[w][lane] = t.pos_lo[sj];
+    const size_t e = static_cast<size_t>(k) * 32 + lane;
+    const unsigned mycol = t.lb.col[e];
+    const int sj = SFFG_IDX(t.lb.slot[e], t.nslot, kCheckSlot);
     {
-      // far chunks never read the radius rho in gbpar.x: it carries the
-      // entry's column mask, one shared read per step fewer
-      float4 gq = t.gbpar[sj];
-      gq.x = __uint_as_float(mycol);
-      sm_gb[w][lane] = gq;
+      const float4 h = t.pos_hi[sj], l = t.pos_lo[sj], g = t.gbpar[sj];
+      float dx, dy, dz, ex, ey, ez;
+      rel_coord(h.x, l.x, cref.x, dx, ex);
+      rel_coord(h.y, l.y, cref.y, dy, ey);
+      rel_coord(h.z, l.z, cref.z, dz, ez);
+      const float4 a = make_float4(dx, dy, dz, g.y);
+      const float4 b = make_float4(g.w, g.y * g.y, g.z, NECK ? __int_as_float((t.param[sj] >> 16) & 0xff) : 0.0f);
+      sm_a[w][lane] = a;
+      sm_a[w][lane + 32] = a;
+      sm_b[w][lane] = b;
+      sm_b[w][lane + 32] = b;
     }
-    if (NECK) sm_par[w][lane] = t.param[sj];
-    const unsigned cols = __ballot_sync(kFull, mycol != 0u);
+    const unsigned m_in = rotation_mask(mycol, lane);
     __syncwarp();
-    float acc_i = 0.0f, acc_j = 0.0f;
+    float acc_i = 0.0f, aj = 0.0f;
 #pragma unroll 1
-    for (int g = 0; g < 32 / kGroup; g++) {
-      float aj[kGroup];
+    for (int g = 0; g < 32; g += 4) {
+      const unsigned gin = m_in >> g;
+      const float4 *pa = &sm_a[w][lane + g];
+      const float4 *pb = &sm_b[w][lane + g];
 #pragma unroll
-      for (int s = 0; s < kGroup; s++) {
-        const int j = g * kGroup + s;
-        aj[s] = 0.0f;
-        if (!((cols >> j) & 1u)) continue;  // padding entry
-        const float4 h = sm_hi[w][j], l = sm_lo[w][j], gp = sm_gb[w][j];
-        const float dx = (xi - h.x) + (xli - l.x);
-        const float dy = (yi - h.y) + (yli - l.y);
-        const float dz = (zi - h.z) + (zli - l.z);
-        const float r2 = fmaf(dx, dx, fmaf(dy, dy, dz * dz));
-        const bool in = ((__float_as_uint(gp.x) >> lane) & 1u) && r2 <= t.born.cutoff2;
-        if (!__any_sync(kFull, in)) continue;  // every lane out of range
-        const float dij1i = rsqrt_nr(r2);
-        const float dij = r2 * dij1i;
-        float ti, tj;
-        descreen_pair<false>(t.born, in, dij, dij1i, si, gp.y, ti, tj);
-        ti = fmaf(ti, gp.w, ti);
+      for (int u = 0; u < 4; u++) {
+        const float4 a = pa[u];
+        const bool in = (gin >> u) & 1u;
+        const float dx = (xi - a.x) + xil;
+        const float dy = (yi - a.y) + yil;
+        const float dz = (zi - a.z) + zil;
+        float r2 = fmaf(dx, dx, fmaf(dy, dy, dz * dz));
+        // off the list, or beyond rgbmax + Fsmax, where the reference skips
+        // the pair (eff.c:1649)
+        r2 = in && r2 <= t.born.cutoff2 ? r2 : kOffList;
+        const float d1 = rsqrt_nr(r2);
+        const float d2i = d1 * d1;
+        const float cj = pb[u].x;
+        float ti = far_term2(d2i, a.w, pb[u].y);
+        float tj = far_term2(d2i, si, si2);
+        const float dij = r2 * d1;
+        {
+          // the smooth tail for dij > rgbmax - s, zero beyond rgbmax + s
+          // (with a negative s, GBneck2's sulfur, that range starts below)
+          const bool qi_ = dij > rgbmax - a.w, qj_ = dij > rgbmax - si;
+          if (__any_sync(kFull, qi_ || qj_)) {
+            const float vi = tail_closed<false>(t.born, dij, d1, a.w);
+            const float vj = tail_closed<false>(t.born, dij, d1, si);
+            ti = qi_ ? vi : ti;
+            tj = qj_ ? vj : tj;
+          }
+          ti = dij > rgbmax + a.w ? 0.0f : ti;
+          tj = dij > rgbmax + si ? 0.0f : tj;
+        }
+        ti = fmaf(ti, cj, ti);
         tj = fmaf(tj, sci, tj);
         if (NECK) {
-          const bool nk = in && dij < rbi + gp.z + 6.8f;
+          const float4 b = pb[u];
+          const bool nk = dij < rbi + b.z + 6.8f;
           if (__any_sync(kFull, nk)) {
-            const int nkj = (sm_par[w][j] >> 16) & 0xff;
-            const float a = neck_term(dij, s_npos[SFFG_IDX(nki * 21 + nkj, 441, kCheckNeck)], s_nval[SFFG_IDX(nki * 21 + nkj, 441, kCheckNeck)], t.neck_scale);
-            const float b = neck_term(dij, s_npos[SFFG_IDX(nkj * 21 + nki, 441, kCheckNeck)], s_nval[SFFG_IDX(nkj * 21 + nki, 441, kCheckNeck)], t.neck_scale);
-            ti += nk ? a : 0.0f;
-            tj += nk ? b : 0.0f;
+            const int nkj = __float_as_int(b.w);
+            const int ij = SFFG_IDX(nki * 21 + nkj, 441, kCheckNeck), ji = SFFG_IDX(nkj * 21 + nki, 441, kCheckNeck);
+            const float na = neck_term(dij, s_npos[ij], s_nval[ij], t.neck_scale);
+            const float nb = neck_term(dij, s_npos[ji], s_nval[ji], t.neck_scale);
+            ti += nk ? na : 0.0f;
+            tj += nk ? nb : 0.0f;
           }
         }
-        acc_i += in ? ti : 0.0f;
-        aj[s] = in ? tj : 0.0f;
+        acc_i += ti;
+        aj = __shfl_sync(kFull, aj + tj, next);
       }
-      acc_j += reduce_to_lane(aj, g, lane);
     }
     sumi64 += to_fixed(acc_i, FB);
-    if (mycol) atomic_add_ll(&t.acc_sumi[sj], to_fixed(acc_j, FB));
+    if (mycol) atomic_add_ll(&t.acc_sumi[sj], to_fixed(aj, FB));
     __syncwarp();
   };
 
@@ -419,8 +542,11 @@ __global__ void __launch_bounds__(256, 3) k_born(const DevTables t) {
         const int sl = I * 32 + lane;
         const float4 h = t.pos_hi[sl], l = t.pos_lo[sl], g = t.gbpar[sl];
         const int pr = t.param[sl];
-        xi = h.x; yi = h.y; zi = h.z; xli = l.x; yli = l.y; zli = l.z;
-        si = g.y; rbi = g.z; sci = g.w;
+        cref = tile_ref(t.box_lo, t.box_hi, I);
+        rel_coord(h.x, l.x, cref.x, xi, xil);
+        rel_coord(h.y, l.y, cref.y, yi, yil);
+        rel_coord(h.z, l.z, cref.z, zi, zil);
+        si = g.y; si2 = g.y * g.y; rbi = g.z; sci = g.w;
         nki = (pr >> 16) & 0xff;
         si_hi[w][lane] = h;
         si_lo[w][lane] = l;
@@ -437,32 +563,53 @@ __global__ void __launch_bounds__(256, 3) k_born(const DevTables t) {
 // ------------------------------------------------------------------ pass 2
 // GB + Coulomb + Lennard-Jones pair energies, dE/dr and sumdeijda
 // (src/sff/eff.c:1902-2063) over list A.
+//
+// Rotation schedule: lane l holds i-atom l of the chunk's i-tile; at step s
+// (0..31) it takes j-entry (l + s) mod 32, so every step the warp evaluates
+// 32 different pairs and each entry meets each lane once.  The entry data
+// sit twice in shared memory (entries 0..31, then again), so lane l's read
+// at step s is element l + s with the step as an immediate offset.  An
+// entry's j-side sums travel with it: after each step every lane hands its
+// j-side partials to lane l - 1, which meets that entry next; after 32
+// steps lane e holds entry e's sums.  The column masks are transposed once
+// per chunk so that bit s of a lane's mask word is its pair at step s.
 // Lennard-Jones tables of up to this many (A, B) entries (all systems of the
 // batch together) are read from shared memory in pass 2.
 constexpr int kLjShared = 4096;
 
 template <bool KAPPA, bool LJS>
 __global__ void __launch_bounds__(256, 3) k_gbpair(const DevTables t) {
-  // j-entries of the chunk: position (hi, lo + Born radius) and
-  // (1/R_j^2 / 4, Lennard-Jones row offset type_j * ntypes, column mask,
-  // exclusion mask), three 16-byte reads per step
-  __shared__ float4 sm_hi[8][32], sm_lo[8][32];
-  __shared__ uint4 sm_aux[8][32];
-  __shared__ float2 s_lj[LJS ? kLjShared : 1];
+  // per warp, the chunk's 32 entries twice: (x, y, z relative to the i-tile's
+  // reference point, q), (R, sqrt(log2 e / 4) / R, Lennard-Jones row) and,
+  // for chunks with close pairs, (the low parts of x, y, z, the slot)
+  __shared__ float4 sm_a[8][64];
+  __shared__ float4 sm_b[8][64];
+  __shared__ float4 sm_e[8][64];
+  // the batch's Lennard-Jones table and, after it, one zero entry (the
+  // coefficients of an excluded pair)
+  __shared__ float2 s_lj[LJS ? kLjShared + 1 : 1];
   if (LJS) {  // a static table: staged before the wait
     for (int i = threadIdx.x; i < t.lj_n; i += blockDim.x) s_lj[i] = t.lj[i];
+    if (threadIdx.x == 0) s_lj[t.lj_n] = make_float2(0.0f, 0.0f);
     __syncthreads();
   }
   pdl_wait();
-  const float2 *const lj_all = LJS ? s_lj : t.lj;
   const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
   const int nchunk = *t.la.nchunk;
+  const int zero_lj = t.lj_n;
+  const int next = (lane + 1) & 31;
   int cur_I = -1, cur_sys = -1;
-  float xi = 0, yi = 0, zi = 0, xli = 0, yli = 0, zli = 0, qi = 0, ri = 1, rvi = 0;
-  int ti = 0, nt = 1;
-  const float2 *lj = lj_all;
+  float3 cref = make_float3(0.f, 0.f, 0.f);
+  float xi = 0, yi = 0, zi = 0, xil = 0, yil = 0, zil = 0, qi = 0, ri = 1, rvi = 0;
+  int lj_i = 0, lj_full_i = 0, nt = 1;
+  const float2 *lj = t.lj;
   long long fx64 = 0, fy64 = 0, fz64 = 0, sd64 = 0, ep64 = 0, ee64 = 0, ev64 = 0;
   const float FS = 4294967296.0f;
+  const double FSD = 4294967296.0;
+  // kappa = 0: dielfac is a constant, applied once per chunk to the GB
+  // energy and the sumdeijda sums (the 1/2 of eff.c's temp5 with it)
+  const float dielfac = t.pair.dielfac0;
+  const float ep_scale = KAPPA ? 1.0f : dielfac, sd_scale = KAPPA ? 0.5f : 0.5f * dielfac;
   auto flush_i = [&]() {
     const int sl = cur_I * 32 + lane;
     atomic_add_ll(&t.acc_fx[sl], fx64);
@@ -479,6 +626,35 @@ __global__ void __launch_bounds__(256, 3) k_gbpair(const DevTables t) {
     }
     ep64 = ee64 = ev64 = 0;
   };
+  // Coulomb and Lennard-Jones of a close pair in FP64 (eff.c:2004-2025),
+  // from the exact relative coordinates (i: high + low parts; entry: its
+  // rounded value and remainder), added to the fixed-point sums directly
+  auto close_pair = [&](const float4 &a, const float4 &b, const float4 &e) {
+    const double dx = (static_cast<double>(xi) - a.x) + (static_cast<double>(xil) - e.x);
+    const double dy = (static_cast<double>(yi) - a.y) + (static_cast<double>(yil) - e.y);
+    const double dz = (static_cast<double>(zi) - a.z) + (static_cast<double>(zil) - e.z);
+    const double r2 = fma(dx, dx, fma(dy, dy, dz * dz));
+    double rinv = rsqrt_ftz(static_cast<float>(r2));
+    rinv = rinv * fma(-0.5 * r2 * rinv, rinv, 1.5);  // two Newton steps: FP64 accuracy
+    rinv = rinv * fma(-0.5 * r2 * rinv, rinv, 1.5);
+    const double r2inv = rinv * rinv;
+    const double2 ab = t.lj64[__float_as_int(b.z) + lj_full_i];
+    const double eel = static_cast<double>(qi) * a.w * rinv;
+    const double r6inv = r2inv * r2inv * r2inv;
+    const double f6 = ab.y * r6inv, f12 = ab.x * (r6inv * r6inv);
+    const double de = -(12.0 * f12 - 6.0 * f6 + eel) * r2inv;
+    const long long gx = __double2ll_rn(de * dx * FSD), gy = __double2ll_rn(de * dy * FSD),
+                    gz = __double2ll_rn(de * dz * FSD);
+    fx64 += gx;
+    fy64 += gy;
+    fz64 += gz;
+    const int sj = __float_as_int(e.w);
+    atomic_add_ll(&t.acc_fx[sj], -gx);
+    atomic_add_ll(&t.acc_fy[sj], -gy);
+    atomic_add_ll(&t.acc_fz[sj], -gz);
+    ee64 += __double2ll_rn(eel * FSD);
+    ev64 += __double2ll_rn((f12 - f6) * FSD);
+  };
   for (;;) {
     const int base = claim_chunk(t.counter, lane, t.claim);
     if (base >= nchunk) break;
@@ -490,92 +666,173 @@ __global__ void __launch_bounds__(256, 3) k_gbpair(const DevTables t) {
       if (sys != cur_sys) {
         if (cur_sys >= 0) flush_e();
         cur_sys = sys;
-        lj = lj_all + t.sys_lj_off[sys];
         nt = t.sys_ntypes[sys];
+        lj = t.lj + t.sys_lj_off[sys];
       }
       if (I != cur_I) {
         if (cur_I >= 0) flush_i();
         cur_I = I;
         fx64 = fy64 = fz64 = sd64 = 0;
         const int sl = I * 32 + lane;
+        cref = tile_ref(t.box_lo, t.box_hi, I);
         const float4 h = t.pos_hi[sl], l = t.pos_lo[sl];
-        xi = h.x; yi = h.y; zi = h.z; qi = h.w; xli = l.x; yli = l.y; zli = l.z;
+        rel_coord(h.x, l.x, cref.x, xi, xil);
+        rel_coord(h.y, l.y, cref.y, yi, yil);
+        rel_coord(h.z, l.z, cref.z, zi, zil);
+        qi = h.w;
         ri = t.reff32[sl];
         rvi = t.rinv2[sl];
-        ti = t.param[sl] & 0xffff;
+        const int ti = t.param[sl] & 0xffff;
+        lj_full_i = t.sys_lj_off[sys] + ti;
+        lj_i = LJS ? lj_full_i : ti;
       }
-      unsigned mycol;
-      const int sj = chunk_entry(t.la, k, lane, mycol, t.nslot);
+      // stage the chunk's entries (lane e: entry e), twice
+      const size_t e = static_cast<size_t>(k) * 32 + lane;
+      const unsigned mycol = t.la.col[e];
+      const unsigned myexc = t.la.exc[e];
+      const unsigned myclose = t.la.close[e];
+      const int sj = SFFG_IDX(t.la.slot[e], t.nslot, kCheckSlot);
+      const bool any_close = __any_sync(kFull, myclose != 0u);
       {
-        float4 l = t.pos_lo[sj];
-        l.w = t.reff32[sj];
-        sm_hi[w][lane] = t.pos_hi[sj];
-        sm_lo[w][lane] = l;
-        sm_aux[w][lane] = make_uint4(__float_as_uint(t.rinv2[sj]), (t.param[sj] & 0xffff) * nt, mycol,
-                                     t.la.exc[static_cast<size_t>(k) * 32 + lane]);
+        const float4 h = t.pos_hi[sj], l = t.pos_lo[sj];
+        float dx, dy, dz, ex, ey, ez;
+        rel_coord(h.x, l.x, cref.x, dx, ex);
+        rel_coord(h.y, l.y, cref.y, dy, ey);
+        rel_coord(h.z, l.z, cref.z, dz, ez);
+        const float4 a = make_float4(dx, dy, dz, h.w);
+        const float4 b = make_float4(t.reff32[sj], t.rinv2[sj], __int_as_float((t.param[sj] & 0xffff) * nt), 0.0f);
+        sm_a[w][lane] = a;
+        sm_a[w][lane + 32] = a;
+        sm_b[w][lane] = b;
+        sm_b[w][lane + 32] = b;
+        if (any_close) {
+          const float4 c = make_float4(ex, ey, ez, __int_as_float(sj));
+          sm_e[w][lane] = c;
+          sm_e[w][lane + 32] = c;
+        }
       }
-      const unsigned cols = __ballot_sync(kFull, mycol != 0u);
+      const unsigned m_in = rotation_mask(mycol, lane);
+      const unsigned m_coul = __any_sync(kFull, myexc != 0u) ? m_in & ~rotation_mask(myexc, lane) : m_in;
+      // pairs that were within kClose + 1 A at the list build (not excluded)
+      const unsigned m_close = any_close ? rotation_mask(myclose, lane) : 0u;
       __syncwarp();
       float fix = 0, fiy = 0, fiz = 0, sdi = 0, ep = 0, ee = 0, ev = 0;
-      float jx = 0, jy = 0, jz = 0, jsd = 0;
+      float jx = 0, jy = 0, jz = 0, jsd = 0;  // j-side sums of the entry this lane meets
+      // the 32 steps of the rotation; CLOSE: the chunk holds pairs that may
+      // be closer than kClose now, whose Coulomb and Lennard-Jones terms
+      // then go to close_pair (FP64) instead of the FP32 sums
+      auto steps = [&](auto close_tag) {
+        constexpr bool CLOSE = decltype(close_tag)::value;
 #pragma unroll 1
-      for (int g = 0; g < 32 / kGroupPair; g++) {
-        float ax[kGroupPair], ay[kGroupPair], az[kGroupPair], as[kGroupPair];
+        for (int g = 0; g < 32; g += 8) {
+          const unsigned gin = m_in >> g, gcoul = m_coul >> g, gclose = m_close >> g;
+          const float4 *pa = &sm_a[w][lane + g];
+          const float4 *pb = &sm_b[w][lane + g];
 #pragma unroll
-        for (int s = 0; s < kGroupPair; s++) {
-          const int j = g * kGroupPair + s;
-          ax[s] = ay[s] = az[s] = as[s] = 0.0f;
-          if (!((cols >> j) & 1u)) continue;  // padding entry
-          const float4 h = sm_hi[w][j], l = sm_lo[w][j];
-          const uint4 au = sm_aux[w][j];
-          const float dx = (xi - h.x) + (xli - l.x);
-          const float dy = (yi - h.y) + (yli - l.y);
-          const float dz = (zi - h.z) + (zli - l.z);
-          const float r2 = fmaf(dx, dx, fmaf(dy, dy, dz * dz));
-          const bool in = (au.z >> lane) & 1u;
-          const bool coul = in && !((au.w >> lane) & 1u);
-          // row type_j: the lanes' i types fall in one row of the symmetric table
+          for (int u = 0; u < 8; u++) {
+            const float4 a = pa[u], b = pb[u];
+            const bool in = (gin >> u) & 1u;
+            bool coul = (gcoul >> u) & 1u;
+            const float dx = (xi - a.x) + xil;
+            const float dy = (yi - a.y) + yil;
+            const float dz = (zi - a.z) + zil;
+            // a lane off the list gets r2 = 1 and zero charges and
+            // coefficients (the self pair of a diagonal tile has r2 = 0), so
+            // its terms are exact zeros
+            const float r2 = in ? fmaf(dx, dx, fmaf(dy, dy, dz * dz)) : 1.0f;
+            bool cl = false;
+            if (CLOSE) {
+              cl = ((gclose >> u) & 1u) && r2 < kClose * kClose;
+              coul = coul && !cl;
+            }
+            const float qij = qi * a.w;
+            const float qq = in ? qij : 0.0f;
+            const float qc = coul ? qij : 0.0f;
+            float lja, ljb;
+            if (LJS) {
+              const float2 ab = s_lj[SFFG_IDX(coul ? __float_as_int(b.z) + lj_i : zero_lj, t.lj_n + 1, kCheckLj)];
+              lja = ab.x;
+              ljb = ab.y;
+            } else {
 #ifdef SFFG_CHECKED
-          const float2 ab = lj_all[SFFG_IDX(static_cast<int>(lj - lj_all) + static_cast<int>(au.y) + ti, t.lj_n,
-                                            kCheckLj)];
+              const float2 ab = t.lj[SFFG_IDX(static_cast<int>(lj - t.lj) + __float_as_int(b.z) + lj_i, t.lj_n,
+                                              kCheckLj)];
 #else
-          const float2 ab = lj[au.y + ti];
+              const float2 ab = lj[__float_as_int(b.z) + lj_i];
 #endif
-          // a lane off the list gets zero charge and coefficients (and r2 = 1:
-          // the self pair of a diagonal tile has r2 = 0), hence zero terms
-          const float qq = in ? qi * h.w : 0.0f;
-          const PairOut o = gb_pair<KAPPA>(t.pair, in ? r2 : 1.0f, qq, coul ? qq : 0.0f, ri, l.w, rvi,
-                                           __uint_as_float(au.x), coul ? ab.x : 0.0f, coul ? ab.y : 0.0f);
-          const float de = o.de;
-          fix = fmaf(de, dx, fix);
-          fiy = fmaf(de, dy, fiy);
-          fiz = fmaf(de, dz, fiz);
-          ax[s] = -de * dx;
-          ay[s] = -de * dy;
-          az[s] = -de * dz;
-          sdi += o.sd_i;
-          as[s] = o.sd_j;
-          ep += o.epol;
-          ee += o.eel;
-          ev += o.evdw;
+              lja = coul ? ab.x : 0.0f;
+              ljb = coul ? ab.y : 0.0f;
+            }
+            // generalized Born (eff.c:1924-1987)
+            const float rb2 = ri * b.x;
+            const float efac = ex2_ftz(-r2 * (rvi * b.y));
+            const float f2 = fmaf(rb2, efac, r2);
+            const float fgbi = rsqrt_ftz(f2);
+            const float temp4 = fgbi * fgbi * fgbi;
+            float de, temp5;
+            if (KAPPA) {
+              const float fgbk = -t.pair.kappa_s * (f2 * fgbi);
+              const float expmkf = expf(fgbk) * t.pair.inv_epsext;
+              const float dfac = 1.0f - expmkf;
+              const float temp6 = qq * temp4 * (dfac + fgbk * expmkf);
+              ep = fmaf(qq * dfac, fgbi, ep);
+              de = temp6 * fmaf(-0.25f, efac, 1.0f);
+              temp5 = efac * temp6 * fmaf(0.25f, r2, rb2);
+            } else {
+              // dielfac factored out of temp6 (into de below, and into the
+              // energy and sumdeijda scales)
+              const float temp6 = qq * temp4;
+              ep = fmaf(qq, fgbi, ep);
+              de = dielfac * (temp6 * fmaf(-0.25f, efac, 1.0f));
+              temp5 = efac * temp6 * fmaf(0.25f, r2, rb2);
+            }
+            sdi += temp5;
+            // Coulomb and Lennard-Jones (eff.c:2004-2025), zero for excluded
+            // and close pairs
+            const float rinv = rsqrt_ftz(r2);
+            const float r2inv = rinv * rinv;
+            const float eel = qc * rinv;
+            const float r6inv = r2inv * r2inv * r2inv;
+            const float f6 = ljb * r6inv;
+            const float f12 = lja * (r6inv * r6inv);
+            ee += eel;
+            ev += f12 - f6;
+            de = fmaf(-fmaf(12.0f, f12, fmaf(-6.0f, f6, eel)), r2inv, de);
+            fix = fmaf(de, dx, fix);
+            fiy = fmaf(de, dy, fiy);
+            fiz = fmaf(de, dz, fiz);
+            jx = fmaf(-de, dx, jx);
+            jy = fmaf(-de, dy, jy);
+            jz = fmaf(-de, dz, jz);
+            jsd += temp5;
+            if (CLOSE) {
+              if (__any_sync(kFull, cl)) {
+                if (cl) close_pair(a, b, sm_e[w][lane + g + u]);
+              }
+            }
+            // hand the entry's sums to the lane that meets it next
+            jx = __shfl_sync(kFull, jx, next);
+            jy = __shfl_sync(kFull, jy, next);
+            jz = __shfl_sync(kFull, jz, next);
+            jsd = __shfl_sync(kFull, jsd, next);
+          }
         }
-        jx += reduce_to_lane(ax, g, lane);
-        jy += reduce_to_lane(ay, g, lane);
-        jz += reduce_to_lane(az, g, lane);
-        jsd += reduce_to_lane(as, g, lane);
-      }
+      };
+      if (any_close) steps(std::true_type());
+      else steps(std::false_type());
       fx64 += to_fixed(fix, FS);
       fy64 += to_fixed(fiy, FS);
       fz64 += to_fixed(fiz, FS);
-      sd64 += to_fixed(sdi, FS);
-      ep64 += to_fixed(ep, FS);
+      sd64 += to_fixed(sdi * (sd_scale * ri), FS);
+      ep64 += to_fixed(ep * ep_scale, FS);
       ee64 += to_fixed(ee, FS);
       ev64 += to_fixed(ev, FS);
+      // after 32 hand-overs lane e holds entry e's sums
       if (mycol) {
         atomic_add_ll(&t.acc_fx[sj], to_fixed(jx, FS));
         atomic_add_ll(&t.acc_fy[sj], to_fixed(jy, FS));
         atomic_add_ll(&t.acc_fz[sj], to_fixed(jz, FS));
-        atomic_add_ll(&t.acc_sd[sj], to_fixed(jsd, FS));
+        atomic_add_ll(&t.acc_sd[sj], to_fixed(jsd * (sd_scale * sm_b[w][lane].x), FS));
       }
       __syncwarp();
     }
@@ -585,11 +842,17 @@ __global__ void __launch_bounds__(256, 3) k_gbpair(const DevTables t) {
 }
 
 // ------------------------------------------------------------------ pass 3
-// Chain rule through the Born radii (src/sff/eff.c:2241-2395) over lists B
-// and C: for each pair within rgbmax + Fsmax, g = sumda_i d_ij +
+// Chain rule through the Born radii (src/sff/eff.c:2241-2395) over lists
+// B and C: for each pair within rgbmax + Fsmax, g = sumda_i d_ij +
 // sumda_j d_ji, f_i -= g r_ij, f_j += g r_ij.
 template <bool NECK>
 __global__ void __launch_bounds__(256, 3) k_chain(const DevTables t) {
+  // far-field chunks (list B): per warp the entries twice, (x, y, z
+  // relative to the i-tile's reference point, s) and (s correction, s^2,
+  // sumda, rborn); the neck index apart
+  __shared__ float4 sm_a[8][64], sm_b[8][64];
+  __shared__ int sm_nk[NECK ? 8 : 1][64];
+  // near-field chunks (list C)
   __shared__ float4 sm_hi[8][32], sm_lo[8][32], sm_gb[8][32];  // j entries (lo.w = sumda)
   __shared__ float4 si_hi[8][32], si_lo[8][32], si_gb[8][32];  // the i-tile (lo.w = sumda)
   __shared__ unsigned sm_col[8][32];
@@ -606,8 +869,11 @@ __global__ void __launch_bounds__(256, 3) k_chain(const DevTables t) {
   const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
   const int nB = *t.lb.nchunk, nC = *t.lc.nchunk, nitem = nB + nC;
   const float FS = 4294967296.0f;
+  const float rgbmax = t.born.rgbmax;
+  const int next = (lane + 1) & 31;
   int cur_I = -1;
-  float xi = 0, yi = 0, zi = 0, xli = 0, yli = 0, zli = 0, si = 0, rbi = 0, sci = 0, sdai = 0;
+  float3 cref = make_float3(0.f, 0.f, 0.f);
+  float xi = 0, yi = 0, zi = 0, xil = 0, yil = 0, zil = 0, si = 0, si2 = 0, rbi = 0, sci = 0, sdai = 0;
   int nki = 0;
   long long fx64 = 0, fy64 = 0, fz64 = 0;
   auto flush_i = [&]() {
@@ -622,66 +888,87 @@ __global__ void __launch_bounds__(256, 3) k_chain(const DevTables t) {
     atomic_add_ll(&t.acc_fz[sj], to_fixed(jz, FS));
   };
 
+  // list B chunk k, rotation schedule
   auto far_chunk = [&](int k) {
-    unsigned mycol;
-    const int sj = chunk_entry(t.lb, k, lane, mycol, t.nslot);
+    const size_t e = static_cast<size_t>(k) * 32 + lane;
+    const unsigned mycol = t.lb.col[e];
+    const int sj = SFFG_IDX(t.lb.slot[e], t.nslot, kCheckSlot);
     {
-      float4 l = t.pos_lo[sj];
-      l.w = t.sumda32[sj];
-      sm_hi[w][lane] = t.pos_hi[sj];
-      sm_lo[w][lane] = l;
-      float4 gq = t.gbpar[sj];
-      gq.x = __uint_as_float(mycol);  // the column mask, as in pass 1
-      sm_gb[w][lane] = gq;
-      if (NECK) sm_par[w][lane] = t.param[sj];
+      const float4 h = t.pos_hi[sj], l = t.pos_lo[sj], g = t.gbpar[sj];
+      float dx, dy, dz, ex, ey, ez;
+      rel_coord(h.x, l.x, cref.x, dx, ex);
+      rel_coord(h.y, l.y, cref.y, dy, ey);
+      rel_coord(h.z, l.z, cref.z, dz, ez);
+      const float4 a = make_float4(dx, dy, dz, g.y);
+      const float4 b = make_float4(g.w, g.y * g.y, t.sumda32[sj], g.z);
+      sm_a[w][lane] = a;
+      sm_a[w][lane + 32] = a;
+      sm_b[w][lane] = b;
+      sm_b[w][lane + 32] = b;
+      if (NECK) {
+        const int nk = (t.param[sj] >> 16) & 0xff;
+        sm_nk[NECK ? w : 0][lane] = nk;
+        sm_nk[NECK ? w : 0][lane + 32] = nk;
+      }
     }
-    const unsigned cols = __ballot_sync(kFull, mycol != 0u);
+    const unsigned m_in = rotation_mask(mycol, lane);
     __syncwarp();
     float fix = 0, fiy = 0, fiz = 0, jx = 0, jy = 0, jz = 0;
 #pragma unroll 1
-    for (int g = 0; g < 32 / kGroup; g++) {
-      float ax[kGroup], ay[kGroup], az[kGroup];
+    for (int g = 0; g < 32; g += 4) {
+      const unsigned gin = m_in >> g;
+      const float4 *pa = &sm_a[w][lane + g];
+      const float4 *pb = &sm_b[w][lane + g];
 #pragma unroll
-      for (int s = 0; s < kGroup; s++) {
-        const int j = g * kGroup + s;
-        ax[s] = ay[s] = az[s] = 0.0f;
-        if (!((cols >> j) & 1u)) continue;
-        const float4 h = sm_hi[w][j], l = sm_lo[w][j], gp = sm_gb[w][j];
-        const float dx = (xi - h.x) + (xli - l.x);
-        const float dy = (yi - h.y) + (yli - l.y);
-        const float dz = (zi - h.z) + (zli - l.z);
-        const float r2 = fmaf(dx, dx, fmaf(dy, dy, dz * dz));
-        const bool in = ((__float_as_uint(gp.x) >> lane) & 1u) && r2 <= t.born.cutoff2;
-        if (!__any_sync(kFull, in)) continue;
-        // the hardware rsqrt alone: pass 3 only shapes the forces, whose RMS
-        // error against FP64 it leaves at 4.70e-6 (to 3 digits) for -2% time
-        const float dij1i = rsqrt_fast(r2);
-        const float dij = r2 * dij1i;
-        float di, dj;
-        descreen_pair<true>(t.born, in, dij, dij1i, si, gp.y, di, dj);
-        di = fmaf(di, gp.w, di);
+      for (int u = 0; u < 4; u++) {
+        const float4 a = pa[u];
+        const float4 b = pb[u];
+        const bool in = (gin >> u) & 1u;
+        const float dx = (xi - a.x) + xil;
+        const float dy = (yi - a.y) + yil;
+        const float dz = (zi - a.z) + zil;
+        float r2 = fmaf(dx, dx, fmaf(dy, dy, dz * dz));
+        // off the list, or beyond rgbmax + Fsmax, where the reference skips
+        // the pair (eff.c:2263)
+        r2 = in && r2 <= t.born.cutoff2 ? r2 : kOffList;
+        // the hardware rsqrt alone: pass 3 only shapes the forces
+        const float d1 = rsqrt_ftz(r2);
+        const float d2i = d1 * d1;
+        float di = far_deriv2(d2i, a.w, b.y);
+        float dj = far_deriv2(d2i, si, si2);
+        const float dij = r2 * d1;
+        {
+          const bool qi_ = dij > rgbmax - a.w, qj_ = dij > rgbmax - si;
+          if (__any_sync(kFull, qi_ || qj_)) {
+            const float vi = tail_closed<true>(t.born, dij, d1, a.w);
+            const float vj = tail_closed<true>(t.born, dij, d1, si);
+            di = qi_ ? vi : di;
+            dj = qj_ ? vj : dj;
+          }
+          di = dij > rgbmax + a.w ? 0.0f : di;
+          dj = dij > rgbmax + si ? 0.0f : dj;
+        }
+        di = fmaf(di, b.x, di);
         dj = fmaf(dj, sci, dj);
         if (NECK) {
-          const bool nk = in && dij < rbi + gp.z + 6.8f;
+          const bool nk = dij < rbi + b.w + 6.8f;
           if (__any_sync(kFull, nk)) {
-            const int nkj = (sm_par[w][j] >> 16) & 0xff;
-            const float a = neck_deriv(dij, s_npos[SFFG_IDX(nki * 21 + nkj, 441, kCheckNeck)], s_nval[SFFG_IDX(nki * 21 + nkj, 441, kCheckNeck)], t.neck_scale);
-            const float b = neck_deriv(dij, s_npos[SFFG_IDX(nkj * 21 + nki, 441, kCheckNeck)], s_nval[SFFG_IDX(nkj * 21 + nki, 441, kCheckNeck)], t.neck_scale);
-            di += nk ? a : 0.0f;
-            dj += nk ? b : 0.0f;
+            const int nkj = sm_nk[NECK ? w : 0][lane + g + u];
+            const int ij = SFFG_IDX(nki * 21 + nkj, 441, kCheckNeck), ji = SFFG_IDX(nkj * 21 + nki, 441, kCheckNeck);
+            const float na = neck_deriv(dij, s_npos[ij], s_nval[ij], t.neck_scale);
+            const float nb = neck_deriv(dij, s_npos[ji], s_nval[ji], t.neck_scale);
+            di += nk ? na : 0.0f;
+            dj += nk ? nb : 0.0f;
           }
         }
-        const float gg = in ? fmaf(sdai, di, l.w * dj) : 0.0f;
+        const float gg = fmaf(sdai, di, b.z * dj);
         fix = fmaf(-gg, dx, fix);
         fiy = fmaf(-gg, dy, fiy);
         fiz = fmaf(-gg, dz, fiz);
-        ax[s] = gg * dx;
-        ay[s] = gg * dy;
-        az[s] = gg * dz;
+        jx = __shfl_sync(kFull, fmaf(gg, dx, jx), next);
+        jy = __shfl_sync(kFull, fmaf(gg, dy, jy), next);
+        jz = __shfl_sync(kFull, fmaf(gg, dz, jz), next);
       }
-      jx += reduce_to_lane(ax, g, lane);
-      jy += reduce_to_lane(ay, g, lane);
-      jz += reduce_to_lane(az, g, lane);
     }
     fx64 += to_fixed(fix, FS);
     fy64 += to_fixed(fiy, FS);
@@ -764,8 +1051,11 @@ __global__ void __launch_bounds__(256, 3) k_chain(const DevTables t) {
         const float4 h = t.pos_hi[sl], g = t.gbpar[sl];
         float4 l = t.pos_lo[sl];
         const int pr = t.param[sl];
-        xi = h.x; yi = h.y; zi = h.z; xli = l.x; yli = l.y; zli = l.z;
-        si = g.y; rbi = g.z; sci = g.w;
+        cref = tile_ref(t.box_lo, t.box_hi, I);
+        rel_coord(h.x, l.x, cref.x, xi, xil);
+        rel_coord(h.y, l.y, cref.y, yi, yil);
+        rel_coord(h.z, l.z, cref.z, zi, zil);
+        si = g.y; si2 = g.y * g.y; rbi = g.z; sci = g.w;
         sdai = t.sumda32[sl];
         nki = (pr >> 16) & 0xff;
         l.w = sdai;

@@ -12,7 +12,10 @@
 //
 // Three lists share one build:
 //   list A, pairs with r < cut: pass 2 (GB + Coulomb + LJ) -- exactly the
-//           reference's list, rebuilt every nsnb evaluations;
+//           reference's list, rebuilt every nsnb evaluations; its entries
+//           also mark the non-excluded pairs closer than kClose + 1 A, whose
+//           Coulomb and Lennard-Jones terms pass 2 takes in FP64 once they
+//           are closer than kClose;
 //   lists B and C, the pairs of list A with r < rgbmax + Fsmax + skin:
 //           passes 1 and 3 (Born radii and chain rule), which the reference
 //           runs over list A skipping pairs beyond rgbmax + Fsmax at every
@@ -24,7 +27,11 @@
 //           soon as one of its atoms has moved more than skin / 3 since its
 //           last remake, so every pair of list A within rgbmax + Fsmax now
 //           is on B or C, and no pair of list B has come within
-//           4 max(s_i, s_j).
+//           4 max(s_i, s_j).  (Splitting list B at rgbmax - Fsmax into pairs
+//           that never reach the smooth rgbmax tail and pairs that can was
+//           tried: half of list B's j-atoms have pairs on both sides, so the
+//           two lists held 1.5 times the lane-steps of one, 27% of them
+//           busy in the tail list, which needs the tail form throughout.)
 //
 // Build stages (one launch each):
 //   1 candidates   warp per i-tile: tile pairs (I, J >= I) whose bounding
@@ -69,13 +76,14 @@ struct ListArgs {
   int ntile;
   float cut2f;   // cut^2 (list A), FP32
   double cut2;   // cut^2, exact FP64 decision for borderline pairs
-  float gbb2f;   // (rgbmax + Fsmax + skin)^2 (list B)
+  float gbb2f;   // (rgbmax + Fsmax + skin)^2 (lists B and C)
+  float close2f; // (kClose + 1 A)^2: list A's possibly close pairs
   // candidates
   int2 *cand;
   int cand_cap;
   int *ncand, *overflow;
   int *cand_start, *cand_count;  // per i-tile
-  unsigned *colA, *colB, *colC, *colE;  // per candidate x 32 lanes
+  unsigned *colA, *colB, *colC, *colE, *colK;  // per candidate x 32 lanes
   int4 *cand_n;                  // entries of (A, B, C) per candidate
   int4 *cand_off;                // their offsets within the i-tile
   int *chunksA, *chunksB, *chunksC;  // per i-tile
@@ -83,7 +91,7 @@ struct ListArgs {
   int *nchunkA, *nchunkB, *nchunkC;
   // the lists
   int *chunkA_i, *entA_slot;
-  unsigned *entA_col, *entA_exc;
+  unsigned *entA_col, *entA_exc, *entA_close;
   int *chunkB_i, *entB_slot;
   unsigned *entB_col;
   int *chunkC_i, *entC_slot;
@@ -151,8 +159,8 @@ __global__ void k_list_candidates(const ListArgs a) {
 // list A: r^2 < cut^2, decided in FP64 from the double coordinates when
 // the FP32 distance is within 1e-5 of the cutoff, as the reference decides
 // (nblist.c:726-746); upper triangle within a tile; no pair of two frozen
-// atoms.  Lists B and C: list A pairs with r^2 < (rgbmax + Fsmax + skin)^2,
-// on C when r < 4 max(s_i, s_j) + skin, else on B.
+// atoms.  Lists B and C: list A pairs with r^2 < (rgbmax + Fsmax +
+// skin)^2, on C when r < 4 max(s_i, s_j) + skin, else on B.
 // GB_ONLY: list A stays as built; lists B and C are remade from its
 // columns.
 template <bool GB_ONLY>
@@ -209,7 +217,7 @@ __global__ void k_list_columns(const ListArgs a) {
   const bool has_ex = __any_sync(kFull, exrow != 0u);
   __syncwarp();
   const unsigned prevA = GB_ONLY ? a.colA[static_cast<size_t>(c) * 32 + lane] : 0u;
-  unsigned colA = 0, colB = 0, colC = 0, colE = 0;
+  unsigned colA = 0, colB = 0, colC = 0, colE = 0, colK = 0;
   const float gbb = a.gbb2f * 1.0001f + 1e-3f;
   // rows to test (warp-uniform): every valid i-atom, or for a remake only
   // those with a list-A pair in this tile pair
@@ -245,7 +253,11 @@ __global__ void k_list_columns(const ListArgs a) {
         in = ddx * ddx + ddy * ddy + ddz * ddz < a.cut2;
       }
       in = in && vj && !(I == J && i >= lane) && !(((frzI >> i) & 1u) && frzj);
-      if (has_ex) colE |= ((s_ex[w][i] >> lane) & 1u) << i;
+      const unsigned exb = has_ex ? (s_ex[w][i] >> lane) & 1u : 0u;
+      colE |= exb << i;
+      // a non-excluded pair this close may come within kClose before the
+      // next build; pass 2 checks those pairs' distance at every evaluation
+      colK |= static_cast<unsigned>(in && !exb && r2 < a.close2f) << i;
     }
     const float nr = 4.0f * fmaxf(s_s[w][i], sjs) + kListSkin;
     const bool gb = in && r2 < gbb, near = r2 < nr * nr * 1.0001f;
@@ -257,6 +269,7 @@ __global__ void k_list_columns(const ListArgs a) {
   if (!GB_ONLY) {
     a.colA[e] = colA;
     a.colE[e] = colE;
+    a.colK[e] = colK;
   }
   a.colB[e] = colB;
   a.colC[e] = colC;
@@ -372,6 +385,7 @@ __global__ void k_list_fill(const ListArgs a) {
       a.entA_slot[pos] = p.y * 32 + lane;
       a.entA_col[pos] = col;
       a.entA_exc[pos] = a.colE[e];
+      a.entA_close[pos] = a.colK[e];
     }
   }
   {
@@ -425,7 +439,10 @@ __global__ void k_list_pad(const ListArgs a) {
       const size_t pos = static_cast<size_t>(ch0) * 32 + k;
       slot[pos] = I * 32;
       col[pos] = 0u;
-      if (list == 0) a.entA_exc[pos] = 0u;
+      if (list == 0) {
+        a.entA_exc[pos] = 0u;
+        a.entA_close[pos] = 0u;
+      }
     }
     for (int k = lane; k < nch; k += 32) owner[ch0 + k] = I;
   }

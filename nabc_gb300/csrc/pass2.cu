@@ -4,7 +4,7 @@
 namespace sffg {
 
 void launch_gbpair(bool kappa, int grid, cudaStream_t st, const DevTables &t) {
-  const bool ljs = t.lj_shared && t.lj_n <= kLjShared;
+  const bool ljs = t.lj_shared && t.lj_n <= kLjShared;  // one more entry: the zero one
   if (kappa) {
     if (ljs) launch_pdl(k_gbpair<true, true>, grid, 256, st, t);
     else launch_pdl(k_gbpair<true, false>, grid, 256, st, t);

@@ -189,6 +189,7 @@ struct HostSystem {
   std::vector<int> neck, type, frozen;
   int ntypes = 0;
   std::vector<float> lj_a, lj_b;          // ntypes^2, zero where no 6-12 term
+  std::vector<double> lj_a64, lj_b64;     // the same in FP64 (close pairs)
   std::vector<std::pair<int, int>> excl;  // excluded pairs i<j (Coulomb/LJ only)
   struct Bond { int a, b; double rk, req; };
   struct Angle { int a, b, c; double tk, teq; };

@@ -113,6 +113,8 @@ void build_host_system(PARMSTRUCT_T *prm, const int *frozen, const Options &o, b
   hs.ntypes = prm->Ntypes;
   hs.lj_a.assign(static_cast<size_t>(prm->Ntypes) * prm->Ntypes, 0.0f);
   hs.lj_b.assign(static_cast<size_t>(prm->Ntypes) * prm->Ntypes, 0.0f);
+  hs.lj_a64.assign(static_cast<size_t>(prm->Ntypes) * prm->Ntypes, 0.0);
+  hs.lj_b64.assign(static_cast<size_t>(prm->Ntypes) * prm->Ntypes, 0.0);
   // the pair kernel reads row type_j, column type_i, which is the
   // reference's row type_i (eff.c:1915, 2015) when the index is symmetric, as
   // Amber's NONBONDED_PARM_INDEX is by construction
@@ -126,6 +128,8 @@ void build_host_system(PARMSTRUCT_T *prm, const int *frozen, const Options &o, b
       if (ic >= 0) {
         hs.lj_a[a * prm->Ntypes + b] = static_cast<float>(prm->Cn1[ic]);
         hs.lj_b[a * prm->Ntypes + b] = static_cast<float>(prm->Cn2[ic]);
+        hs.lj_a64[a * prm->Ntypes + b] = prm->Cn1[ic];
+        hs.lj_b64[a * prm->Ntypes + b] = prm->Cn2[ic];
       }
     }
   // Exclusions: row i marks the listed atoms j > i (1-based, 0 = none); the

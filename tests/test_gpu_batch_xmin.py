@@ -80,9 +80,12 @@ def test_single_system_batch_equals_solo(lib, checks, opts):
 @pytest.mark.parametrize("opts", CASES)
 def test_mixed_batch_deterministic_and_close_to_solo(lib, checks, opts):
     """Three systems together: two runs give the same bits; each system's
-    final energy is within 1e-5 relative of its lone run for PRCG and
-    L-BFGS (measured: about 1e-6 after 40 L-BFGS iterations, the growth of
-    FP32 rounding along a minimisation).  TNCG's truncated CG amplifies any
+    final energy is within 1e-5 relative of its lone run for L-BFGS
+    (measured: about 1e-6 after 40 iterations, the growth of FP32 rounding
+    along a minimisation).  PRCG's conjugate directions carry a rounding
+    difference further: its runs are required to end within 5e-4 (measured:
+    1.0e-4 apart after 25 iterations; run on to a gradient of 0.1 the two
+    paths ended in different nearby minima of xfin, 7e-5 apart).  TNCG's truncated CG amplifies any
     rounding difference into another path (its Hessian products are finite
     differences of gradients), so for it the runs are only required to end
     within 3% of each other, both far below the start (measured: 1.1%, the
@@ -104,7 +107,7 @@ def test_mixed_batch_deterministic_and_close_to_solo(lib, checks, opts):
     for s, (prm, x, frozen) in enumerate(sysl):
         ret, xs, iters, err = solo_xmin(prm, x.copy(), frozen, **opts)
         assert st[s] == err == 0
-        tol = 3e-2 if opts["method"] == 3 else 1e-5
+        tol = {1: 5e-4, 2: 1e-5, 3: 3e-2}[opts["method"]]
         assert abs(en[s] - ret) <= tol * abs(ret)
 
 
