@@ -289,6 +289,21 @@ int sffg_server_destroy(sffg_server *s);
 int sffg_born_radii_static(int natom, const double *x, const double *rborn, const double *fs, int gb,
                            double rgbmax, double *reff, void *stream);
 
+/* ---- pair-list builds ---------------------------------------------------- */
+
+/* Pair-list rebuilds inside device-resident md (sffg_batch_md,
+ * sffg_batch_md_steps, md requests of the server) and inside mme() launch
+ * all their stages without reading counts back to the host: the list
+ * stores keep 50% headroom over the last build's counts and the stages
+ * check the stores' capacities on the device.  When a store proves too
+ * small (the pairs grew by more than the headroom between two rebuilds),
+ * mme() redoes its evaluation with the stores sized exactly, and md
+ * replays the steps since that rebuild from a snapshot of the state it
+ * started from, before any result is read; the results are the ones an
+ * exactly sized build gives.  Returns how many rebuilds of this process
+ * were redone that way. */
+long long sffg_list_overflows(void);
+
 /* ---- checked build ------------------------------------------------------ */
 
 /* A library built with -DSFFG_CHECKED (for example SFFG_NVCC_EXTRA=

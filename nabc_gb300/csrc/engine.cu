@@ -3,6 +3,7 @@
 #include <cuda_runtime.h>
 
 #include <algorithm>
+#include <atomic>
 #include <cmath>
 #include <cstring>
 #include <map>
@@ -55,6 +56,12 @@ struct DeviceState {
   // the FP32 pair passes (fork after the pack, join before the gather)
   cudaStream_t side = nullptr;
   cudaEvent_t fork_ev = nullptr, join_ev = nullptr;
+  // a queued list build's counters (pinned) and the event after their copy
+  int *list_host = nullptr;
+  cudaEvent_t list_ev = nullptr;
+  // md replay snapshot
+  DBuf<double> ck_x, ck_v, ck_accel, ck_tscal;
+  DBuf<long long> ck_ekin_last;
   int nsm = 0;
   cudaEvent_t tune_ev[3][2] = {};  // pass timing while the work split is tuned
   // per slot
@@ -132,6 +139,9 @@ struct DeviceState {
         for (auto &e : pe)
           if (e) cudaEventDestroy(e);
     if (fork_ev) cudaEventDestroy(fork_ev);
+    if (list_ev) cudaEventDestroy(list_ev);
+    if (list_host) cudaFreeHost(list_host);
+    ck_x.release(); ck_v.release(); ck_accel.release(); ck_tscal.release(); ck_ekin_last.release();
     if (join_ev) cudaEventDestroy(join_ev);
     if (side) cudaStreamDestroy(side);
     if (stream) cudaStreamDestroy(stream);
@@ -163,6 +173,13 @@ struct DeviceState {
       last_error = std::string(#call) + ": " + cudaGetErrorString(e_);              \
       return SFFG_ECUDA;                                                            \
     }                                                                               \
+  } while (0)
+
+// Settles a queued list build first (see Batch::settle).
+#define SFFG_SETTLE(stream)                      \
+  do {                                           \
+    const int settle_rc_ = settle(stream);       \
+    if (settle_rc_ != SFFG_OK) return settle_rc_; \
   } while (0)
 
 Batch::Batch(const Options &opts) : opts_(opts), mp_(model_from_options(opts)) {}
@@ -598,6 +615,7 @@ static cudaStream_t pick(DeviceState &d, void *stream) {
 }
 
 int Batch::set_coords(int s, const double *x, void *stream) {
+  SFFG_SETTLE(stream);
   if (!finalized_ || s < 0 || s >= num_systems()) return SFFG_EINVAL;
   const SystemInfo &si = sys_[s];
   cudaStream_t st = pick(*d_, stream);
@@ -622,16 +640,19 @@ static int copy_out(Batch &b, DeviceState &d, double *dev, int s, double *host, 
 }
 
 int Batch::get_coords(int s, double *x, void *stream) {
+  SFFG_SETTLE(stream);
   if (!finalized_ || s < 0 || s >= num_systems()) return SFFG_EINVAL;
   return copy_out(*this, *d_, d_->x.p, s, x, 3, stream, last_error);
 }
 
 int Batch::get_grad(int s, double *g, void *stream) {
+  SFFG_SETTLE(stream);
   if (!finalized_ || s < 0 || s >= num_systems()) return SFFG_EINVAL;
   return copy_out(*this, *d_, d_->grad.p, s, g, 3, stream, last_error);
 }
 
 int Batch::set_velocities(int s, const double *v, void *stream) {
+  SFFG_SETTLE(stream);
   if (!finalized_ || s < 0 || s >= num_systems()) return SFFG_EINVAL;
   const SystemInfo &si = sys_[s];
   SFFG_CK(cudaMemcpyAsync(d_->v.p + 3 * static_cast<size_t>(si.atom_off), v, 3 * sizeof(double) * si.natom,
@@ -640,11 +661,13 @@ int Batch::set_velocities(int s, const double *v, void *stream) {
 }
 
 int Batch::get_velocities(int s, double *v, void *stream) {
+  SFFG_SETTLE(stream);
   if (!finalized_ || s < 0 || s >= num_systems()) return SFFG_EINVAL;
   return copy_out(*this, *d_, d_->v.p, s, v, 3, stream, last_error);
 }
 
 int Batch::get_reff(int s, double *reff, void *stream) {
+  SFFG_SETTLE(stream);
   if (!finalized_ || s < 0 || s >= num_systems()) return SFFG_EINVAL;
   const SystemInfo &si = sys_[s];
   std::vector<double> r(static_cast<size_t>(si.ntile) * 32);
@@ -674,6 +697,7 @@ static void ene_from_fixed(const long long *e, double *ene) {
 }
 
 int Batch::get_energy(int s, double *ene, void *stream) {
+  SFFG_SETTLE(stream);
   if (!finalized_ || s < 0 || s >= num_systems()) return SFFG_EINVAL;
   long long e[kEnergySlots];
   cudaStream_t st = pick(*d_, stream);
@@ -684,6 +708,7 @@ int Batch::get_energy(int s, double *ene, void *stream) {
 }
 
 int Batch::get_energy_grad(int s, double *ene, double *g, void *stream) {
+  SFFG_SETTLE(stream);
   if (!finalized_ || s < 0 || s >= num_systems()) return SFFG_EINVAL;
   const SystemInfo &si = sys_[s];
   long long e[kEnergySlots];
@@ -697,6 +722,7 @@ int Batch::get_energy_grad(int s, double *ene, double *g, void *stream) {
 }
 
 int Batch::set_all_coords(const double *x, void *stream) {
+  SFFG_SETTLE(stream);
   if (!finalized_) return SFFG_ESTATE;
   cudaStream_t st = pick(*d_, stream);
   SFFG_CK(cudaMemcpyAsync(d_->x.p, x, 3 * sizeof(double) * natom_total_, cudaMemcpyHostToDevice, st));
@@ -709,6 +735,7 @@ constexpr char kStateMagic[8] = {'S', 'F', 'F', 'G', 'M', 'D', '1', 0};
 }
 
 int Batch::save_state(const char *path, void *stream) {
+  SFFG_SETTLE(stream);
   if (!finalized_) return SFFG_ESTATE;
   DeviceState &d = *d_;
   cudaStream_t st = pick(d, stream);
@@ -736,6 +763,7 @@ int Batch::save_state(const char *path, void *stream) {
 }
 
 int Batch::load_state(const char *path, void *stream) {
+  SFFG_SETTLE(stream);
   if (!finalized_) return SFFG_ESTATE;
   DeviceState &d = *d_;
   cudaStream_t st = pick(d, stream);
@@ -767,6 +795,7 @@ int Batch::load_state(const char *path, void *stream) {
 }
 
 int Batch::system_status(std::vector<int> &status, void *stream) {
+  SFFG_SETTLE(stream);
   if (!finalized_) return SFFG_ESTATE;
   const int nsys = num_systems();
   std::vector<int> bad(nsys);
@@ -779,6 +808,7 @@ int Batch::system_status(std::vector<int> &status, void *stream) {
 }
 
 int Batch::set_all_active(const std::vector<int> &on, void *stream) {
+  SFFG_SETTLE(stream);
   if (!finalized_ || static_cast<int>(on.size()) != num_systems()) return SFFG_EINVAL;
   note_active(on);
   SFFG_CK(cudaMemcpyAsync(d_->sys_active.p, ones_.data(), ones_.size() * sizeof(int), cudaMemcpyHostToDevice,
@@ -787,6 +817,7 @@ int Batch::set_all_active(const std::vector<int> &on, void *stream) {
 }
 
 int Batch::get_all_energy_grad(std::vector<double> &out, double *grad, void *stream, std::vector<int> *status) {
+  SFFG_SETTLE(stream);
   if (!finalized_) return SFFG_ESTATE;
   const int nsys = num_systems();
   std::vector<long long> e(kEnergySlots * static_cast<size_t>(nsys));
@@ -807,6 +838,7 @@ int Batch::get_all_energy_grad(std::vector<double> &out, double *grad, void *str
 }
 
 int Batch::get_all_energies(std::vector<double> &out, void *stream) {
+  SFFG_SETTLE(stream);
   if (!finalized_) return SFFG_ESTATE;
   const int nsys = num_systems();
   std::vector<long long> e(kEnergySlots * static_cast<size_t>(nsys));
@@ -916,8 +948,10 @@ ListArgs Batch::list_args(double fsmax) {
   a.gbb2f = static_cast<float>(std::min(list_b_cut2(mp_, fsmax), 1e30));
   a.cand = d.cand.p;
   a.cand_cap = static_cast<int>(d.cand.n);
+  a.ent_cap = static_cast<int>(std::min<size_t>(d.entA_slot.n / 32, 0x7fffffff));
   a.ncand = d.counters.p + 0;
   a.overflow = d.counters.p + 1;
+  a.chunks_needed = d.counters.p + 12;
   a.cand_start = d.cand_start.p;
   a.cand_count = d.cand_count.p;
   a.colA = d.colA.p;
@@ -961,12 +995,17 @@ double Batch::fsmax_all() const {
   return f;
 }
 
-// Both pair lists from the current coordinates (lists.cuh, stages 1-6).
-// The host reads two counts back (candidates, chunks) to size the stores.
+// The pair lists from the current coordinates (lists.cuh, stages 1-6).
+// Synchronous form: the host reads two counts back (candidates, chunks) to
+// size the stores exactly; the first build, and any build asked to, takes
+// it.  Queued form (build_lists_queued), while queued_builds_ is set: no
+// host round trip.
 int Batch::build_lists(void *stream) {
   Range range("sffg list build");
   DeviceState &d = *d_;
   cudaStream_t st = pick(d, stream);
+  if (queued_builds_ && sized_ && !force_sync_build_) return build_lists_queued(st);
+  force_sync_build_ = false;
   const double fsmax = fsmax_all();
   const int tile_blocks = (ntile_ * 32 + 255) / 256;
   if (d.cand.n == 0) SFFG_CK(d.cand.alloc(static_cast<size_t>(std::min<long long>(cand_max_, 64LL * ntile_ + 1024))));
@@ -978,15 +1017,19 @@ int Batch::build_lists(void *stream) {
     launches_++;
     SFFG_CK(cudaMemcpyAsync(c, d.counters.p, sizeof(c), cudaMemcpyDeviceToHost, st));
     SFFG_CK(cudaStreamSynchronize(st));
-    if (!c[1]) break;
+    // the store keeps at least 25% headroom (the queued builds' margin):
+    // below it, it is grown to 150% of the count and the stage runs again
+    const long long keep = std::min<long long>(cand_max_, c[0] + c[0] / 4 + 512);
+    if (!c[1] && static_cast<long long>(d.cand.n) >= keep) break;
     if (attempt >= 3) {
       last_error = "pair list build did not fit";
       return SFFG_ENOMEM;
     }
-    SFFG_CK(d.cand.alloc(static_cast<size_t>(std::min<long long>(cand_max_, c[0] + c[0] / 4 + 1024))));
+    SFFG_CK(d.cand.alloc(static_cast<size_t>(std::min<long long>(cand_max_, c[0] + c[0] / 2 + 1024))));
   }
   ncand_ = c[0];
-  const size_t nc = std::max(1, ncand_);
+  // the column stores hold as many candidates as the candidate store
+  const size_t nc = std::max<size_t>(1, d.cand.n);
   SFFG_CK(ensure(d.colA, nc * 32));
   SFFG_CK(ensure(d.colB, nc * 32));
   SFFG_CK(ensure(d.colC, nc * 32));
@@ -996,7 +1039,8 @@ int Batch::build_lists(void *stream) {
   SFFG_CK(ensure(d.cand_off, nc));
   const int cand_blocks = static_cast<int>(std::min<long long>((static_cast<long long>(nc) * 32 + 255) / 256, 16LL * d.nsm));
   {
-    const ListArgs a = list_args(fsmax);
+    ListArgs a = list_args(fsmax);
+    a.ent_cap = 0x7fffffff;  // the entry stores are sized below, from the count
     k_list_columns<false><<<cand_blocks, 256, 0, st>>>(a);
     k_list_offsets<false><<<tile_blocks, 256, 0, st>>>(a);
     k_list_scan<false><<<1, 1024, 0, st>>>(a);
@@ -1007,8 +1051,10 @@ int Batch::build_lists(void *stream) {
   SFFG_CK(cudaMemcpyAsync(&nch, d.counters.p + 2, sizeof(int), cudaMemcpyDeviceToHost, st));
   SFFG_CK(cudaStreamSynchronize(st));
   // lists B and C are subsets of list A: the same capacity serves all
-  // three, also when B and C are remade later
-  const size_t ne = static_cast<size_t>(std::max(1, nch)) * 32;
+  // three, also when B and C are remade later; 25% headroom at least
+  // (below it, 50%), the queued builds' margin
+  const size_t keep_ne = static_cast<size_t>(nch + nch / 4 + 32) * 32;
+  const size_t ne = d.entA_slot.n >= keep_ne ? d.entA_slot.n : static_cast<size_t>(nch + nch / 2 + 64) * 32;
   SFFG_CK(ensure(d.entA_slot, ne));
   SFFG_CK(ensure(d.entA_col, ne));
   SFFG_CK(ensure(d.entA_exc, ne));
@@ -1030,7 +1076,155 @@ int Batch::build_lists(void *stream) {
   }
   have_list_ = true;
   list_builds_++;
+  last_ncand_ = ncand_;
+  last_nch_ = nch;
+  sized_ = true;
   return SFFG_OK;
+}
+
+// The queued form: the stores keep 50% headroom over the last known counts
+// (growing them here if need be), all six stages launch at once, and the
+// stages check the stores' capacities themselves (lists.cuh): a store too
+// small sets the overflow flag, and the lists come out empty.  The counters
+// then go to pinned host memory behind an event; resolve_list_check() reads
+// them.  Callers that queue a build check it before trusting the results
+// (eval_checked, md_steps).
+int Batch::build_lists_queued(cudaStream_t st) {
+  DeviceState &d = *d_;
+  const double fsmax = fsmax_all();
+  const int tile_blocks = (ntile_ * 32 + 255) / 256;
+  // grown (to 150% of the last count) only once the headroom falls below
+  // 25%: a store that moves frees the old one, which waits for the device,
+  // and every captured graph must be captured again
+  const long long keep_cand = std::min<long long>(cand_max_, last_ncand_ + last_ncand_ / 4 + 512);
+  if (static_cast<long long>(d.cand.n) < keep_cand)
+    SFFG_CK(d.cand.alloc(static_cast<size_t>(std::min<long long>(cand_max_, last_ncand_ + last_ncand_ / 2 + 1024))));
+  const size_t nc = std::max<size_t>(1, d.cand.n);
+  // the column stores hold as many candidates as the candidate store
+  SFFG_CK(ensure(d.colA, nc * 32));
+  SFFG_CK(ensure(d.colB, nc * 32));
+  SFFG_CK(ensure(d.colC, nc * 32));
+  SFFG_CK(ensure(d.colK, nc * 32));
+  SFFG_CK(ensure(d.colE, nc * 32));
+  SFFG_CK(ensure(d.cand_n, nc));
+  SFFG_CK(ensure(d.cand_off, nc));
+  const size_t keep_ne = static_cast<size_t>(last_nch_ + last_nch_ / 4 + 32) * 32;
+  const size_t ne = d.entA_slot.n >= keep_ne ? d.entA_slot.n : static_cast<size_t>(last_nch_ + last_nch_ / 2 + 64) * 32;
+  SFFG_CK(ensure(d.entA_slot, ne));
+  SFFG_CK(ensure(d.entA_col, ne));
+  SFFG_CK(ensure(d.entA_exc, ne));
+  SFFG_CK(ensure(d.entA_close, ne));
+  SFFG_CK(ensure(d.entB_slot, ne));
+  SFFG_CK(ensure(d.entB_col, ne));
+  SFFG_CK(ensure(d.chunkA_i, ne / 32));
+  SFFG_CK(ensure(d.chunkB_i, ne / 32));
+  SFFG_CK(ensure(d.entC_slot, ne));
+  SFFG_CK(ensure(d.entC_col, ne));
+  SFFG_CK(ensure(d.chunkC_i, ne / 32));
+  if (!d.list_ev) SFFG_CK(cudaEventCreateWithFlags(&d.list_ev, cudaEventDisableTiming));
+  if (!d.list_host) SFFG_CK(cudaHostAlloc(reinterpret_cast<void **>(&d.list_host), 16 * sizeof(int), cudaHostAllocDefault));
+  // the smallest store of each kind sets the capacity the stages check
+  ListArgs a = list_args(fsmax);
+  a.cand_cap = static_cast<int>(std::min({d.cand.n, d.cand_n.n, d.cand_off.n, d.colA.n / 32, d.colB.n / 32,
+                                          d.colC.n / 32, d.colK.n / 32, d.colE.n / 32}));
+  a.ent_cap = static_cast<int>(std::min({d.entA_slot.n, d.entA_col.n, d.entA_exc.n, d.entA_close.n, d.entB_slot.n,
+                                         d.entB_col.n, d.entC_slot.n, d.entC_col.n, d.chunkA_i.n * 32,
+                                         d.chunkB_i.n * 32, d.chunkC_i.n * 32}) / 32);
+  const int cand_blocks = static_cast<int>(std::min<long long>((static_cast<long long>(nc) * 32 + 255) / 256, 16LL * d.nsm));
+  SFFG_CK(cudaMemsetAsync(d.counters.p, 0, 2 * sizeof(int), st));
+  k_list_candidates<<<tile_blocks, 256, 0, st>>>(a);
+  launch_pdl(k_list_columns<false>, cand_blocks, 256, st, a);
+  launch_pdl(k_list_offsets<false>, tile_blocks, 256, st, a);
+  launch_pdl(k_list_scan<false>, 1, 1024, st, a);
+  launch_pdl(k_list_fill<false>, cand_blocks, 256, st, a);
+  launch_pdl(k_list_pad<false>, tile_blocks, 256, st, a);
+  launch_pdl(k_list_done, (a.ntile + 255) / 256, 256, st, a.flagB, a.tile_flagB, a.ntile);
+  SFFG_CK(cudaGetLastError());
+  launches_ += 7;
+  SFFG_CK(cudaMemcpyAsync(d.list_host, d.counters.p, 16 * sizeof(int), cudaMemcpyDeviceToHost, st));
+  SFFG_CK(cudaEventRecord(d.list_ev, st));
+  list_check_pending_ = true;
+  have_list_ = true;
+  list_builds_++;
+  return SFFG_OK;
+}
+
+// Reads the counters of the last queued list build (waiting for them if
+// need be): overflowed when a store was too small.  The counts seen update
+// the ones the next queued build sizes its stores from.
+std::atomic<long long> g_list_overflows{0};
+
+int Batch::resolve_list_check(bool *overflowed) {
+  *overflowed = false;
+  if (!list_check_pending_) return SFFG_OK;
+  DeviceState &d = *d_;
+  SFFG_CK(cudaEventSynchronize(d.list_ev));
+  list_check_pending_ = false;
+  const int *c = d.list_host;
+  *overflowed = c[1] != 0;
+  if (*overflowed) g_list_overflows++;
+  // counters[0]: candidates wanted (also when they did not fit); [12]: the
+  // chunks list A needed (written when the candidates fitted)
+  last_ncand_ = std::max<long long>(c[0], *overflowed ? last_ncand_ : 0);
+  if (!*overflowed) ncand_ = c[0];
+  last_nch_ = std::max<long long>(c[12], *overflowed ? last_nch_ : 0);
+  return SFFG_OK;
+}
+
+// Settles a queued list build: when it overflowed (its lists came out
+// empty), md steps taken since its snapshot are replayed from the snapshot
+// with a synchronous build; otherwise the snapshot is dropped.
+int Batch::settle_md(cudaStream_t st) {
+  DeviceState &d = *d_;
+  bool ovf = false;
+  int rc = resolve_list_check(&ovf);
+  if (rc) return rc;
+  if (!ovf) {
+    md_ckpt_valid_ = false;
+    return SFFG_OK;
+  }
+  if (!md_ckpt_valid_) {
+    // no snapshot (cannot happen: queued builds come from eval_checked,
+    // which resolves its own, or md_steps, which takes one): rebuild next
+    have_list_ = false;
+    return SFFG_OK;
+  }
+  const size_t n3 = 3 * static_cast<size_t>(natom_total_);
+  SFFG_CK(cudaMemcpyAsync(d.x.p, d.ck_x.p, n3 * sizeof(double), cudaMemcpyDeviceToDevice, st));
+  SFFG_CK(cudaMemcpyAsync(d.v.p, d.ck_v.p, n3 * sizeof(double), cudaMemcpyDeviceToDevice, st));
+  SFFG_CK(cudaMemcpyAsync(d.accel.p, d.ck_accel.p, n3 * sizeof(double), cudaMemcpyDeviceToDevice, st));
+  SFFG_CK(cudaMemcpyAsync(d.tscal.p, d.ck_tscal.p, d.tscal.bytes(), cudaMemcpyDeviceToDevice, st));
+  SFFG_CK(cudaMemcpyAsync(d.ekin_last.p, d.ck_ekin_last.p, d.ekin_last.bytes(), cudaMemcpyDeviceToDevice, st));
+  const int from = md_ckpt_step_, nsteps = md_ckpt_steps_;
+  md_ckpt_valid_ = false;
+  force_sync_build_ = true;
+  rc = md_steps(from, nsteps, nullptr, nullptr, st, true);
+  force_sync_build_ = false;
+  return rc;
+}
+
+int Batch::settle(void *stream) {
+  if (!list_check_pending_ && !md_ckpt_valid_) return SFFG_OK;
+  if (!d_) return SFFG_OK;
+  return settle_md(pick(*d_, stream));
+}
+
+int Batch::eval_checked(bool rebuild, void *stream) {
+  int rc = settle(stream);
+  if (rc) return rc;
+  if (!rebuild || !sized_ || !finalized_) return eval(rebuild, stream);
+  queued_builds_ = true;
+  rc = eval(true, stream);
+  queued_builds_ = false;
+  if (rc) return rc;
+  bool ovf = false;
+  if ((rc = resolve_list_check(&ovf))) return rc;
+  if (ovf) {  // a store was too small: again, with the stores sized exactly
+    force_sync_build_ = true;
+    rc = eval(true, stream);
+    force_sync_build_ = false;
+  }
+  return rc;
 }
 
 // Remakes list B from list A when k_pack found an atom that moved too far
@@ -1051,6 +1245,7 @@ void Batch::rebuild_list_b(void *stream) {
 }
 
 int Batch::eval(bool rebuild, void *stream) {
+  SFFG_SETTLE(stream);
   if (!finalized_) {
     last_error = "eval before finalize";
     return SFFG_ESTATE;
@@ -1325,6 +1520,7 @@ int Batch::run_eval_direct(bool rebuild, void *stream) {
 }
 
 long long Batch::num_pairs(int s) {
+  if (settle(nullptr) != SFFG_OK) return -1;
   // Count the pairs of system s on list A (the reference's list; a
   // diagnostic path, synchronous).
   if (!finalized_ || !have_list_) return -1;
@@ -1470,6 +1666,7 @@ static int upload_noise(Batch &b, DeviceState &d, Batch::NoiseFn noise, void *ct
 }
 
 int Batch::md_begin(bool rebuild, NoiseFn noise, void *noise_ctx, void *stream) {
+  SFFG_SETTLE(stream);
   if (!finalized_) return SFFG_ESTATE;
   DeviceState &d = *d_;
   cudaStream_t st = pick(d, stream);
@@ -1498,8 +1695,13 @@ int Batch::md_begin(bool rebuild, NoiseFn noise, void *noise_ctx, void *stream) 
 
 int Batch::md_com_remove(void *stream) {
   if (!finalized_) return SFFG_ESTATE;
+  const int rc = settle(stream);
+  if (rc) return rc;
+  return md_com_remove_direct(pick(*d_, stream));
+}
+
+int Batch::md_com_remove_direct(cudaStream_t st) {
   DeviceState &d = *d_;
-  cudaStream_t st = pick(d, stream);
   k_com_remove<<<num_systems(), kComThreads, 0, st>>>(d.x.p, d.v.p, d.minv.p, d.sys_atom_off.p, d.sys_natom.p,
                                                       d.sys_active.p, opts_.gamma_ln == 0.0 || opts_.hcp != 0);
   SFFG_CK(cudaGetLastError());
@@ -1541,12 +1743,40 @@ int Batch::md_steps(int step0, int k, NoiseFn noise, void *noise_ctx, void *stre
     SFFG_CK(cudaGetLastError());
     return SFFG_OK;
   };
+  // a queued list build that has finished by now is checked without waiting
+  if (list_check_pending_ && cudaEventQuery(d.list_ev) == cudaSuccess && (rc = settle_md(st))) return rc;
   for (int i = 1; i <= k; i++) {
     const int nstep = step0 + i;
     const bool rebuild = opts_.nsnb > 0 && nstep % opts_.nsnb == 0;
     // centre-of-mass motion removal every nscm steps (sff.c:2346-2351)
     const bool com = opts_.nscm > 0 && nstep % opts_.nscm == 0 && (i < k || com_at_end);
-    if (!rebuild && !noise && !com && graphs_ok()) {
+    if (rebuild && !noise && sized_ && !force_sync_build_) {
+      // a rebuild step without host round trips: the previous queued build
+      // is settled first, then the state this step starts from is kept, so
+      // that if this build's stores prove too small the steps from here can
+      // be replayed (settle_md)
+      if ((rc = settle_md(st))) break;
+      const size_t n3 = 3 * static_cast<size_t>(natom_total_);
+      if (d.ck_x.n < n3) {
+        SFFG_CK(d.ck_x.alloc(n3));
+        SFFG_CK(d.ck_v.alloc(n3));
+        SFFG_CK(d.ck_accel.alloc(n3));
+      }
+      if (d.ck_tscal.n < d.tscal.n) SFFG_CK(d.ck_tscal.alloc(d.tscal.n));
+      if (d.ck_ekin_last.n < d.ekin_last.n) SFFG_CK(d.ck_ekin_last.alloc(d.ekin_last.n));
+      SFFG_CK(cudaMemcpyAsync(d.ck_x.p, d.x.p, n3 * sizeof(double), cudaMemcpyDeviceToDevice, st));
+      SFFG_CK(cudaMemcpyAsync(d.ck_v.p, d.v.p, n3 * sizeof(double), cudaMemcpyDeviceToDevice, st));
+      SFFG_CK(cudaMemcpyAsync(d.ck_accel.p, d.accel.p, n3 * sizeof(double), cudaMemcpyDeviceToDevice, st));
+      SFFG_CK(cudaMemcpyAsync(d.ck_tscal.p, d.tscal.p, d.tscal.bytes(), cudaMemcpyDeviceToDevice, st));
+      SFFG_CK(cudaMemcpyAsync(d.ck_ekin_last.p, d.ekin_last.p, d.ekin_last.bytes(), cudaMemcpyDeviceToDevice, st));
+      md_ckpt_valid_ = true;
+      md_ckpt_step_ = nstep - 1;
+      md_ckpt_steps_ = 0;
+      queued_builds_ = true;
+      rc = step_body(st, true, false);
+      queued_builds_ = false;
+      if (rc) break;
+    } else if (!rebuild && !noise && !com && graphs_ok()) {
       if ((rc = ensure_tuned(st))) break;
       if ((rc = capture(d.g_step, d.sig_step, d.launches_step, [&](cudaStream_t cs) { return step_body(cs, false, true); })))
         break;
@@ -1556,12 +1786,14 @@ int Batch::md_steps(int step0, int k, NoiseFn noise, void *noise_ctx, void *stre
     } else if ((rc = step_body(st, rebuild, false))) {
       break;
     }
-    if (com && (rc = md_com_remove(st))) break;
+    if (md_ckpt_valid_) md_ckpt_steps_++;
+    if (com && (rc = md_com_remove_direct(st))) break;
   }
   return rc;
 }
 
 int Batch::md_kinetic(std::vector<double> &ekin, void *stream) {
+  SFFG_SETTLE(stream);
   if (!finalized_) return SFFG_ESTATE;
   DeviceState &d = *d_;
   cudaStream_t st = pick(d, stream);
@@ -1577,6 +1809,7 @@ int Batch::md_kinetic(std::vector<double> &ekin, void *stream) {
 }
 
 int Batch::md_set_tscal(const std::vector<double> &tscal, void *stream) {
+  SFFG_SETTLE(stream);
   if (!finalized_ || static_cast<int>(tscal.size()) != num_systems()) return SFFG_EINVAL;
   SFFG_CK(cudaMemcpyAsync(d_->tscal.p, tscal.data(), tscal.size() * sizeof(double), cudaMemcpyHostToDevice,
                           pick(*d_, stream)));
@@ -1834,12 +2067,14 @@ __global__ void __launch_bounds__(kCgThreads) k_cg_post(CgArgs a) {
 // without waiting; cg_poll reads the states back; cg_end restores the
 // active flags.  cg() runs them to completion.
 int Batch::cg_begin(int maxiter, double rmsgrad, double dfpred, void *stream) {
+  SFFG_SETTLE(stream);
   return cg_begin(std::vector<int>(num_systems(), maxiter), std::vector<double>(num_systems(), rmsgrad), dfpred,
                   stream);
 }
 
 int Batch::cg_begin(const std::vector<int> &maxiter, const std::vector<double> &rmsgrad, double dfpred,
                     void *stream) {
+  SFFG_SETTLE(stream);
   if (!finalized_) return SFFG_ESTATE;
   if (static_cast<int>(maxiter.size()) != num_systems() || static_cast<int>(rmsgrad.size()) != num_systems()) {
     last_error = "cg_begin: one maxiter and rmsgrad per system";
@@ -1874,6 +2109,7 @@ int Batch::cg_begin(const std::vector<int> &maxiter, const std::vector<double> &
 }
 
 int Batch::cg_turns(int n, bool first_rebuild, void *stream, const std::function<int(int)> &after_eval) {
+  SFFG_SETTLE(stream);
   Range range("sffg conjgrad turns");
   DeviceState &d = *d_;
   cudaStream_t st = pick(d, stream);
@@ -1902,6 +2138,7 @@ int Batch::cg_turns(int n, bool first_rebuild, void *stream, const std::function
 }
 
 int Batch::cg_poll(int *nactive, std::vector<int> *status, std::vector<double> *energy, void *stream) {
+  SFFG_SETTLE(stream);
   DeviceState &d = *d_;
   cudaStream_t st = pick(d, stream);
   const int nsys = num_systems();
@@ -1948,6 +2185,7 @@ void Batch::note_active(const std::vector<int> &on) {
 }
 
 int Batch::set_active(int sys, bool on, void *stream) {
+  SFFG_SETTLE(stream);
   if (!finalized_ || sys < 0 || sys >= num_systems()) return SFFG_EINVAL;
   DeviceState &d = *d_;
   ones_.resize(num_systems(), 1);
@@ -1958,6 +2196,7 @@ int Batch::set_active(int sys, bool on, void *stream) {
 }
 
 int Batch::cg_end(void *stream) {
+  SFFG_SETTLE(stream);
   DeviceState &d = *d_;
   cudaStream_t st = pick(d, stream);
   // a system the minimiser switched off on the device misses the list
@@ -1990,6 +2229,8 @@ int Batch::cg(int maxiter, double rmsgrad, double dfpred, bool first_rebuild, st
 
 // The first failed bounds check of a build with -DSFFG_CHECKED (a
 // CheckCode), 0 when none failed, -1 in the normal build.
+extern "C" long long sffg_list_overflows(void) { return sffg::g_list_overflows.load(); }
+
 extern "C" int sffg_checked_code(void) {
 #ifdef SFFG_CHECKED
   int c = 0;

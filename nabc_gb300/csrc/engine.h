@@ -146,6 +146,16 @@ class Batch {
   // One energy+gradient evaluation of every active system.  rebuild
   // requests a pair-list rebuild first (always done on the first call).
   int eval(bool rebuild, void *stream);
+  // The same, with a list rebuild that launches without reading counts back
+  // (see build_lists); returns once the list build has run on the device,
+  // and when a list store was too small it grows the stores and evaluates
+  // again, so the results are always complete.
+  int eval_checked(bool rebuild, void *stream);
+  // Resolves a queued list build still unchecked (waiting for it if need
+  // be); after one whose stores were too small, md steps taken since are
+  // replayed from their snapshot.  Every method that reads or changes the
+  // batch's device state calls it first.
+  int settle(void *stream);
   long long num_pairs(int sys);
 
   // Device-resident Langevin/Berendsen md (the reference's integrator,
@@ -213,6 +223,10 @@ class Batch {
   int capture(cudaGraphExec_t &exec, std::vector<const void *> &sig, long long &nlaunch,
               const std::function<int(cudaStream_t)> &body);
   int build_lists(void *stream);
+  int build_lists_queued(cudaStream_t st);
+  int resolve_list_check(bool *overflowed);
+  int settle_md(cudaStream_t st);
+  int md_com_remove_direct(cudaStream_t st);
   void rebuild_list_b(void *stream);
   ListArgs list_args(double fsmax);
   double fsmax_all() const;
@@ -240,6 +254,18 @@ class Batch {
   int cg_nsys_ = 0, cg_turn_ = 0, cg_maxiter_ = 0;
   long long cand_max_ = 0;  // candidate tile pairs the batch could ever need
   int ncand_ = 0;           // candidates of the current pair list
+  // Queued list builds: allowed while queued_builds_ is set and a
+  // synchronous build has sized the stores (sized_); the last known
+  // candidate and chunk counts size the next queued build's stores with
+  // headroom.  list_check_pending_: a queued build's overflow flag is still
+  // unread.  force_sync_build_: the next build reads its counts back.
+  bool queued_builds_ = false, sized_ = false, list_check_pending_ = false, force_sync_build_ = false;
+  long long last_ncand_ = 0, last_nch_ = 0;
+  // md replay: the state (coordinates, velocities, accelerations, kinetic
+  // sums, Berendsen factors) before the md step whose list build was
+  // queued, that step's predecessor number and the steps taken since
+  bool md_ckpt_valid_ = false;
+  int md_ckpt_step_ = 0, md_ckpt_steps_ = 0;
   bool finalized_ = false, have_list_ = false, profile_ = false;
   long long launches_ = 0;
   std::unique_ptr<DeviceState> d_;

@@ -249,7 +249,9 @@ extern "C" REAL_T mme(REAL_T *x, REAL_T *f, INT_T *iter) {
     write_checkpoint(checkpoint_name(), s.natom, x, *iter);
   const bool rebuild = !s.list_built || (*iter > 0 && o.nsnb > 0 && *iter % o.nsnb == 0) || *iter == -4;
   check(b.set_coords(0, x, nullptr), "set_coords");
-  check(b.eval(rebuild, nullptr), "eval");
+  // a rebuild launches without host round trips; the call redoes it in the
+  // rare case that a list store proved too small
+  check(b.eval_checked(rebuild, nullptr), "eval");
   s.list_built = true;
   const double e = finish_eval(*iter, f);
   timers().mme += wall_seconds() - t0;

@@ -80,8 +80,13 @@ struct ListArgs {
   float close2f; // (kClose + 1 A)^2: list A's possibly close pairs
   // candidates
   int2 *cand;
-  int cand_cap;
-  int *ncand, *overflow;
+  int cand_cap;  // candidates the store holds (the column arrays hold as many)
+  int ent_cap;   // list chunks each entry store holds
+  // overflow: set when a store is too small (the candidates, or the entries
+  // of list A); every later stage then returns at once and the chunk counts
+  // are zero, so the passes read nothing past a store.  chunks_needed: the
+  // chunks list A needed.
+  int *ncand, *overflow, *chunks_needed;
   int *cand_start, *cand_count;  // per i-tile
   unsigned *colA, *colB, *colC, *colE, *colK;  // per candidate x 32 lanes
   int4 *cand_n;                  // entries of (A, B, C) per candidate
@@ -170,9 +175,9 @@ __global__ void k_list_columns(const ListArgs a) {
   __shared__ float s_s[8][32];
   __shared__ int s_atom[8][32];
   __shared__ unsigned s_ex[8][32];
-  if (GB_ONLY && !*a.flagB) return;
+  if ((GB_ONLY && !*a.flagB) || *a.overflow) return;
   const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
-  const int ncand = *a.ncand, nwarps = (gridDim.x * blockDim.x) >> 5;
+  const int ncand = min(*a.ncand, a.cand_cap), nwarps = (gridDim.x * blockDim.x) >> 5;
   for (int c = (blockIdx.x * blockDim.x + threadIdx.x) >> 5; c < ncand; c += nwarps) {
   const int2 p = a.cand[c];
   const int I = p.x, J = p.y;
@@ -284,7 +289,7 @@ __global__ void k_list_columns(const ListArgs a) {
 template <bool GB_ONLY>
 __global__ void k_list_offsets(const ListArgs a) {
   pdl_wait();
-  if (GB_ONLY && !*a.flagB) return;
+  if ((GB_ONLY && !*a.flagB) || *a.overflow) return;
   const int lane = threadIdx.x & 31;
   const int I = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
   if (I >= a.ntile) return;
@@ -328,6 +333,14 @@ __global__ void __launch_bounds__(1024) k_list_scan(const ListArgs a) {
   __shared__ int s_a[1024], s_b[1024], s_c[1024];
   if (GB_ONLY && !*a.flagB) return;
   const int t = threadIdx.x, n = a.ntile;
+  if (*a.overflow) {  // a store was too small: empty lists
+    if (t == 0) {
+      *a.nchunkA = 0;
+      *a.nchunkB = 0;
+      *a.nchunkC = 0;
+    }
+    return;
+  }
   const int per = (n + 1023) / 1024, lo = min(n, t * per), hi = min(n, lo + per);
   int sa = 0, sb = 0, sc = 0;
   for (int i = lo; i < hi; i++) {
@@ -359,9 +372,15 @@ __global__ void __launch_bounds__(1024) k_list_scan(const ListArgs a) {
     rc += a.chunksC[i];
   }
   if (t == 1023) {
-    if (!GB_ONLY) *a.nchunkA = s_a[1023];
-    *a.nchunkB = s_b[1023];
-    *a.nchunkC = s_c[1023];
+    // list A's entries must fit their store (B and C hold subsets of them)
+    const bool fits = GB_ONLY || static_cast<long long>(s_a[1023]) <= a.ent_cap;
+    if (!GB_ONLY) {
+      *a.chunks_needed = s_a[1023];
+      if (!fits) atomicExch(a.overflow, 1);
+      *a.nchunkA = fits ? s_a[1023] : 0;
+    }
+    *a.nchunkB = fits ? s_b[1023] : 0;
+    *a.nchunkC = fits ? s_c[1023] : 0;
   }
 }
 
@@ -369,9 +388,9 @@ __global__ void __launch_bounds__(1024) k_list_scan(const ListArgs a) {
 template <bool GB_ONLY>
 __global__ void k_list_fill(const ListArgs a) {
   pdl_wait();
-  if (GB_ONLY && !*a.flagB) return;
+  if ((GB_ONLY && !*a.flagB) || *a.overflow) return;
   const int lane = threadIdx.x & 31;
-  const int ncand = *a.ncand, nwarps = (gridDim.x * blockDim.x) >> 5;
+  const int ncand = min(*a.ncand, a.cand_cap), nwarps = (gridDim.x * blockDim.x) >> 5;
   for (int c = (blockIdx.x * blockDim.x + threadIdx.x) >> 5; c < ncand; c += nwarps) {
   const int2 p = a.cand[c];
   const int4 off = a.cand_off[c];
@@ -416,7 +435,7 @@ __global__ void k_list_fill(const ListArgs a) {
 template <bool GB_ONLY>
 __global__ void k_list_pad(const ListArgs a) {
   pdl_wait();
-  if (GB_ONLY && !*a.flagB) return;
+  if ((GB_ONLY && !*a.flagB) || *a.overflow) return;
   const int lane = threadIdx.x & 31;
   const int I = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
   if (I >= a.ntile) return;

@@ -169,6 +169,8 @@ def lib():
         L.sffg_batch_status.argtypes = [vp, INT_P, vp]
         L.sffg_checked_code.argtypes = []
         L.sffg_checked_code.restype = C.c_int
+        L.sffg_list_overflows.argtypes = []
+        L.sffg_list_overflows.restype = C.c_longlong
         L.sffg_batch_save.argtypes = [vp, C.c_char_p, vp]
         L.sffg_batch_load.argtypes = [vp, C.c_char_p, vp]
         L.mm_set_checkpoint.argtypes = [C.POINTER(C.c_char_p)]
