@@ -8,8 +8,8 @@ constants.  These numbers are model parameters and must be bit-identical to
 the reference's (src/sff/gbneck.h:7-170), so this script extracts them from
 that header and writes them into flat arrays of our own layout.
 
-Usage (development container only):
-    python nabc_gb300/csrc/gen_neck_tables.py /root/reference/src/sff/gbneck.h
+Usage (where the reference's source tree is at hand):
+    python nabc_gb300/csrc/gen_neck_tables.py <reference tree>/src/sff/gbneck.h
 """
 import os
 import re

@@ -1,9 +1,10 @@
 """Regenerate the golden fixtures under tests/golden/.
 
-Run in the development container, where the reference tree is mounted:
+Run where the reference's source tree is at hand (by default the directory
+"reference" beside this repository):
 
-    make -C oracle ref
-    python tests/golden/make_golden.py /root/reference
+    make -C oracle ref [REFROOT=<reference tree>]
+    python tests/golden/make_golden.py [<reference tree>]
 
 It produces
   ref/          the reference's own test inputs for the GB path (prmtops,
@@ -156,7 +157,8 @@ def read_dump(path):
 
 
 def main():
-    refroot = sys.argv[1] if len(sys.argv) > 1 else "/root/reference"
+    repo = os.path.dirname(os.path.dirname(HERE))
+    refroot = sys.argv[1] if len(sys.argv) > 1 else os.path.join(os.path.dirname(repo), "reference")
     test = os.path.join(refroot, "test")
     if not os.path.exists(SFFREF):
         raise SystemExit("build the reference first: make -C oracle ref")
