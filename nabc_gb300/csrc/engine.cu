@@ -347,6 +347,7 @@ int Batch::upload() {
       const float sf = static_cast<float>(sd);
       const float scorr = sf != 0.0f ? static_cast<float>(3.0 * (sd - static_cast<double>(sf)) / sf) : 0.0f;
       gbpar[sl] = make_float4(static_cast<float>(rho), sf, static_cast<float>(hs.rborn[i]), scorr);
+      smax_abs_ = std::max(smax_abs_, std::fabs(sd));
       param[sl] = (hs.type[i] & 0xffff) | (hs.neck[i] << 16) | (hs.frozen[i] ? (1 << 24) : 0);
       q32[sl] = static_cast<float>(hs.q[i]);
       q64[sl] = hs.q[i];
@@ -899,6 +900,7 @@ DevTables make_tables(DeviceState &d, const ModelParams &mp, double fsmax, int q
   t.born.rgbmax1i = static_cast<float>(1.0 / mp.rgbmax);
   t.born.rgbmax2i = static_cast<float>(1.0 / (mp.rgbmax * mp.rgbmax));
   t.born.cutoff2 = static_cast<float>((mp.rgbmax + fsmax) * (mp.rgbmax + fsmax));
+  t.born.tail_poly_only = 0;
   t.pair.kappa_s = static_cast<float>(mp.kappa * kKscale);
   t.pair.inv_epsext = static_cast<float>(1.0 / mp.epsext);
   t.pair.dielfac0 = static_cast<float>(1.0 - 1.0 / mp.epsext);
@@ -1434,6 +1436,7 @@ int Batch::run_eval_direct(bool rebuild, void *stream) {
   }
   {
     DevTables t = make_tables(d, mp_, fsmax, 5);
+    t.born.tail_poly_only = 2.0 * smax_abs_ <= 0.3 * mp_.rgbmax * 0.999;
     t.claim = cfg_[0].claim;
     if (tuning_) SFFG_CK(cudaEventRecord(d.tune_ev[0][0], st));
     {
@@ -1493,6 +1496,7 @@ int Batch::run_eval_direct(bool rebuild, void *stream) {
   if (profile_) SFFG_CK(cudaEventRecord(d.events[ring][2][0], st));
   {
     DevTables t = make_tables(d, mp_, fsmax, 7);
+    t.born.tail_poly_only = 2.0 * smax_abs_ <= 0.3 * mp_.rgbmax * 0.999;
     t.claim = cfg_[2].claim;
     if (tuning_) SFFG_CK(cudaEventRecord(d.tune_ev[2][0], st));
     {

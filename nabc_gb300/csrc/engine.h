@@ -230,6 +230,7 @@ class Batch {
   void rebuild_list_b(void *stream);
   ListArgs list_args(double fsmax);
   double fsmax_all() const;
+  double smax_abs_ = 0.0;  // largest |s| = |fs (rborn - offset)| of the batch's atoms
   int run_eval(bool rebuild, void *stream);
   void collect_pass_times(DeviceState &d, long long max_evals);
   Options opts_;

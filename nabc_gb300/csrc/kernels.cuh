@@ -4,19 +4,19 @@
 // 1770-2066, 2131-2405) run over compacted pair-list chunks (lists.cuh): a
 // chunk is an i-tile of 32 atoms and 32 packed j-atoms with a column mask
 // each.  A warp owns one chunk at a time: lane l holds i-atom l in
-// registers; the 32 j-atoms are staged in shared memory and read by
-// broadcast, so at step s every lane pairs its i-atom with j-atom s.  Both
-// directions of each unordered pair are handled in one visit (Newton's
-// third law); the j-side partial sums, spread over the 32 lanes, are folded
-// with a shuffle transpose-reduction every few steps.  Per chunk the FP32
-// partial sums are converted to 64-bit fixed point, so the totals do not
-// depend on how chunks are scheduled.
+// registers; the far-field chunks are walked in a rotation (lane l meets
+// j-entry (l + s) mod 32 at step s, the entry's j-side sums moving one lane
+// per step), the near-field chunks pair by pair.  Both directions of each
+// unordered pair are handled in one visit (Newton's third law).  Per chunk
+// the FP32 partial sums are converted to 64-bit fixed point, so the totals
+// do not depend on how chunks are scheduled.
 #pragma once
 
 #include <cstdint>
 #include <type_traits>
 
 #include "gbmath.cuh"
+#include "pack2.cuh"
 
 namespace sffg {
 
@@ -100,55 +100,6 @@ __device__ __forceinline__ long long to_fixed(float v, float scale) {
   return __float2ll_rn(v * scale);
 }
 
-// Steps per group of the pair loops: j-side partial sums are kept in
-// registers for a group of steps, then folded across the warp.  Fewer steps
-// per group keep the unrolled loop body (and the instruction-cache
-// footprint) small at the cost of more shuffles per step; measured best:
-// 4 for all three passes (with pass 2 at 3 blocks per SM; at 2 blocks per
-// SM, 8 was better for it).
-#ifndef SFFG_GROUP_BORN
-#define SFFG_GROUP_BORN 4
-#endif
-#ifndef SFFG_GROUP_PAIR
-#define SFFG_GROUP_PAIR 4
-#endif
-constexpr int kGroup = SFFG_GROUP_BORN;
-constexpr int kGroupPair = SFFG_GROUP_PAIR;
-
-constexpr int ilog2(int k) { return k == 8 ? 3 : k == 4 ? 2 : k == 2 ? 1 : 0; }
-
-// Sum of v[e] over the 32 lanes for e = 0..K-1, delivered to lane K*g + e
-// (zero in the other lanes): log2(K) transposing shuffle stages (each lane
-// keeps half of its values and sends the other half across), then a plain
-// butterfly over the remaining lane bits.  After the transposing stages
-// lane L holds element L >> (5 - log2 K).
-template <int K>
-__device__ __forceinline__ float reduce_to_lane(const float (&v)[K], int g, int lane) {
-  static_assert(K == 2 || K == 4 || K == 8, "group of 2, 4 or 8 steps");
-  constexpr int kLog2 = ilog2(K);
-  float a[K];
-#pragma unroll
-  for (int k = 0; k < K; k++) a[k] = v[k];
-  int m = K, dist = 16;
-#pragma unroll
-  for (int st = 0; st < kLog2; st++) {
-    const bool b = lane & dist;
-    m >>= 1;
-#pragma unroll
-    for (int k = 0; k < m; k++) {
-      const float send = b ? a[k] : a[k + m];
-      const float keep = b ? a[k + m] : a[k];
-      a[k] = keep + __shfl_xor_sync(kFull, send, dist);
-    }
-    dist >>= 1;
-  }
-  float c = a[0];
-#pragma unroll
-  for (int d = 16 >> kLog2; d > 0; d >>= 1) c += __shfl_xor_sync(kFull, c, d);
-  const float r = __shfl_sync(kFull, c, (lane & (K - 1)) << (5 - kLog2));
-  return (lane >> kLog2) == g ? r : 0.0f;
-}
-
 __device__ __forceinline__ long long warp_sum_ll(long long v) {
 #pragma unroll
   for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(kFull, v, o);
@@ -171,39 +122,6 @@ __device__ __forceinline__ int claim_chunk(int *counter, int lane, int claim) {
   int base = 0;
   if (lane == 0) base = atomicAdd(counter, claim);
   return __shfl_sync(kFull, base, 0);
-}
-
-// Both directions of the descreening of one pair of list B (value, or for
-// DERIV the derivative / dij): vi is atom i descreened by sphere j, vj the
-// converse.  List B holds no pair within near-field range, so only the far
-// field (evaluated for every lane), the rgbmax tail (evaluated when any
-// lane of the warp needs it) and the zero beyond rgbmax + s remain; the
-// branches are warp-uniform.
-template <bool DERIV>
-__device__ __forceinline__ void descreen_pair(const BornConst &c, bool in, float dij, float d1, float s_i,
-                                              float s_j, float &vi, float &vj) {
-  vi = DERIV ? far_deriv(d1, s_j) : far_term(d1, s_j);
-  vj = DERIV ? far_deriv(d1, s_i) : far_term(d1, s_i);
-  const bool ti = dij > c.rgbmax - s_j, tj = dij > c.rgbmax - s_i;
-  if (__any_sync(kFull, in && (ti || tj))) {
-    const float qi = tail_closed<DERIV>(c, dij, d1, s_j);
-    const float qj = tail_closed<DERIV>(c, dij, d1, s_i);
-    vi = ti ? qi : vi;
-    vj = tj ? qj : vj;
-  }
-  // beyond rgbmax + s the term is zero; with a negative s (GBneck2 screens
-  // sulfur with fs < 0) that range starts below rgbmax - s
-  vi = dij > c.rgbmax + s_j ? 0.0f : vi;
-  vj = dij > c.rgbmax + s_i ? 0.0f : vj;
-}
-
-// Stages the j-entries of chunk k in shared memory: lane l loads entry l.
-// Returns this lane's j slot (padding entries point at a real slot of the
-// i-tile and have an empty column).
-__device__ __forceinline__ int chunk_entry(const ChunkList &L, int k, int lane, unsigned &col, int nslot) {
-  const size_t e = static_cast<size_t>(k) * 32 + lane;
-  col = L.col[e];
-  return SFFG_IDX(L.slot[e], nslot, kCheckSlot);
 }
 
 // ------------------------------------------------------ rotation schedule
@@ -441,19 +359,27 @@ __global__ void __launch_bounds__(256, 3) k_born(const DevTables t) {
         const float d1 = rsqrt_nr(r2);
         const float d2i = d1 * d1;
         const float cj = pb[u].x;
-        float ti = far_term2(d2i, a.w, pb[u].y);
-        float tj = far_term2(d2i, si, si2);
+        // both directions as packed pairs: (sphere j on atom i, sphere i on
+        // atom j)
+        const f2 S = pk(a.w, si);
+        float ti, tj;
+        upk(far_term_x2(d2i, S, pk(pb[u].y, si2)), ti, tj);
         const float dij = r2 * d1;
         {
           // the smooth tail for dij > rgbmax - s, zero beyond rgbmax + s
-          // (with a negative s, GBneck2's sulfur, that range starts below)
+          // (with a negative s, GBneck2's sulfur, that range starts below);
+          // nearly every step of a chunk has some tail pair, so it is
+          // evaluated throughout
           const bool qi_ = dij > rgbmax - a.w, qj_ = dij > rgbmax - si;
-          if (__any_sync(kFull, qi_ || qj_)) {
-            const float vi = tail_closed<false>(t.born, dij, d1, a.w);
-            const float vj = tail_closed<false>(t.born, dij, d1, si);
-            ti = qi_ ? vi : ti;
-            tj = qj_ ? vj : tj;
+          float vi, vj;
+          if (t.born.tail_poly_only) {
+            upk(tail_x2<false>(t.born, dij, d1, S), vi, vj);
+          } else {
+            vi = tail_closed<false>(t.born, dij, d1, a.w);
+            vj = tail_closed<false>(t.born, dij, d1, si);
           }
+          ti = qi_ ? vi : ti;
+          tj = qj_ ? vj : tj;
           ti = dij > rgbmax + a.w ? 0.0f : ti;
           tj = dij > rgbmax + si ? 0.0f : tj;
         }
@@ -934,17 +860,21 @@ __global__ void __launch_bounds__(256, 3) k_chain(const DevTables t) {
         // the hardware rsqrt alone: pass 3 only shapes the forces
         const float d1 = rsqrt_ftz(r2);
         const float d2i = d1 * d1;
-        float di = far_deriv2(d2i, a.w, b.y);
-        float dj = far_deriv2(d2i, si, si2);
+        const f2 S = pk(a.w, si);
+        float di, dj;
+        upk(far_deriv_x2(d2i, S, pk(b.y, si2)), di, dj);
         const float dij = r2 * d1;
         {
           const bool qi_ = dij > rgbmax - a.w, qj_ = dij > rgbmax - si;
-          if (__any_sync(kFull, qi_ || qj_)) {
-            const float vi = tail_closed<true>(t.born, dij, d1, a.w);
-            const float vj = tail_closed<true>(t.born, dij, d1, si);
-            di = qi_ ? vi : di;
-            dj = qj_ ? vj : dj;
+          float vi, vj;
+          if (t.born.tail_poly_only) {
+            upk(tail_x2<true>(t.born, dij, d1, S), vi, vj);
+          } else {
+            vi = tail_closed<true>(t.born, dij, d1, a.w);
+            vj = tail_closed<true>(t.born, dij, d1, si);
           }
+          di = qi_ ? vi : di;
+          dj = qj_ ? vj : dj;
           di = dij > rgbmax + a.w ? 0.0f : di;
           dj = dij > rgbmax + si ? 0.0f : dj;
         }
