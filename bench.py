@@ -58,7 +58,7 @@ MUFU_PASS = (1.0, 4.0, 1.0)
 # one ncu capture (dram__bytes_read.sum + dram__bytes_write.sum): the inputs
 # (~1.6 MB of per-atom data, the lists) stay in L2, so traffic is far below
 # what the FP32 work would allow.
-TRAFFIC_PASS = (6.77e6, 17.87e6, 7.28e6)
+TRAFFIC_PASS = (6.62e6, 21.71e6, 7.13e6)
 PASS_NAMES = ("k_born (pass 1, Born radii)", "k_gbpair (pass 2, GB+Coulomb+LJ)", "k_chain (pass 3, chain rule)")
 # Per SM and clock: FP32 lanes (an FFMA counts 2 flops) and MUFU results.
 FP32_LANES_PER_SM, MUFU_PER_SM = 128, 16
@@ -361,11 +361,15 @@ def bench_serving(args):
             if nr == 0 and npend == 0 and k < n:
                 time.sleep(max(0.0, min(arrive[k] - (time.perf_counter() - t0), 0.01)))
         span = time.perf_counter() - t0
-        lat = np.array([s.result(i)["latency_ms"] for i in ids])
+        res = [s.result(i) for i in ids]
+        lat = np.array([r["latency_ms"] for r in res])
         s.close()
+        codes, counts = np.unique([r["status"] for r in res], return_counts=True)
         rates.append({"arrival_per_s": rate, "throughput_requests_per_s": n / span,
-                      "p50_ms": float(np.percentile(lat, 50)), "p99_ms": float(np.percentile(lat, 99))})
+                      "p50_ms": float(np.percentile(lat, 50)), "p99_ms": float(np.percentile(lat, 99)),
+                      "conjgrad_returns": {str(int(c)): int(k) for c, k in zip(codes, counts)}})
     out["served"] = rates
+    out["atoms"] = [int(v) for v in sizes]
     return out
 
 
@@ -539,10 +543,10 @@ def main():
     ap.add_argument("--no-tune", action="store_true",
                     help="default work split instead of the autotuned one (for profiler runs, whose timing the "
                          "tuner would otherwise follow)")
-    ap.add_argument("--serve-requests", type=int, default=48)
-    ap.add_argument("--serve-max-atoms", type=int, default=5000, help="50000: the full request size range")
-    ap.add_argument("--serve-maxiter", type=int, default=300, help="2000: the full conjgrad limit")
-    ap.add_argument("--serve-rates", type=float, nargs="*", default=[50.0, 500.0])
+    ap.add_argument("--serve-requests", type=int, default=12, help="requests per arrival-rate run")
+    ap.add_argument("--serve-max-atoms", type=int, default=50000, help="requests log-uniform in 500 .. this")
+    ap.add_argument("--serve-maxiter", type=int, default=2000, help="conjgrad evaluation limit per request")
+    ap.add_argument("--serve-rates", type=float, nargs="*", default=[10.0, 100.0, 1000.0, 2000.0])
     args = ap.parse_args()
     rank, world, local = rank_info()
     cores = os.cpu_count() or 1
