@@ -155,6 +155,45 @@ def timed(fn, reps, stream, flush):
     return [a.elapsed_time(c) for a, c in ev]
 
 
+def uneven_sizes(n):
+    """Atom counts of the uneven-size batch: log-uniform 200..20,000."""
+    rng = np.random.default_rng(4242)
+    return np.floor(np.exp(rng.uniform(np.log(200), np.log(20000), n))).astype(int)
+
+
+def bench_uneven_alone(args, stream, sp, flush):
+    """The uneven-size batch's evaluations alone (no plain loop, no oracle):
+    for profiling the batched GBneck evaluation by itself."""
+    import torch
+    from nabc_gb300.batch import Batch
+    sizes = uneven_sizes(args.uneven)
+    mols = make_molecules(sizes, 9000)
+    b = Batch(UNEVEN_OPTS + (", sffg_tune=0" if args.no_tune else ""))
+    for prm, x, _ in mols:
+        b.add(prm, x)
+    b.finalize()
+    b.eval(rebuild=True, stream=sp)
+    b.eval(stream=sp)
+    torch.cuda.synchronize()
+    t = timed(lambda: b.eval(stream=sp), max(1, args.steps), stream, flush)
+    res = {"systems": len(sizes), "atoms": int(sizes.sum()), "options": UNEVEN_OPTS, "evals": len(t),
+           "ms_per_eval_of_all": float(np.median(t)), "tuned_split_claim_blocks": b.tuned_split()}
+    if args.uneven_md > 0:
+        # md steps of every molecule at once (the integrator's kernels at
+        # millions of atoms)
+        b.md_begin(stream=sp)
+        steps = [0]
+
+        def one():
+            b.md_steps(steps[0], 1, stream=sp)
+            steps[0] += 1
+        tm = timed(one, args.uneven_md, stream, flush)
+        res["md_steps"] = len(tm)
+        res["ms_per_md_step_of_all"] = float(np.median(tm))
+    b.close()
+    return res
+
+
 def bench_batched(args, stream, sp, flush):
     """Batched versus plain evaluation on the GPU: many systems in one
     flattened work queue (one Batch) against one Batch per system evaluated
@@ -194,8 +233,7 @@ def bench_batched(args, stream, sp, flush):
         return b, plain, res
 
     # uneven-size batch: log-uniform 200..20,000 atoms, each its own topology
-    rng = np.random.default_rng(4242)
-    sizes = np.floor(np.exp(rng.uniform(np.log(200), np.log(20000), args.uneven))).astype(int)
+    sizes = uneven_sizes(args.uneven)
     mols = make_molecules(sizes, 9000)
     b, plain, res = compare(UNEVEN_OPTS, [(prm, x) for prm, x, _ in mols], 3, "uneven")
     # accuracy of the smallest, the median and the largest molecule against
@@ -334,14 +372,18 @@ def bench_serving(args):
            "rmsgrad": 0.01, "maxiter": args.serve_maxiter, "memory_budget_gb": 150.0}
     # plain: one request at a time
     t0 = time.perf_counter()
+    plain_ms = []
     for prm, x, _ in mols:
+        t1 = time.perf_counter()
         b = Batch(SERVE_OPTS)
         b.add(prm, x)
         b.finalize()
         b.cg(args.serve_maxiter, 0.01)
         b.close()
+        plain_ms.append(round((time.perf_counter() - t1) * 1e3, 1))
     plain_s = time.perf_counter() - t0
     out["plain_requests_per_s"] = n / plain_s
+    out["plain_ms_per_request"] = plain_ms
     rates = []
     for rate in args.serve_rates:
         arrive = np.cumsum(rng.exponential(1.0 / rate, n))
@@ -363,11 +405,15 @@ def bench_serving(args):
         span = time.perf_counter() - t0
         res = [s.result(i) for i in ids]
         lat = np.array([r["latency_ms"] for r in res])
+        adm = s.counts()
         s.close()
         codes, counts = np.unique([r["status"] for r in res], return_counts=True)
         rates.append({"arrival_per_s": rate, "throughput_requests_per_s": n / span,
                       "p50_ms": float(np.percentile(lat, 50)), "p99_ms": float(np.percentile(lat, 99)),
-                      "conjgrad_returns": {str(int(c)): int(k) for c, k in zip(codes, counts)}})
+                      "conjgrad_returns": {str(int(c)): int(k) for c, k in zip(codes, counts)},
+                      "admission": adm,
+                      "per_request": [{"atoms": int(sizes[i]), "status": int(res[i]["status"]),
+                                       "latency_ms": round(float(res[i]["latency_ms"]), 1)} for i in range(n)]})
     out["served"] = rates
     out["atoms"] = [int(v) for v in sizes]
     return out
@@ -547,6 +593,9 @@ def main():
     ap.add_argument("--serve-max-atoms", type=int, default=50000, help="requests log-uniform in 500 .. this")
     ap.add_argument("--serve-maxiter", type=int, default=2000, help="conjgrad evaluation limit per request")
     ap.add_argument("--serve-rates", type=float, nargs="*", default=[10.0, 100.0, 1000.0, 2000.0])
+    ap.add_argument("--uneven-md", type=int, default=0, help="with --only uneven: md steps of the whole batch")
+    ap.add_argument("--only", choices=["serving", "batched", "uneven"],
+                    help="run only this section and print its JSON (for profiling it alone)")
     args = ap.parse_args()
     rank, world, local = rank_info()
     cores = os.cpu_count() or 1
@@ -566,6 +615,18 @@ def main():
     from nabc_gb300.batch import Batch
     sff.lib()
     sff.set_output(os.devnull)
+    if args.only:
+        stream = torch.cuda.Stream()
+        torch.cuda.set_stream(stream)
+        flush = torch.empty(256 * 1024 * 1024 // 4, dtype=torch.float32, device="cuda")
+        if args.only == "serving":
+            out = bench_serving(args)
+        elif args.only == "uneven":
+            out = bench_uneven_alone(args, stream, C.c_void_p(stream.cuda_stream), flush)
+        else:
+            out = bench_batched(args, stream, C.c_void_p(stream.cuda_stream), flush)
+        print(json.dumps({args.only: out}))
+        return
     seed = args.seed + rank  # each replica its own molecule
     cfg, mol = workload(args.natom, seed, world)
     prm, x, _ = sff.synth_molecule(args.natom, seed)

@@ -32,6 +32,7 @@ extern "C" {
 #define SFFG_ESTATE (-4)    /* call not valid in the handle's current state */
 #define SFFG_ENONFINITE (-5) /* non-finite coordinates or energy in a system */
 #define SFFG_ENODEV (-6)    /* no usable CUDA device */
+#define SFFG_ECONSTRAINT (-7) /* RATTLE's sweeps reached their limit in md (the reference stops there) */
 
 /* Energy components of one system, in the reference's ene[] layout
  * (src/sff/eff.c:2864-2874): 0 total, 1 vdW, 2 elec, 3 bond, 4 angle,
@@ -85,10 +86,13 @@ int sffg_batch_get_energy(sffg_batch *b, int sys, double *ene, void *stream);
 int sffg_batch_get_grad(sffg_batch *b, int sys, double *g, void *stream);
 /* Effective Born radii of the last evaluation, in atom order. */
 int sffg_batch_get_reff(sffg_batch *b, int sys, double *reff, void *stream);
-/* Per-system status: status[s] is SFFG_OK, or SFFG_ENONFINITE once an
+/* Per-system status: status[s] is SFFG_OK; SFFG_ENONFINITE once an
  * evaluation met a non-finite coordinate of system s (its results are then
- * meaningless; the other systems' results are unaffected).  Setting the
- * system's coordinates again clears it.  Synchronises the stream. */
+ * meaningless; the other systems' results are unaffected; setting the
+ * system's coordinates again clears it); or SFFG_ECONSTRAINT once RATTLE's
+ * sweeps (md with the option rattle = 1 or 2) reached their limit of 1,000
+ * for system s, where the reference stops with "ERROR in RATTLE".
+ * Synchronises the stream. */
 int sffg_batch_status(sffg_batch *b, int *status, void *stream);
 
 /* Number of unordered pairs on the current pair lists of one system. */
@@ -96,7 +100,10 @@ long long sffg_batch_num_pairs(sffg_batch *b, int sys);
 
 /* Langevin md() on every system with device Philox noise (the reference's
  * integrator, src/sff/sff.c:2223-2354, options dt/temp0/gamma_ln/...).
- * Velocities start at zero unless set with sffg_batch_set_velocities. */
+ * Velocities start at zero unless set with sffg_batch_set_velocities.  With
+ * the option rattle = 1 (all bonds) or 2 (bonds to hydrogen) every system's
+ * bond lengths are held by RATTLE (src/sff/rattle.c) on the device, with the
+ * reference's sweep order and arithmetic. */
 int sffg_batch_md(sffg_batch *b, int nsteps, void *stream);
 /* The same integrator split for callers that drive it step by step: md_begin
  * evaluates the first force and initial accelerations; md_steps advances
@@ -208,14 +215,20 @@ int sffg_batch_destroy(sffg_batch *b);
 /* A request loop with continuous batching (no counterpart in the
  * reference).  Requests -- a minimisation (the reference's conjgrad() to
  * rmsgrad or nsteps evaluations) or nsteps of Langevin md with the batch
- * integrator -- wait in arrival order; every sffg_server_pump admits the
- * waiting requests at the head of the queue that fit the device-memory
- * budget as a new group (one batch on its own stream, resident until the
- * group ends), advances every running group by `turns` evaluations or
- * steps without waiting between groups, so their work overlaps on the GPU,
- * and takes the result of every system that ended.  A result is the same
- * whether the request ran alone or among others.  All requests of a server
- * share its model options.  Not thread-safe: one thread drives a server. */
+ * integrator -- are admitted in arrival order while they fit the
+ * device-memory budget.  Requests run in groups, one batch on its own
+ * stream each.  A minimisation joins the running minimisation group: it
+ * enters that batch's flattened work queue at the group's next turn that is
+ * a multiple of nsnb, where the running systems move into a new batch with
+ * the newcomers.  With no such group, or for md, it starts a new group.
+ * (Option sffg_serve_classes=1: one minimisation group per size class --
+ * under 4,096 atoms, then one class per doubling.)
+ * Every sffg_server_pump launches the next `turns` evaluations or steps of
+ * every group whose earlier turns have finished, waits until some group's
+ * turns finish, and takes the result of every system that ended.  A result
+ * is the same whether the request ran alone or among others, and whether
+ * it joined or started a group.  All requests of a server share its model
+ * options.  Not thread-safe: one thread drives a server. */
 #define SFFG_REQ_MINIMIZE 0
 #define SFFG_REQ_MD 1
 
@@ -229,8 +242,8 @@ int sffg_server_create(const char *opts, double memory_budget_gb, int max_groups
  * identifies it.  SFFG_ENOMEM when the request alone exceeds the budget. */
 int sffg_server_submit(sffg_server *s, PARMSTRUCT_T *prm, const double *x, int kind, int nsteps, double rmsgrad,
                        long long *id);
-/* Admit, advance, collect; reports the groups running and the requests
- * waiting. */
+/* Admit, launch, wait for one group, collect; reports the groups running
+ * and the requests waiting. */
 int sffg_server_pump(sffg_server *s, int turns, int *nrunning, int *npending);
 /* The result of a finished request: the driver's return code (conjgrad's,
  * or the steps run for md), final energy, coordinates (3*Natom, may be
@@ -239,6 +252,12 @@ int sffg_server_pump(sffg_server *s, int turns, int *nrunning, int *npending);
 int sffg_server_result(sffg_server *s, long long id, int *status, double *energy, double *x, double *latency_ms);
 /* Device memory the running groups hold (bytes). */
 size_t sffg_server_device_bytes(const sffg_server *s);
+/* Counts since creation (any pointer may be NULL): groups started, joins
+ * (a running group's batch formed again with newcomers), requests that
+ * entered a running group by a join, and the host milliseconds spent
+ * forming batches (starts and joins). */
+int sffg_server_counts(const sffg_server *s, long long *groups_started, long long *joins, long long *joined,
+                       double *form_ms);
 /* The most recent failure of this server. */
 const char *sffg_server_error(const sffg_server *s);
 int sffg_server_destroy(sffg_server *s);

@@ -69,6 +69,7 @@ struct DeviceState {
   DBuf<int> param, slot_atom;
   DBuf<float> q32, reff32, rinv2, sumda32;
   DBuf<double> rborn64, q64, alpha, beta, gamma, reff64, psi64, chainfac;
+  DBuf<double2> rinv64;  // 1 / (rborn - offset), 1 / rborn
   DBuf<long long> acc_sumi, acc_sd, acc_fx, acc_fy, acc_fz;
   // per tile
   DBuf<unsigned> tile_valid;
@@ -81,6 +82,8 @@ struct DeviceState {
   DBuf<int> sys_natom, sys_atom_off;
   DBuf<float2> lj;
   DBuf<double2> lj64;  // the same table in FP64 (close pairs)
+  DBuf<float2> sys_born;  // (rgbmax + Fsmax)^2, polynomial-tail flag (DevTables::sys_born)
+  DBuf<float> sys_gbb2;   // (rgbmax + Fsmax + skin)^2: lists B and C
   DBuf<long long> energy;
   DBuf<double> etot;
   // per atom
@@ -115,6 +118,12 @@ struct DeviceState {
   DBuf<float> neck_pos, neck_val;
   // dynamics
   DBuf<double> tscal, noise, rndf;
+  // RATTLE (option rattle = 1 or 2): the constrained bonds of every system
+  // by level (k_rattle), the coordinates before each drift, and a status
+  // word per system
+  DBuf<int2> rat_atoms;
+  DBuf<double> rat_req, xold;
+  DBuf<int> rat_level, rat_sys_level, rat_status;
   DBuf<long long> ekin, ekin_last;  // the step's kinetic sum, and the last finished step's
   // minimisation
   DBuf<double> cg_w;
@@ -148,12 +157,12 @@ struct DeviceState {
     // DBuf members release in their own destructors? they are PODs: free here
     auto rel = [](auto &b) { b.release(); };
     rel(pos_hi); rel(pos_lo); rel(gbpar); rel(param); rel(slot_atom); rel(q32); rel(reff32);
-    rel(rinv2); rel(sumda32); rel(rborn64); rel(q64); rel(alpha); rel(beta); rel(gamma);
+    rel(rinv2); rel(sumda32); rel(rborn64); rel(rinv64); rel(q64); rel(alpha); rel(beta); rel(gamma);
     rel(reff64); rel(psi64); rel(chainfac); rel(acc_sumi); rel(acc_sd); rel(acc_fx); rel(acc_fy);
     rel(acc_fz); rel(tile_valid); rel(tile_sys); rel(box_lo); rel(box_hi); rel(excl_tile_start);
     rel(excl_tile_j); rel(excl_tile_idx); rel(excl_masks); rel(sys_active); rel(sys_lj_off);
     rel(sys_ntypes); rel(sys_tile_end); rel(sys_has_frozen); rel(nonfinite); rel(sys_natom);
-    rel(sys_atom_off); rel(lj); rel(lj64); rel(energy); rel(etot); rel(x); rel(grad); rel(v); rel(accel);
+    rel(sys_atom_off); rel(lj); rel(lj64); rel(sys_born); rel(sys_gbb2); rel(energy); rel(etot); rel(x); rel(grad); rel(v); rel(accel);
     rel(minv); rel(sqrmass); rel(atom_slot); rel(atom_sys); rel(atom_frozen); rel(bond_atoms);
     rel(bond_par); rel(angle_par); rel(angle_atoms); rel(dih_atoms); rel(p14_atoms); rel(dih_par);
     rel(p14_par); rel(cand); rel(cand_n); rel(cand_off); rel(colA); rel(colB); rel(colC); rel(colE);
@@ -162,7 +171,8 @@ struct DeviceState {
     rel(chunkC_i); rel(entC_slot); rel(entA_col); rel(entA_exc); rel(entB_col); rel(entC_col);
     rel(colK); rel(entA_close);
     rel(xb); rel(counters); rel(step); rel(cg_nactive); rel(sys_key); rel(tile_flagB); rel(cons_w); rel(cons_x0); rel(neck_pos); rel(neck_val); rel(tscal);
-    rel(noise); rel(rndf); rel(ekin); rel(ekin_last); rel(cg_w); rel(cg_state);
+    rel(noise); rel(rndf); rel(rat_atoms); rel(rat_req); rel(xold); rel(rat_level); rel(rat_sys_level);
+    rel(rat_status); rel(ekin); rel(ekin_last); rel(cg_w); rel(cg_state);
   }
 };
 
@@ -231,6 +241,12 @@ int Batch::add_host_system(HostSystem hs, const double *x) {
 }
 
 namespace {
+
+// Squared list-B cutoff: rgbmax + Fsmax + skin.
+double list_b_cut2(const ModelParams &mp, double fsmax) {
+  const double c = mp.rgbmax + fsmax + kListSkin;
+  return c * c;
+}
 
 // Tile order: recursive balanced bisection of the atoms along the longest
 // extent of each group, the first part holding a whole number of 32-atom
@@ -308,12 +324,14 @@ int Batch::upload() {
   std::vector<float> q32(nslot_, 0.f);
   std::vector<float4> gbpar(nslot_, make_float4(1.f, 0.f, 1.f, 0.f));
   std::vector<double> rb64(nslot_, 1.0), q64(nslot_, 0.0), al(nslot_, 0.0), be(nslot_, 0.0), ga(nslot_, 0.0);
+  std::vector<double2> rinv64(nslot_, make_double2(1.0, 1.0));
   std::vector<int> atom_slot(natom_total_), atom_sys(natom_total_), atom_frozen(natom_total_);
   std::vector<double> x(3 * static_cast<size_t>(natom_total_)), minv(3 * static_cast<size_t>(natom_total_)),
       sqrmass(3 * static_cast<size_t>(natom_total_));
   std::vector<int> sys_tile_end(nsys), sys_has_frozen(nsys), sys_ntypes(nsys), sys_lj_off(nsys),
       sys_natom(nsys), sys_atom_off(nsys);
-  std::vector<float2> lj;
+  std::vector<float2> lj, sys_born(nsys);
+  std::vector<float> sys_gbb2(nsys);
   std::vector<double2> lj64;
   std::map<std::vector<double>, int> lj_dedupe;
   std::vector<int> excl_tile_start(ntile_ + 1, 0);
@@ -336,6 +354,7 @@ int Batch::upload() {
     bisect_tiles(xs.data(), order.data(), n);
     std::vector<int> local_slot(n);
     for (int k = 0; k < n; k++) local_slot[order[k]] = k;
+    double smax = 0.0;  // largest |s| = |fs (rborn - offset)| of the system's atoms
     for (int i = 0; i < n; i++) {
       const int sl = si.slot_off + local_slot[i];
       const int a = si.atom_off + i;
@@ -347,11 +366,12 @@ int Batch::upload() {
       const float sf = static_cast<float>(sd);
       const float scorr = sf != 0.0f ? static_cast<float>(3.0 * (sd - static_cast<double>(sf)) / sf) : 0.0f;
       gbpar[sl] = make_float4(static_cast<float>(rho), sf, static_cast<float>(hs.rborn[i]), scorr);
-      smax_abs_ = std::max(smax_abs_, std::fabs(sd));
+      smax = std::max(smax, std::fabs(sd));
       param[sl] = (hs.type[i] & 0xffff) | (hs.neck[i] << 16) | (hs.frozen[i] ? (1 << 24) : 0);
       q32[sl] = static_cast<float>(hs.q[i]);
       q64[sl] = hs.q[i];
       rb64[sl] = hs.rborn[i];
+      rinv64[sl] = make_double2(1.0 / (hs.rborn[i] - off), 1.0 / hs.rborn[i]);
       al[sl] = hs.alpha[i];
       be[sl] = hs.beta[i];
       ga[sl] = hs.gamma[i];
@@ -370,6 +390,10 @@ int Batch::upload() {
     sys_tile_end[s] = si.tile_off + si.ntile;
     sys_has_frozen[s] = si.has_frozen;
     sys_ntypes[s] = hs.ntypes;
+    // a tail pair has q = (rgbmax - d + s_j) / rgbmax <= 2 |s_j| / rgbmax
+    const double rc = mp_.rgbmax + si.fsmax;
+    sys_born[s] = make_float2(static_cast<float>(rc * rc), 2.0 * smax <= 0.3 * mp_.rgbmax * 0.999 ? 1.0f : 0.0f);
+    sys_gbb2[s] = static_cast<float>(std::min(list_b_cut2(mp_, si.fsmax), 1e30));
     sys_natom[s] = n;
     sys_atom_off[s] = si.atom_off;
     {
@@ -451,6 +475,7 @@ int Batch::upload() {
   SFFG_CK(up(d.q32, q32));
   SFFG_CK(up(d.gbpar, gbpar));
   SFFG_CK(up(d.rborn64, rb64));
+  SFFG_CK(up(d.rinv64, rinv64));
   SFFG_CK(up(d.q64, q64));
   SFFG_CK(up(d.alpha, al));
   SFFG_CK(up(d.beta, be));
@@ -460,6 +485,8 @@ int Batch::upload() {
   SFFG_CK(up(d.sys_tile_end, sys_tile_end));
   SFFG_CK(up(d.sys_has_frozen, sys_has_frozen));
   SFFG_CK(up(d.sys_ntypes, sys_ntypes));
+  SFFG_CK(up(d.sys_born, sys_born));
+  SFFG_CK(up(d.sys_gbb2, sys_gbb2));
   SFFG_CK(up(d.sys_lj_off, sys_lj_off));
   SFFG_CK(up(d.sys_natom, sys_natom));
   SFFG_CK(up(d.sys_atom_off, sys_atom_off));
@@ -561,14 +588,60 @@ int Batch::upload() {
   SFFG_CK(d.ekin.alloc(nsys));
   SFFG_CK(d.ekin_last.alloc(nsys));
   {
-    // kinetic degrees of freedom per system: 3N minus frozen (sff.c:2142)
+    // kinetic degrees of freedom per system: 3N minus frozen, minus one per
+    // RATTLE constraint (sff.c:2142-2146)
     std::vector<double> rndf(nsys);
     for (int s = 0; s < nsys; s++) {
       int nf = 0;
       for (int f : sys_[s].frozen) nf += f != 0;
-      rndf[s] = 3.0 * sys_[s].natom - 3.0 * nf;
+      rndf[s] = 3.0 * sys_[s].natom - 3.0 * nf - rattle_bonds(s);
     }
     SFFG_CK(up(d.rndf, rndf));
+  }
+  if (opts_.irattle) {
+    // level schedule of each system's constrained bonds: a bond's level is
+    // one more than the highest level of the earlier bonds sharing an atom
+    // with it; the bonds then go level by level, in the reference's order
+    // within a level
+    std::vector<int2> atoms;
+    std::vector<double> req;
+    std::vector<int> level_start, sys_level(nsys + 1);
+    for (int s = 0; s < nsys; s++) {
+      const HostSystem &hs = host_[s];
+      const int nb = rattle_bonds(s), ao = 3 * sys_[s].atom_off;
+      std::vector<int> last(hs.natom, 0), lev(nb);
+      int nlev = 0;
+      for (int k = 0; k < nb; k++) {
+        const HostSystem::Bond &b = hs.rattle_bonds[k];
+        const int l = std::max(last[b.a], last[b.b]);
+        lev[k] = l;
+        last[b.a] = last[b.b] = l + 1;
+        nlev = std::max(nlev, l + 1);
+      }
+      std::vector<int> start(nlev + 1, 0);
+      for (int k = 0; k < nb; k++) start[lev[k] + 1]++;
+      for (int l = 0; l < nlev; l++) start[l + 1] += start[l];
+      const int base = static_cast<int>(atoms.size());
+      sys_level[s] = static_cast<int>(level_start.size());
+      for (int l = 0; l < nlev; l++) level_start.push_back(base + start[l]);
+      atoms.resize(base + nb);
+      req.resize(base + nb);
+      for (int k = 0; k < nb; k++) {
+        const HostSystem::Bond &b = hs.rattle_bonds[k];
+        const int at = base + start[lev[k]]++;
+        atoms[at] = make_int2(ao + 3 * b.a, ao + 3 * b.b);
+        req[at] = b.req;
+      }
+    }
+    sys_level[nsys] = static_cast<int>(level_start.size());
+    level_start.push_back(static_cast<int>(atoms.size()));
+    SFFG_CK(up(d.rat_atoms, atoms));
+    SFFG_CK(up(d.rat_req, req));
+    SFFG_CK(up(d.rat_level, level_start));
+    SFFG_CK(up(d.rat_sys_level, sys_level));
+    SFFG_CK(d.rat_status.alloc(nsys));
+    SFFG_CK(cudaMemset(d.rat_status.p, 0, d.rat_status.bytes()));
+    SFFG_CK(d.xold.alloc(3 * static_cast<size_t>(natom_total_)));
   }
   std::vector<double> onesd(nsys, 1.0);
   SFFG_CK(cudaMemcpy(d.tscal.p, onesd.data(), nsys * sizeof(double), cudaMemcpyHostToDevice));
@@ -801,10 +874,13 @@ int Batch::system_status(std::vector<int> &status, void *stream) {
   const int nsys = num_systems();
   std::vector<int> bad(nsys);
   cudaStream_t st = pick(*d_, stream);
+  std::vector<int> rat(nsys, 0);
   SFFG_CK(cudaMemcpyAsync(bad.data(), d_->nonfinite.p, nsys * sizeof(int), cudaMemcpyDeviceToHost, st));
+  if (d_->rat_status.p)
+    SFFG_CK(cudaMemcpyAsync(rat.data(), d_->rat_status.p, nsys * sizeof(int), cudaMemcpyDeviceToHost, st));
   SFFG_CK(cudaStreamSynchronize(st));
   status.resize(nsys);
-  for (int s = 0; s < nsys; s++) status[s] = bad[s] ? SFFG_ENONFINITE : SFFG_OK;
+  for (int s = 0; s < nsys; s++) status[s] = bad[s] ? SFFG_ENONFINITE : rat[s] ? SFFG_ECONSTRAINT : SFFG_OK;
   return SFFG_OK;
 }
 
@@ -851,7 +927,7 @@ int Batch::get_all_energies(std::vector<double> &out, void *stream) {
   return SFFG_OK;
 }
 
-DevTables make_tables(DeviceState &d, const ModelParams &mp, double fsmax, int queue) {
+DevTables make_tables(DeviceState &d, const ModelParams &mp, int queue) {
   DevTables t;
   t.pos_hi = d.pos_hi.p;
   t.pos_lo = d.pos_lo.p;
@@ -866,6 +942,7 @@ DevTables make_tables(DeviceState &d, const ModelParams &mp, double fsmax, int q
   t.sys_active = d.sys_active.p;
   t.sys_lj_off = d.sys_lj_off.p;
   t.sys_ntypes = d.sys_ntypes.p;
+  t.sys_born = d.sys_born.p;
   t.lj = d.lj.p;
   t.lj64 = d.lj64.p;
   t.lj_n = static_cast<int>(d.lj.n);
@@ -899,8 +976,7 @@ DevTables make_tables(DeviceState &d, const ModelParams &mp, double fsmax, int q
   t.born.rgbmax = static_cast<float>(mp.rgbmax);
   t.born.rgbmax1i = static_cast<float>(1.0 / mp.rgbmax);
   t.born.rgbmax2i = static_cast<float>(1.0 / (mp.rgbmax * mp.rgbmax));
-  t.born.cutoff2 = static_cast<float>((mp.rgbmax + fsmax) * (mp.rgbmax + fsmax));
-  t.born.tail_poly_only = 0;
+  t.born.cutoff2 = 0.0f;  // per system: sys_born
   t.pair.kappa_s = static_cast<float>(mp.kappa * kKscale);
   t.pair.inv_epsext = static_cast<float>(1.0 / mp.epsext);
   t.pair.dielfac0 = static_cast<float>(1.0 - 1.0 / mp.epsext);
@@ -912,12 +988,6 @@ DevTables make_tables(DeviceState &d, const ModelParams &mp, double fsmax, int q
 
 namespace {
 
-// Squared list-B cutoff: rgbmax + Fsmax + skin.
-double list_b_cut2(const ModelParams &mp, double fsmax) {
-  const double c = mp.rgbmax + fsmax + kListSkin;
-  return c * c;
-}
-
 template <class T>
 cudaError_t ensure(DBuf<T> &b, size_t n) {
   if (b.n >= n) return cudaSuccess;
@@ -926,7 +996,7 @@ cudaError_t ensure(DBuf<T> &b, size_t n) {
 
 }  // namespace
 
-ListArgs Batch::list_args(double fsmax) {
+ListArgs Batch::list_args() {
   DeviceState &d = *d_;
   ListArgs a;
   a.pos_hi = d.pos_hi.p;
@@ -947,7 +1017,7 @@ ListArgs Batch::list_args(double fsmax) {
   a.ntile = ntile_;
   a.cut2f = static_cast<float>(mp_.cut * mp_.cut);
   a.cut2 = mp_.cut * mp_.cut;
-  a.gbb2f = static_cast<float>(std::min(list_b_cut2(mp_, fsmax), 1e30));
+  a.sys_gbb2 = d.sys_gbb2.p;
   a.cand = d.cand.p;
   a.cand_cap = static_cast<int>(d.cand.n);
   a.ent_cap = static_cast<int>(std::min<size_t>(d.entA_slot.n / 32, 0x7fffffff));
@@ -991,12 +1061,6 @@ ListArgs Batch::list_args(double fsmax) {
   return a;
 }
 
-double Batch::fsmax_all() const {
-  double f = 0.0;
-  for (auto &sy : sys_) f = std::max(f, sy.fsmax);
-  return f;
-}
-
 // The pair lists from the current coordinates (lists.cuh, stages 1-6).
 // Synchronous form: the host reads two counts back (candidates, chunks) to
 // size the stores exactly; the first build, and any build asked to, takes
@@ -1008,13 +1072,12 @@ int Batch::build_lists(void *stream) {
   cudaStream_t st = pick(d, stream);
   if (queued_builds_ && sized_ && !force_sync_build_) return build_lists_queued(st);
   force_sync_build_ = false;
-  const double fsmax = fsmax_all();
   const int tile_blocks = (ntile_ * 32 + 255) / 256;
   if (d.cand.n == 0) SFFG_CK(d.cand.alloc(static_cast<size_t>(std::min<long long>(cand_max_, 64LL * ntile_ + 1024))));
   int c[2] = {0, 0};
   for (int attempt = 0;; attempt++) {
     SFFG_CK(cudaMemsetAsync(d.counters.p, 0, 2 * sizeof(int), st));
-    k_list_candidates<<<tile_blocks, 256, 0, st>>>(list_args(fsmax));
+    k_list_candidates<<<tile_blocks, 256, 0, st>>>(list_args());
     SFFG_CK(cudaGetLastError());
     launches_++;
     SFFG_CK(cudaMemcpyAsync(c, d.counters.p, sizeof(c), cudaMemcpyDeviceToHost, st));
@@ -1041,7 +1104,7 @@ int Batch::build_lists(void *stream) {
   SFFG_CK(ensure(d.cand_off, nc));
   const int cand_blocks = static_cast<int>(std::min<long long>((static_cast<long long>(nc) * 32 + 255) / 256, 16LL * d.nsm));
   {
-    ListArgs a = list_args(fsmax);
+    ListArgs a = list_args();
     a.ent_cap = 0x7fffffff;  // the entry stores are sized below, from the count
     k_list_columns<false><<<cand_blocks, 256, 0, st>>>(a);
     k_list_offsets<false><<<tile_blocks, 256, 0, st>>>(a);
@@ -1069,7 +1132,7 @@ int Batch::build_lists(void *stream) {
   SFFG_CK(ensure(d.entC_col, ne));
   SFFG_CK(ensure(d.chunkC_i, ne / 32));
   {
-    const ListArgs a = list_args(fsmax);
+    const ListArgs a = list_args();
     k_list_fill<false><<<cand_blocks, 256, 0, st>>>(a);
     k_list_pad<false><<<tile_blocks, 256, 0, st>>>(a);
     k_list_done<<<(a.ntile + 255) / 256, 256, 0, st>>>(a.flagB, a.tile_flagB, a.ntile);
@@ -1093,7 +1156,6 @@ int Batch::build_lists(void *stream) {
 // (eval_checked, md_steps).
 int Batch::build_lists_queued(cudaStream_t st) {
   DeviceState &d = *d_;
-  const double fsmax = fsmax_all();
   const int tile_blocks = (ntile_ * 32 + 255) / 256;
   // grown (to 150% of the last count) only once the headroom falls below
   // 25%: a store that moves frees the old one, which waits for the device,
@@ -1126,7 +1188,7 @@ int Batch::build_lists_queued(cudaStream_t st) {
   if (!d.list_ev) SFFG_CK(cudaEventCreateWithFlags(&d.list_ev, cudaEventDisableTiming));
   if (!d.list_host) SFFG_CK(cudaHostAlloc(reinterpret_cast<void **>(&d.list_host), 16 * sizeof(int), cudaHostAllocDefault));
   // the smallest store of each kind sets the capacity the stages check
-  ListArgs a = list_args(fsmax);
+  ListArgs a = list_args();
   a.cand_cap = static_cast<int>(std::min({d.cand.n, d.cand_n.n, d.cand_off.n, d.colA.n / 32, d.colB.n / 32,
                                           d.colC.n / 32, d.colK.n / 32, d.colE.n / 32}));
   a.ent_cap = static_cast<int>(std::min({d.entA_slot.n, d.entA_col.n, d.entA_exc.n, d.entA_close.n, d.entB_slot.n,
@@ -1236,7 +1298,7 @@ void Batch::rebuild_list_b(void *stream) {
   cudaStream_t st = pick(d, stream);
   const int tile_blocks = (ntile_ * 32 + 255) / 256;
   const int cand_blocks = 16 * d.nsm;  // grid-stride over the candidates (fixed, for graph capture)
-  const ListArgs a = list_args(fsmax_all());
+  const ListArgs a = list_args();
   launch_pdl(k_list_columns<true>, cand_blocks, 256, st, a);
   launch_pdl(k_list_offsets<true>, tile_blocks, 256, st, a);
   launch_pdl(k_list_scan<true>, 1, 1024, st, a);
@@ -1426,7 +1488,6 @@ int Batch::run_eval_direct(bool rebuild, void *stream) {
     rebuild_list_b(st);
     SFFG_CK(cudaGetLastError());
   }
-  const double fsmax = fsmax_all();
   // pass 1
   const bool neck = mp_.gb == 7 || mp_.gb == 8;
   const int ring = static_cast<int>(d.ev_head % DeviceState::kRing);
@@ -1435,8 +1496,7 @@ int Batch::run_eval_direct(bool rebuild, void *stream) {
     SFFG_CK(cudaEventRecord(d.events[ring][0][0], st));
   }
   {
-    DevTables t = make_tables(d, mp_, fsmax, 5);
-    t.born.tail_poly_only = 2.0 * smax_abs_ <= 0.3 * mp_.rgbmax * 0.999;
+    DevTables t = make_tables(d, mp_, 5);
     t.claim = cfg_[0].claim;
     if (tuning_) SFFG_CK(cudaEventRecord(d.tune_ev[0][0], st));
     {
@@ -1458,6 +1518,7 @@ int Batch::run_eval_direct(bool rebuild, void *stream) {
     f.sys_active = d.sys_active.p;
     f.param = d.param.p;
     f.rborn64 = d.rborn64.p;
+    f.rinv64 = d.rinv64.p;
     f.q64 = d.q64.p;
     f.alpha = d.alpha.p;
     f.beta = d.beta.p;
@@ -1478,7 +1539,7 @@ int Batch::run_eval_direct(bool rebuild, void *stream) {
   // pass 2
   if (profile_) SFFG_CK(cudaEventRecord(d.events[ring][1][0], st));
   {
-    DevTables t = make_tables(d, mp_, fsmax, 6);
+    DevTables t = make_tables(d, mp_, 6);
     t.claim = cfg_[1].claim;
     t.lj_shared = opts_.sffg_lj_shared != 0;
     if (tuning_) SFFG_CK(cudaEventRecord(d.tune_ev[1][0], st));
@@ -1495,8 +1556,7 @@ int Batch::run_eval_direct(bool rebuild, void *stream) {
   // pass 3
   if (profile_) SFFG_CK(cudaEventRecord(d.events[ring][2][0], st));
   {
-    DevTables t = make_tables(d, mp_, fsmax, 7);
-    t.born.tail_poly_only = 2.0 * smax_abs_ <= 0.3 * mp_.rgbmax * 0.999;
+    DevTables t = make_tables(d, mp_, 7);
     t.claim = cfg_[2].claim;
     if (tuning_) SFFG_CK(cudaEventRecord(d.tune_ev[2][0], st));
     {
@@ -1641,6 +1701,7 @@ static void md_args(Batch &b, DeviceState &d, const Options &o, int natom_total,
   a.step = d.step.p;
   a.sys_atom_off = d.sys_atom_off.p;
   a.sys_key = d.sys_key.p;
+  a.xold = o.irattle ? d.xold.p : nullptr;
   c_ave = gammai > 0.0 ? 1.0 + gammai * dt5 : 1.0;
   (void)b;
 }
@@ -1730,8 +1791,28 @@ int Batch::md_steps(int step0, int k, NoiseFn noise, void *noise_ctx, void *stre
   step_host_ = static_cast<unsigned>(step0 + 1);
   SFFG_CK(cudaMemcpyAsync(d.step.p, &step_host_, sizeof(unsigned), cudaMemcpyHostToDevice, st));
   // one step after the drift: evaluation, kick, kinetic energy, counter
+  RattleArgs ra;
+  if (opts_.irattle) {
+    ra.x = d.x.p;
+    ra.v = d.v.p;
+    ra.xold = d.xold.p;
+    ra.minv = d.minv.p;
+    ra.atoms = d.rat_atoms.p;
+    ra.req = d.rat_req.p;
+    ra.level = d.rat_level.p;
+    ra.sys_level = d.rat_sys_level.p;
+    ra.sys_active = d.sys_active.p;
+    ra.status = d.rat_status.p;
+    ra.dt = a.dtx;
+  }
   auto step_body = [&](cudaStream_t s, bool rebuild, bool capturing) -> int {
     launch_pdl(k_md_drift, nb, 256, s, a);
+    if (opts_.irattle) {
+      // the reference keeps the position tolerance in single precision
+      ra.eps = static_cast<double>(static_cast<float>(0.0000001));
+      launch_pdl(k_rattle<false>, nsys, kRattleThreads, s, ra);
+      launches_++;
+    }
     int r = capturing ? run_eval_direct(false, s) : run_eval(rebuild, s);
     if (r) return r;
     if (noise && a.gammai != 0.0) {
@@ -1739,6 +1820,12 @@ int Batch::md_steps(int step0, int k, NoiseFn noise, void *noise_ctx, void *stre
       a.noise = d.noise.p;
     }
     launch_pdl(k_md_kick, nb, 256, s, a, 0);
+    if (opts_.irattle) {
+      ra.eps = 0.0000001 / a.dtx;
+      launch_pdl(k_rattle<true>, nsys, kRattleThreads, s, ra);
+      launch_pdl(k_md_ekin, nb, 256, s, a);
+      launches_ += 2;
+    }
     launch_pdl(k_md_tscal, (nsys + 127) / 128, 128, s, d.ekin.p, d.ekin_last.p, d.tscal.p,
                static_cast<double *>(nullptr), nsys,
                boltz2 * opts_.temp0, static_cast<const double *>(d.rndf.p), opts_.dt / opts_.tautp, c_ave,
@@ -2162,6 +2249,49 @@ int Batch::cg_poll(int *nactive, std::vector<int> *status, std::vector<double> *
     for (int s = 0; s < nsys; s++) (*energy)[s] = cg_host_[s].f;
   }
   return SFFG_OK;
+}
+
+int Batch::cg_export(int sys, CgCarry &c, void *stream) {
+  SFFG_SETTLE(stream);
+  if (!finalized_ || sys < 0 || sys >= num_systems() || !d_->cg_state.p) return SFFG_ESTATE;
+  DeviceState &d = *d_;
+  cudaStream_t st = pick(d, stream);
+  const size_t n = 3 * static_cast<size_t>(sys_[sys].natom), off = 3 * static_cast<size_t>(sys_[sys].atom_off);
+  c.x.resize(n);
+  c.g.resize(n);
+  c.w.resize(6 * n);
+  SFFG_CK(cudaMemcpyAsync(&c.st, d.cg_state.p + sys, sizeof(CgState), cudaMemcpyDeviceToHost, st));
+  SFFG_CK(cudaMemcpyAsync(c.x.data(), d.x.p + off, n * sizeof(double), cudaMemcpyDeviceToHost, st));
+  SFFG_CK(cudaMemcpyAsync(c.g.data(), d.grad.p + off, n * sizeof(double), cudaMemcpyDeviceToHost, st));
+  SFFG_CK(cudaMemcpyAsync(c.w.data(), d.cg_w.p + 6 * off, 6 * n * sizeof(double), cudaMemcpyDeviceToHost, st));
+  SFFG_CK(cudaStreamSynchronize(st));
+  return SFFG_OK;
+}
+
+int Batch::cg_import(int sys, const CgCarry &c, void *stream) {
+  SFFG_SETTLE(stream);
+  if (!finalized_ || sys < 0 || sys >= num_systems() || !d_->cg_state.p || cg_turn_ != 0) return SFFG_ESTATE;
+  const size_t n = 3 * static_cast<size_t>(sys_[sys].natom), off = 3 * static_cast<size_t>(sys_[sys].atom_off);
+  if (c.x.size() != n || c.g.size() != n || c.w.size() != 6 * n) {
+    last_error = "cg_import: state of another system size";
+    return SFFG_EINVAL;
+  }
+  DeviceState &d = *d_;
+  cudaStream_t st = pick(d, stream);
+  cg_host_[sys] = c.st;
+  SFFG_CK(cudaMemcpyAsync(d.cg_state.p + sys, &cg_host_[sys], sizeof(CgState), cudaMemcpyHostToDevice, st));
+  SFFG_CK(cudaMemcpyAsync(d.x.p + off, c.x.data(), n * sizeof(double), cudaMemcpyHostToDevice, st));
+  SFFG_CK(cudaMemcpyAsync(d.grad.p + off, c.g.data(), n * sizeof(double), cudaMemcpyHostToDevice, st));
+  SFFG_CK(cudaMemcpyAsync(d.cg_w.p + 6 * off, c.w.data(), 6 * n * sizeof(double), cudaMemcpyHostToDevice, st));
+  // the host vectors may go once this returns
+  SFFG_CK(cudaStreamSynchronize(st));
+  return SFFG_OK;
+}
+
+void Batch::adopt_split(const Batch &from) {
+  if (!from.tuned_) return;
+  for (int p = 0; p < 3; p++) cfg_[p] = from.cfg_[p];
+  tuned_ = true;
 }
 
 int Batch::set_restraints(int sys, const int *constrained, const double *x0) {

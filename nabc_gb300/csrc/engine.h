@@ -96,6 +96,13 @@ class Batch {
   int finalize();
   bool finalized() const { return finalized_; }
   int num_systems() const { return static_cast<int>(sys_.size()); }
+  // RATTLE constraints of system sys under the option rattle (0: none; 1: all
+  // bonds; 2: bonds to hydrogen)
+  int rattle_bonds(int sys) const {
+    return opts_.irattle == 0 ? 0
+           : opts_.irattle == 2 ? host_[sys].rattle_nh
+                                : static_cast<int>(host_[sys].rattle_bonds.size());
+  }
   const SystemInfo &system(int s) const { return sys_[s]; }
   const ModelParams &model() const { return mp_; }
   const Options &opts() const { return opts_; }
@@ -119,8 +126,9 @@ class Batch {
   // order, systems in order), the active flags, and every system's energy
   // components (13 each) with the whole gradient.
   int set_all_coords(const double *x, void *stream);
-  // Per system: SFFG_OK, or SFFG_ENONFINITE once an evaluation met a
-  // non-finite coordinate (cleared when its coordinates are set again).
+  // Per system: SFFG_OK; SFFG_ENONFINITE once an evaluation met a
+  // non-finite coordinate (cleared when its coordinates are set again);
+  // SFFG_ECONSTRAINT once RATTLE's sweeps reached their limit in md.
   int system_status(std::vector<int> &status, void *stream);
   // The md state of every system (coordinates, velocities, accelerations,
   // Berendsen factors) to or from a file.  load_state evaluates at the
@@ -194,6 +202,26 @@ class Batch {
   int cg_turns(int n, bool first_rebuild, void *stream, const std::function<int(int)> &after_eval = nullptr);
   int cg_poll(int *nactive, std::vector<int> *status, std::vector<double> *energy, void *stream);
   int cg_end(void *stream);
+  // Turns cg_turns has run since cg_begin.
+  int cg_turn() const { return cg_turn_; }
+  // Moving a running minimisation into another batch: cg_export reads one
+  // system's state machine, coordinates, gradient and work vectors
+  // (synchronous); cg_import writes them into system sys of a batch after
+  // its cg_begin and before its first turn.  The system continues
+  // bit for bit when the move happens where its own evaluation count is a
+  // multiple of nsnb (a list rebuild either way) and the receiving batch
+  // was built from the same topology and initial coordinates (which fix
+  // the atom order; host_system and initial_coords give them).
+  struct CgCarry {
+    CgState st;
+    std::vector<double> x, g, w;
+  };
+  int cg_export(int sys, CgCarry &c, void *stream);
+  int cg_import(int sys, const CgCarry &c, void *stream);
+  const HostSystem &host_system(int sys) const { return host_[sys]; }
+  const std::vector<double> &initial_coords(int sys) const { return x0_[sys]; }
+  // Takes another batch's tuned work split instead of tuning this one.
+  void adopt_split(const Batch &from);
   // True once a pair list has been built.
   bool have_list() const { return have_list_; }
 
@@ -228,9 +256,7 @@ class Batch {
   int settle_md(cudaStream_t st);
   int md_com_remove_direct(cudaStream_t st);
   void rebuild_list_b(void *stream);
-  ListArgs list_args(double fsmax);
-  double fsmax_all() const;
-  double smax_abs_ = 0.0;  // largest |s| = |fs (rborn - offset)| of the batch's atoms
+  ListArgs list_args();
   int run_eval(bool rebuild, void *stream);
   void collect_pass_times(DeviceState &d, long long max_evals);
   Options opts_;

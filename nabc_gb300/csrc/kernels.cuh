@@ -53,6 +53,11 @@ struct DevTables {
   const int *sys_active;
   const int *sys_lj_off;
   const int *sys_ntypes;
+  // (rgbmax + Fsmax)^2 with the system's own Fsmax (the reference skips a
+  // pair beyond it, eff.c:1649), and 1 where every rgbmax tail of the
+  // system has q = (rgbmax - d + s) / rgbmax <= 0.3, so that the polynomial
+  // form alone serves (passes 1 and 3)
+  const float2 *sys_born;
   const float2 *lj;       // (A, B) per type pair, per system blocks
   const double2 *lj64;    // the same table in FP64 (close pairs)
   int lj_n;               // entries of lj
@@ -317,6 +322,10 @@ __global__ void __launch_bounds__(256, 3) k_born(const DevTables t) {
   float3 cref = make_float3(0.f, 0.f, 0.f);
   float xi = 0, yi = 0, zi = 0, xil = 0, yil = 0, zil = 0, si = 0, si2 = 0, rbi = 0, sci = 0;
   int nki = 0;
+  // the i-tile's system: (rgbmax + Fsmax)^2 over its own atoms, and whether
+  // its rgbmax tails take the polynomial form
+  float cut2 = 0.0f;
+  bool tpoly = false;
   long long sumi64 = 0;
 
   // list B chunk k, rotation schedule
@@ -355,7 +364,7 @@ __global__ void __launch_bounds__(256, 3) k_born(const DevTables t) {
         float r2 = fmaf(dx, dx, fmaf(dy, dy, dz * dz));
         // off the list, or beyond rgbmax + Fsmax, where the reference skips
         // the pair (eff.c:1649)
-        r2 = in && r2 <= t.born.cutoff2 ? r2 : kOffList;
+        r2 = in && r2 <= cut2 ? r2 : kOffList;
         const float d1 = rsqrt_nr(r2);
         const float d2i = d1 * d1;
         const float cj = pb[u].x;
@@ -372,7 +381,7 @@ __global__ void __launch_bounds__(256, 3) k_born(const DevTables t) {
           // evaluated throughout
           const bool qi_ = dij > rgbmax - a.w, qj_ = dij > rgbmax - si;
           float vi, vj;
-          if (t.born.tail_poly_only) {
+          if (tpoly) {
             upk(tail_x2<false>(t.born, dij, d1, S), vi, vj);
           } else {
             vi = tail_closed<false>(t.born, dij, d1, a.w);
@@ -425,7 +434,7 @@ __global__ void __launch_bounds__(256, 3) k_born(const DevTables t) {
         const float dy = (hi.y - h.y) + (li.y - l.y);
         const float dz = (hi.z - h.z) + (li.z - l.z);
         const float r2 = fmaf(dx, dx, fmaf(dy, dy, dz * dz));
-        if (r2 <= t.born.cutoff2) {
+        if (r2 <= cut2) {
           const float d1 = rsqrt_nr(r2);
           const float dij = r2 * d1;
           ti = descreen(t.born, dij, r2, d1, gi.x, gp.y);
@@ -460,8 +469,12 @@ __global__ void __launch_bounds__(256, 3) k_born(const DevTables t) {
       int k;
       const bool nr = merged_item(m, nB, nC, k);
       const int I = SFFG_IDX(nr ? t.lc.chunk_i[k] : t.lb.chunk_i[k], t.ntile, kCheckTile);
-      if (!t.sys_active[t.tile_sys[I]]) continue;
+      const int sys = t.tile_sys[I];
+      if (!t.sys_active[sys]) continue;
       if (I != cur_I) {
+        const float2 sb = t.sys_born[sys];
+        cut2 = sb.x;
+        tpoly = sb.y != 0.0f;
         if (cur_I >= 0) atomic_add_ll(&t.acc_sumi[cur_I * 32 + lane], sumi64);
         cur_I = I;
         sumi64 = 0;
@@ -801,6 +814,10 @@ __global__ void __launch_bounds__(256, 3) k_chain(const DevTables t) {
   float3 cref = make_float3(0.f, 0.f, 0.f);
   float xi = 0, yi = 0, zi = 0, xil = 0, yil = 0, zil = 0, si = 0, si2 = 0, rbi = 0, sci = 0, sdai = 0;
   int nki = 0;
+  // the i-tile's system: (rgbmax + Fsmax)^2 over its own atoms, and whether
+  // its rgbmax tails take the polynomial form
+  float cut2 = 0.0f;
+  bool tpoly = false;
   long long fx64 = 0, fy64 = 0, fz64 = 0;
   auto flush_i = [&]() {
     const int sl = cur_I * 32 + lane;
@@ -856,7 +873,7 @@ __global__ void __launch_bounds__(256, 3) k_chain(const DevTables t) {
         float r2 = fmaf(dx, dx, fmaf(dy, dy, dz * dz));
         // off the list, or beyond rgbmax + Fsmax, where the reference skips
         // the pair (eff.c:2263)
-        r2 = in && r2 <= t.born.cutoff2 ? r2 : kOffList;
+        r2 = in && r2 <= cut2 ? r2 : kOffList;
         // the hardware rsqrt alone: pass 3 only shapes the forces
         const float d1 = rsqrt_ftz(r2);
         const float d2i = d1 * d1;
@@ -867,7 +884,7 @@ __global__ void __launch_bounds__(256, 3) k_chain(const DevTables t) {
         {
           const bool qi_ = dij > rgbmax - a.w, qj_ = dij > rgbmax - si;
           float vi, vj;
-          if (t.born.tail_poly_only) {
+          if (tpoly) {
             upk(tail_x2<true>(t.born, dij, d1, S), vi, vj);
           } else {
             vi = tail_closed<true>(t.born, dij, d1, a.w);
@@ -925,7 +942,7 @@ __global__ void __launch_bounds__(256, 3) k_chain(const DevTables t) {
         const float dy = (hi.y - h.y) + (li.y - l.y);
         const float dz = (hi.z - h.z) + (li.z - l.z);
         const float r2 = fmaf(dx, dx, fmaf(dy, dy, dz * dz));
-        if (r2 <= t.born.cutoff2) {
+        if (r2 <= cut2) {
           const float d1 = rsqrt_nr(r2);
           const float dij = r2 * d1;
           float di = descreen_deriv(t.born, dij, r2, d1, gi.x, gp.y);
@@ -972,8 +989,12 @@ __global__ void __launch_bounds__(256, 3) k_chain(const DevTables t) {
       int k;
       const bool nr = merged_item(m, nB, nC, k);
       const int I = SFFG_IDX(nr ? t.lc.chunk_i[k] : t.lb.chunk_i[k], t.ntile, kCheckTile);
-      if (!t.sys_active[t.tile_sys[I]]) continue;
+      const int sys = t.tile_sys[I];
+      if (!t.sys_active[sys]) continue;
       if (I != cur_I) {
+        const float2 sb = t.sys_born[sys];
+        cut2 = sb.x;
+        tpoly = sb.y != 0.0f;
         if (cur_I >= 0) flush_i();
         cur_I = I;
         fx64 = fy64 = fz64 = 0;

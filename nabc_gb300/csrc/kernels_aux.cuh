@@ -93,6 +93,7 @@ struct FinishArgs {
   long long *energy;
   const int *slot_atom, *tile_sys, *sys_active, *param;
   const double *rborn64, *q64, *alpha, *beta, *gamma;
+  const double2 *rinv64;  // per slot: 1 / (rborn - offset), 1 / rborn
   double *reff64, *psi64, *chainfac;
   float *reff32, *rinv2;
   int nslot, gb;
@@ -109,30 +110,38 @@ __global__ void k_born_finish(const FinishArgs a) {
   if (slot < a.nslot) {
     const int at = a.slot_atom[slot];
     if (at >= 0 && a.sys_active[sys]) {
+      // one FP64 division per atom (the reciprocal radii are static; GB300's
+      // FP64 divisions are slow): inv = 1 / reff
       const double rb = a.rborn64[slot], ri = rb - a.gboffset;
+      const double2 ir = a.rinv64[slot];
       const double sumi = -static_cast<double>(a.acc_sumi[slot]) * (1.0 / 1099511627776.0);
-      double reff, psi = 0.0, fac = 1.0;
+      double reff, inv, psi = 0.0, fac = 1.0;
       if (a.gb == 1) {
-        reff = 1.0 / (1.0 / ri + sumi);
-        if (reff < 0.0) reff = 30.0;
+        inv = ir.x + sumi;
+        reff = 1.0 / inv;
+        if (reff < 0.0) {
+          reff = 30.0;
+          inv = 1.0 / 30.0;
+        }
       } else {
         psi = -ri * sumi;
         const double al = a.alpha[slot], be = a.beta[slot], ga = a.gamma[slot];
         const double th = tanh((al - be * psi + ga * psi * psi) * psi);
-        reff = 1.0 / (1.0 / ri - th / rb);
-        fac = (al - 2.0 * be * psi + 3.0 * ga * psi * psi) * (1.0 - th * th) * ri / rb;
+        inv = ir.x - th * ir.y;
+        reff = 1.0 / inv;
+        fac = (al - 2.0 * be * psi + 3.0 * ga * psi * psi) * (1.0 - th * th) * (ri * ir.y);
       }
       a.reff64[slot] = reff;
       a.psi64[slot] = psi;
       a.chainfac[slot] = fac;
       a.reff32[slot] = static_cast<float>(reff);
-      a.rinv2[slot] = static_cast<float>(kLog2eQuarterSqrt / reff);
+      a.rinv2[slot] = static_cast<float>(kLog2eQuarterSqrt * inv);
       double sd = 0.0;
       if (!((a.param[slot] >> 24) & 1)) {
         const double qi = a.q64[slot];
-        const double expmkf = exp(-kKscale * a.kappa * reff) / a.epsext;
+        const double expmkf = (a.kappa != 0.0 ? exp(-kKscale * a.kappa * reff) : 1.0) / a.epsext;
         const double dielfac = 1.0 - expmkf, qi2h = 0.5 * qi * qi, qid2h = qi2h * dielfac;
-        ediag = -qid2h / reff;
+        ediag = -qid2h * inv;
         sd = qid2h - kKscale * a.kappa * qi2h * expmkf * reff;
       }
       a.acc_sd[slot] = __double2ll_rn(sd * 4294967296.0);
@@ -556,6 +565,10 @@ struct MdArgs {
   // system draws the same noise alone or in any batch
   const int *sys_atom_off;
   const unsigned long long *sys_key;
+  // RATTLE (null without): the coordinates before the drift, kept for the
+  // position sweeps; with it the kick leaves the kinetic energy to k_md_ekin,
+  // which runs after the velocity sweeps
+  double *xold;
 };
 
 // First half of a step (src/sff/sff.c:2243-2248): half-kick and drift.
@@ -569,6 +582,7 @@ __global__ void k_md_drift(const MdArgs a) {
   v = a.gammai == 0.0 ? (v + a.accel[i]) * a.tscal[sys] : a.c_explic * v + a.accel[i];
   v = fmin(a.vlimit, fmax(-a.vlimit, v));
   a.v[i] = v;
+  if (a.xold) a.xold[i] = a.x[i];
   a.x[i] += v * a.dtx;
 }
 
@@ -614,6 +628,7 @@ __global__ void k_md_kick(const MdArgs a, int init) {
       ek = v * v / minv;
     }
   }
+  if (a.xold && !init) return;  // k_md_ekin sums it after the velocity sweeps
   // kinetic energy per system, fixed point; warps of one system use one atomic
   const long long t = __double2ll_rn(ek * 4294967296.0);
   const int s0 = __shfl_sync(kFull, sys, 0);
@@ -623,6 +638,142 @@ __global__ void k_md_kick(const MdArgs a, int init) {
   } else if (sys >= 0) {
     atomic_add_ll(&a.ekin[sys], t);
   }
+}
+
+// Kinetic energy per system after RATTLE's velocity sweeps (sff.c:2294-2306),
+// summed as k_md_kick sums it.
+__global__ void k_md_ekin(const MdArgs a) {
+  pdl_wait();
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  int sys = -1;
+  double ek = 0.0;
+  if (i < a.n3) {
+    sys = a.atom_sys[i / 3];
+    if (!a.sys_active[sys]) {
+      sys = -1;
+    } else {
+      const double v = a.v[i];
+      ek = v * v / a.minv[i];
+    }
+  }
+  const long long t = __double2ll_rn(ek * 4294967296.0);
+  const int s0 = __shfl_sync(kFull, sys, 0);
+  if (__all_sync(kFull, sys == s0 || sys < 0)) {
+    const long long tt = warp_sum_ll(sys >= 0 ? t : 0);
+    if ((threadIdx.x & 31) == 0 && s0 >= 0) atomic_add_ll(&a.ekin[s0], tt);
+  } else if (sys >= 0) {
+    atomic_add_ll(&a.ekin[sys], t);
+  }
+}
+
+// ------------------------------------------------------------------ RATTLE
+// Bond-length constraints (src/sff/rattle.c, after TINKER): Gauss-Seidel
+// sweeps over the constrained bonds in the topology's order until no bond
+// needs a correction.  One block per system.  The bonds of a system are
+// grouped by level: a bond's level is one more than the highest level of
+// the earlier bonds (in the reference's order) that share an atom with it,
+// so the bonds of one level share no atom and run in parallel, and every
+// atom sees its corrections in the reference's order: the sweeps give the
+// sequential loop's values bit for bit.  The arithmetic is written with
+// round-to-nearest intrinsics in the reference's order of operations (no
+// contraction into FMA).  A system whose sweeps reach the reference's limit
+// (1,000, an error there) gets its status word set and its loop ends.
+struct RattleArgs {
+  double *x, *v;
+  const double *xold, *minv;
+  const int2 *atoms;      // coordinate offsets (3 * atom) of each bond's two atoms
+  const double *req;      // bond lengths
+  const int *level;       // start of each level's bonds (levels of all systems, then the end)
+  const int *sys_level;   // per system: its first level (nsys + 1 entries)
+  const int *sys_active;
+  int *status;            // per system: 1 once a sweep loop hit its limit
+  double dt;              // time step (the integrator's units)
+  double eps;             // tolerance: positions (float) 1e-7, velocities 1e-7 / dt
+};
+
+constexpr int kRattleThreads = 128;
+
+// One bond of the position sweep (rattle.c:55-97); true if it was corrected.
+__device__ __forceinline__ bool rattle_bond_pos(const RattleArgs &a, int k) {
+  const int2 ab = a.atoms[k];
+  const int i = ab.x, j = ab.y;
+  double *x = a.x, *v = a.v;
+  const double xr = __dsub_rn(x[j], x[i]), yr = __dsub_rn(x[j + 1], x[i + 1]), zr = __dsub_rn(x[j + 2], x[i + 2]);
+  const double dist2 = __dadd_rn(__dadd_rn(__dmul_rn(xr, xr), __dmul_rn(yr, yr)), __dmul_rn(zr, zr));
+  const double req = a.req[k];
+  const double delta = __dsub_rn(__dmul_rn(req, req), dist2);
+  if (!(fabs(delta) > a.eps)) return false;
+  const double xo = __dsub_rn(a.xold[j], a.xold[i]), yo = __dsub_rn(a.xold[j + 1], a.xold[i + 1]),
+               zo = __dsub_rn(a.xold[j + 2], a.xold[i + 2]);
+  const double dot = __dadd_rn(__dadd_rn(__dmul_rn(xr, xo), __dmul_rn(yr, yo)), __dmul_rn(zr, zo));
+  double ra = a.minv[i], rb = a.minv[j];
+  const double term = __ddiv_rn(__dmul_rn(1.2, delta), __dmul_rn(__dmul_rn(2.0, __dadd_rn(ra, rb)), dot));
+  const double tx = __dmul_rn(xo, term), ty = __dmul_rn(yo, term), tz = __dmul_rn(zo, term);
+  x[i] = __dsub_rn(x[i], __dmul_rn(tx, ra));
+  x[i + 1] = __dsub_rn(x[i + 1], __dmul_rn(ty, ra));
+  x[i + 2] = __dsub_rn(x[i + 2], __dmul_rn(tz, ra));
+  x[j] = __dadd_rn(x[j], __dmul_rn(tx, rb));
+  x[j + 1] = __dadd_rn(x[j + 1], __dmul_rn(ty, rb));
+  x[j + 2] = __dadd_rn(x[j + 2], __dmul_rn(tz, rb));
+  ra = __ddiv_rn(ra, a.dt);
+  rb = __ddiv_rn(rb, a.dt);
+  v[i] = __dsub_rn(v[i], __dmul_rn(tx, ra));
+  v[i + 1] = __dsub_rn(v[i + 1], __dmul_rn(ty, ra));
+  v[i + 2] = __dsub_rn(v[i + 2], __dmul_rn(tz, ra));
+  v[j] = __dadd_rn(v[j], __dmul_rn(tx, rb));
+  v[j + 1] = __dadd_rn(v[j + 1], __dmul_rn(ty, rb));
+  v[j + 2] = __dadd_rn(v[j + 2], __dmul_rn(tz, rb));
+  return true;
+}
+
+// One bond of the velocity sweep (rattle2, rattle.c:137-172).
+__device__ __forceinline__ bool rattle_bond_vel(const RattleArgs &a, int k) {
+  const int2 ab = a.atoms[k];
+  const int i = ab.x, j = ab.y;
+  const double *x = a.x;
+  double *v = a.v;
+  const double xr = __dsub_rn(x[j], x[i]), yr = __dsub_rn(x[j + 1], x[i + 1]), zr = __dsub_rn(x[j + 2], x[i + 2]);
+  const double xv = __dsub_rn(v[j], v[i]), yv = __dsub_rn(v[j + 1], v[i + 1]), zv = __dsub_rn(v[j + 2], v[i + 2]);
+  const double dot = __dadd_rn(__dadd_rn(__dmul_rn(xr, xv), __dmul_rn(yr, yv)), __dmul_rn(zr, zv));
+  const double ra = a.minv[i], rb = a.minv[j], req = a.req[k];
+  const double term = __ddiv_rn(__dmul_rn(-dot, 1.2), __dmul_rn(__dmul_rn(__dadd_rn(ra, rb), req), req));
+  if (!(fabs(term) > a.eps)) return false;
+  const double tx = __dmul_rn(xr, term), ty = __dmul_rn(yr, term), tz = __dmul_rn(zr, term);
+  v[i] = __dsub_rn(v[i], __dmul_rn(tx, ra));
+  v[i + 1] = __dsub_rn(v[i + 1], __dmul_rn(ty, ra));
+  v[i + 2] = __dsub_rn(v[i + 2], __dmul_rn(tz, ra));
+  v[j] = __dadd_rn(v[j], __dmul_rn(tx, rb));
+  v[j + 1] = __dadd_rn(v[j + 1], __dmul_rn(ty, rb));
+  v[j + 2] = __dadd_rn(v[j + 2], __dmul_rn(tz, rb));
+  return true;
+}
+
+// VEL = false: rattle() on the positions (and the velocities with them);
+// VEL = true: rattle2() on the velocities.
+template <bool VEL>
+__global__ void __launch_bounds__(kRattleThreads) k_rattle(const RattleArgs a) {
+  pdl_wait();
+  const int s = blockIdx.x;
+  if (!a.sys_active[s]) return;
+  const int l0 = a.sys_level[s], l1 = a.sys_level[s + 1];
+  if (l0 == l1) return;
+  __shared__ int s_done;
+  int niter = 0;
+  bool done = false;
+  while (!done && niter < 1000) {
+    niter++;
+    if (threadIdx.x == 0) s_done = 1;
+    __syncthreads();
+    for (int L = l0; L < l1; L++) {
+      const int k1 = a.level[L + 1];
+      for (int k = a.level[L] + static_cast<int>(threadIdx.x); k < k1; k += kRattleThreads)
+        if (VEL ? rattle_bond_vel(a, k) : rattle_bond_pos(a, k)) s_done = 0;
+      __syncthreads();
+    }
+    done = s_done != 0;
+    __syncthreads();
+  }
+  if (niter >= 999 && threadIdx.x == 0) a.status[s] = 1;
 }
 
 }  // namespace sffg

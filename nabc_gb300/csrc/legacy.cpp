@@ -511,9 +511,9 @@ extern "C" INT_T md(INT_T n, INT_T maxstep, REAL_T *x, REAL_T *f, REAL_T *v,
                     REAL_T (*func)(REAL_T *, REAL_T *, INT_T *)) {
   Session &s = session();
   const double t0 = wall_seconds();
-  // RATTLE's sweeps run on the host, so md with bond constraints takes the
-  // host loop (each evaluation still on the device)
-  if (func != &sffg::mme || !s.batch || n != 3 * s.natom || options().irattle) {
+  // another energy function, coordinates that are not the session's, or a
+  // rattle option set after the session's batch was made take the host loop
+  if (func != &sffg::mme || !s.batch || n != 3 * s.natom || options().irattle != s.batch->opts().irattle) {
     const int rc = md_host(n, maxstep, x, f, v, func);
     timers().md += wall_seconds() - t0;
     return rc;
@@ -524,7 +524,8 @@ extern "C" INT_T md(INT_T n, INT_T maxstep, REAL_T *x, REAL_T *f, REAL_T *v,
   Batch &b = *s.batch;
   int nfrozen = 0;
   for (int i = 0; s.frozen && i < s.natom; i++) nfrozen += s.frozen[i] != 0;
-  const double rndf = n - 3.0 * nfrozen, ekin0 = boltz2 * rndf * o.temp0, dttp = o.dt / o.tautp;
+  // RATTLE's constraints take one degree of freedom each (sff.c:2142-2146)
+  const double rndf = n - 3.0 * nfrozen - b.rattle_bonds(0), ekin0 = boltz2 * rndf * o.temp0, dttp = o.dt / o.tautp;
   const double gammai = o.gamma_ln / 20.455;
   // initial velocities (sff.c:2165-2188), drawn from the shared stream
   double ekin = 0.0;
@@ -582,6 +583,11 @@ extern "C" INT_T md(INT_T n, INT_T maxstep, REAL_T *x, REAL_T *f, REAL_T *v,
       check(b.md_set_tscal(ts, nullptr), "md");
     }
     check(b.md_steps(step, next - step, noise, nullptr, nullptr, !com_after), "md");
+    if (o.irattle) {
+      std::vector<int> st;
+      check(b.system_status(st, nullptr), "md");
+      if (st[0] == SFFG_ECONSTRAINT) fatal("ERROR in RATTLE");
+    }
     t += o.dt * (next - step);
     step = next;
     std::vector<double> ek;

@@ -76,7 +76,7 @@ struct ListArgs {
   int ntile;
   float cut2f;   // cut^2 (list A), FP32
   double cut2;   // cut^2, exact FP64 decision for borderline pairs
-  float gbb2f;   // (rgbmax + Fsmax + skin)^2 (lists B and C)
+  const float *sys_gbb2;  // per system (rgbmax + Fsmax + skin)^2, its own Fsmax (lists B and C)
   float close2f; // (kClose + 1 A)^2: list A's possibly close pairs
   // candidates
   int2 *cand;
@@ -223,7 +223,7 @@ __global__ void k_list_columns(const ListArgs a) {
   __syncwarp();
   const unsigned prevA = GB_ONLY ? a.colA[static_cast<size_t>(c) * 32 + lane] : 0u;
   unsigned colA = 0, colB = 0, colC = 0, colE = 0, colK = 0;
-  const float gbb = a.gbb2f * 1.0001f + 1e-3f;
+  const float gbb = a.sys_gbb2[a.tile_sys[I]] * 1.0001f + 1e-3f;
   // rows to test (warp-uniform): every valid i-atom, or for a remake only
   // those with a list-A pair in this tile pair
   unsigned rows = prevA;

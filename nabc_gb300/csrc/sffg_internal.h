@@ -41,6 +41,7 @@ struct Options {
   int sffg_tune = 1;            // autotune the pair passes' work split
   int sffg_lj_shared = 1;       // pass 2 reads small Lennard-Jones tables from shared memory
   int sffg_warps = 8;           // warps per CTA for the pair kernels (0 = tuned)
+  int sffg_serve_classes = 0;   // serving: one minimisation group per size class (1) or one for all (0)
   int sffg_verbose = 0;
 };
 
@@ -195,6 +196,11 @@ struct HostSystem {
   struct Angle { int a, b, c; double tk, teq; };
   struct Pair14 { int a, b; double scee, scnb, c12, c6; int pow10; };
   std::vector<Bond> bonds;
+  // RATTLE's bond list (src/sff/rattle.c:41-53): the bonds to hydrogen, then
+  // the others, in the topology's order, none left out; rattle_nh of them
+  // are bonds to hydrogen
+  std::vector<Bond> rattle_bonds;
+  int rattle_nh = 0;
   std::vector<Angle> angles;
   std::vector<DihTerm> dihedrals;
   std::vector<Pair14> pairs14;

@@ -161,6 +161,11 @@ void build_host_system(PARMSTRUCT_T *prm, const int *frozen, const Options &o, b
   };
   add_bonds(prm->Nbonh, prm->BondHAt1, prm->BondHAt2, prm->BondHNum);
   add_bonds(prm->Mbona, prm->BondAt1, prm->BondAt2, prm->BondNum);
+  for (int i = 0; i < prm->Nbonh; i++)
+    hs.rattle_bonds.push_back({prm->BondHAt1[i] / 3, prm->BondHAt2[i] / 3, 0.0, prm->Req[prm->BondHNum[i] - 1]});
+  for (int i = 0; i < prm->Mbona; i++)
+    hs.rattle_bonds.push_back({prm->BondAt1[i] / 3, prm->BondAt2[i] / 3, 0.0, prm->Req[prm->BondNum[i] - 1]});
+  hs.rattle_nh = prm->Nbonh;
   auto add_angles = [&](int na, const int *a1, const int *a2, const int *a3, const int *t) {
     for (int i = 0; i < na; i++) {
       int a = a1[i] / 3, b = a2[i] / 3, c = a3[i] / 3, ty = t[i] - 1;

@@ -25,6 +25,8 @@ def _proto(L):
                                      C.POINTER(C.c_double)]
     L.sffg_server_device_bytes.argtypes = [vp]
     L.sffg_server_device_bytes.restype = C.c_size_t
+    L.sffg_server_counts.argtypes = [vp, C.POINTER(C.c_longlong), C.POINTER(C.c_longlong), C.POINTER(C.c_longlong),
+                                     C.POINTER(C.c_double)]
     L.sffg_server_error.argtypes = [vp]
     L.sffg_server_error.restype = C.c_char_p
     L.sffg_server_destroy.argtypes = [vp]
@@ -34,8 +36,11 @@ def _proto(L):
 
 class Server:
     """Requests wait in arrival order; every pump() admits those that fit
-    the memory budget as a new group, advances all running groups by
-    `turns` evaluations or md steps (their work overlaps on the GPU) and
+    the memory budget -- a minimisation into the running minimisation group
+    (joining that batch at its next list-rebuild turn) or a new group, md
+    requests as a new group -- launches `turns` evaluations or md
+    steps of every group whose earlier turns have finished (the groups'
+    work overlaps on the GPU), waits until one group's turns finish and
     takes the results of systems that ended."""
 
     def __init__(self, opts, memory_budget_gb=150.0, max_groups=8):
@@ -76,6 +81,15 @@ class Server:
 
     def device_bytes(self):
         return self.L.sffg_server_device_bytes(self.h)
+
+    def counts(self):
+        """Groups started, joins, requests that joined a running group, and
+        the host milliseconds spent forming batches."""
+        v = [C.c_longlong(0) for _ in range(3)]
+        ms = C.c_double(0.0)
+        self._check(self.L.sffg_server_counts(self.h, *[C.byref(a) for a in v], C.byref(ms)), "counts")
+        return {"groups_started": v[0].value, "joins": v[1].value, "joined_requests": v[2].value,
+                "form_ms": ms.value}
 
     def run(self, turns=16):
         """Pumps until no request runs or waits."""

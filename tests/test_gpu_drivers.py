@@ -35,6 +35,51 @@ def test_batch_equals_individual(lib):
     b.close()
 
 
+def test_batch_mixed_screens_equals_individual(lib, oracle_mod):
+    """Systems with different screened radii in one batch.  Each system's
+    rgbmax + Fsmax cutoff (eff.c:1520), its list-B radius and the form of
+    its rgbmax tails follow its own atoms, so a system's result is
+    bit-identical alone and batched with a system of larger screens, and
+    each matches the FP64 oracle.  With rgbmax 10 the plain molecule's
+    largest screened radius (1.28 A) lets every tail take the polynomial
+    form; the scaled one's (1.79 A) does not."""
+    from nabc_gb300 import sff
+    from nabc_gb300.batch import Batch
+    from test_gpu_parity import assert_close
+    opts = "gb=5, cut=30.0, rgbmax=10.0"
+    mols = [sff.synth_molecule(n, 900 + n) for n in (300, 520)]
+    prm1 = mols[1][0]
+    n1 = prm1.contents.Natom
+    fs = np.ctypeslib.as_array(prm1.contents.Fs, shape=(n1,))
+    rb = np.ctypeslib.as_array(prm1.contents.Rborn, shape=(n1,))
+    fs *= 1.4
+    prm1.contents.Fsmax = float(np.max(fs * (rb - 0.09)))
+    assert prm1.contents.Fsmax > mols[0][0].contents.Fsmax + 0.4
+    alone = []
+    for prm, x, _ in mols:
+        b = Batch(opts)
+        b.add(prm, x)
+        b.finalize()
+        b.eval(rebuild=True)
+        alone.append((b.energy(0), b.grad(0)))
+        b.close()
+        o = oracle_mod.Oracle(prm, opts)
+        e0, ene0, g0, reff0 = o.mme(x)
+        assert_close(alone[-1][0], alone[-1][1], None, ene0, g0, reff0)
+    for order in ((0, 1), (1, 0)):
+        b = Batch(opts)
+        for k in order:
+            b.add(mols[k][0], mols[k][1])
+        b.finalize()
+        b.eval(rebuild=True)
+        for s, k in enumerate(order):
+            assert np.array_equal(b.energy(s), alone[k][0])
+            assert np.array_equal(b.grad(s), alone[k][1])
+        b.close()
+    for prm, _, _ in mols:
+        sff.free_prm(prm)
+
+
 def test_legacy_mme_matches_oracle(lib, oracle_mod, checks):
     """mm_options + mme_init_sff + mme(iter=-1), the reference's drop-in path."""
     from nabc_gb300 import sff
@@ -421,3 +466,47 @@ def test_variable_14_scaling(lib, checks):
         assert b[idx] == pytest.approx(c["sp"][k], abs=1e-6 * tot), k
     assert e == pytest.approx(c["sp"]["Total"], abs=1e-6 * tot)
     assert round(e, 2) == c["ff"][0][1]
+
+
+@pytest.mark.parametrize("rattle", [1, 2])
+def test_batched_md_rattle(lib, rattle):
+    """Batched md with RATTLE on the device (rattle=1: all bonds, 2: bonds to
+    hydrogen).  After the run every constrained bond has the length the
+    position sweeps hold it to (|req^2 - r^2| within the reference's
+    tolerance, 1e-7 A^2, at the last sweep), the bonds left free do not,
+    every system ends with status OK, and each system's trajectory is
+    bit-identical alone and batched (Berendsen coupling, no noise: a
+    batch's default noise key is the system's index)."""
+    from nabc_gb300 import sff
+    from nabc_gb300.batch import Batch
+    opts = f"gb=1, cut=999.0, rgbmax=15.0, dt=0.002, gamma_ln=0.0, temp0=300.0, tempi=0.0, rattle={rattle}"
+    mols = [sff.synth_molecule(n, 60 + n) for n in (150, 420)]
+    nsteps = 30
+
+    def run(idx):
+        b = Batch(opts)
+        for k in idx:
+            b.add(mols[k][0], mols[k][1])
+        b.finalize()
+        b.md(nsteps)
+        out = [(b.coords(s), b.velocities(s)) for s in range(len(idx))]
+        assert list(b.status()) == [0] * len(idx)
+        b.close()
+        return out
+
+    alone = [run([k])[0] for k in range(len(mols))]
+    both = run([0, 1])
+    for (x, v), (xa, va) in zip(both, alone):
+        assert np.array_equal(x, xa) and np.array_equal(v, va)
+    for (prm, x0, _), (x, _) in zip(mols, both):
+        p = prm.contents
+        nh, na = p.Nbonh, p.Mbona
+        bonds = [(p.BondHAt1[i] // 3, p.BondHAt2[i] // 3, p.Req[p.BondHNum[i] - 1]) for i in range(nh)]
+        heavy = [(p.BondAt1[i] // 3, p.BondAt2[i] // 3, p.Req[p.BondNum[i] - 1]) for i in range(na)]
+        held = bonds + (heavy if rattle == 1 else [])
+        xr = x.reshape(-1, 3)
+        dev = [abs(req * req - ((xr[a] - xr[b]) ** 2).sum()) for a, b, req in held]
+        assert max(dev) < 2e-7, max(dev)
+        if rattle == 2 and heavy:
+            free = [abs(req * req - ((xr[a] - xr[b]) ** 2).sum()) for a, b, req in heavy]
+            assert max(free) > 1e-4

@@ -71,6 +71,11 @@ def test_gb8_radii_known_answer(lib, checks):
     (97, "gb=8, cut=999.0, rgbmax=25.0"),
     (2000, "gb=1, cut=999.0, rgbmax=15.0"),        # the 2,000-atom all-pairs workload
     (3000, "gb=5, cut=25.0, rgbmax=15.0"),         # cutoff list with partial tile pairs
+    # rgbmax below 2 max(s) / 0.3: rgbmax tails with q > 0.3 take the
+    # logarithmic form instead of the polynomial one
+    (520, "gb=5, cut=20.0, rgbmax=6.0"),
+    (520, "gb=1, cut=20.0, rgbmax=6.0"),
+    (520, "gb=8, cut=20.0, rgbmax=6.0"),
 ])
 def test_sizes_and_lists(lib, oracle_mod, natom, opts):
     from nabc_gb300 import sff
