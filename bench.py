@@ -369,6 +369,7 @@ def bench_serving(args):
     sizes = np.floor(np.exp(rng.uniform(np.log(500), np.log(args.serve_max_atoms), n))).astype(int)
     mols = make_molecules(sizes, 12000)
     out = {"requests": n, "atoms_log_uniform": [500, args.serve_max_atoms], "options": SERVE_OPTS,
+           "groups": "one per size class" if args.serve_classes else "one minimisation group",
            "rmsgrad": 0.01, "maxiter": args.serve_maxiter, "memory_budget_gb": 150.0}
     # plain: one request at a time
     t0 = time.perf_counter()
@@ -387,7 +388,8 @@ def bench_serving(args):
     rates = []
     for rate in args.serve_rates:
         arrive = np.cumsum(rng.exponential(1.0 / rate, n))
-        s = Server(SERVE_OPTS, memory_budget_gb=150.0, max_groups=16)
+        s = Server(SERVE_OPTS + (", sffg_serve_classes=1" if args.serve_classes else ""), memory_budget_gb=150.0,
+                   max_groups=16)
         ids = [None] * n
         t0 = time.perf_counter()
         k = 0
@@ -593,6 +595,8 @@ def main():
     ap.add_argument("--serve-max-atoms", type=int, default=50000, help="requests log-uniform in 500 .. this")
     ap.add_argument("--serve-maxiter", type=int, default=2000, help="conjgrad evaluation limit per request")
     ap.add_argument("--serve-rates", type=float, nargs="*", default=[10.0, 100.0, 1000.0, 2000.0])
+    ap.add_argument("--serve-classes", action="store_true",
+                    help="serving: one minimisation group per size class (option sffg_serve_classes=1)")
     ap.add_argument("--uneven-md", type=int, default=0, help="with --only uneven: md steps of the whole batch")
     ap.add_argument("--only", choices=["serving", "batched", "uneven"],
                     help="run only this section and print its JSON (for profiling it alone)")
@@ -671,6 +675,7 @@ def main():
 
     ev = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(args.steps)]
     launches0 = b.launches()
+    overflows0 = sff.lib().sffg_list_overflows()
     with ClockSampler(local) as clk:
         torch.cuda.synchronize()
         for k in range(args.steps):
@@ -681,6 +686,7 @@ def main():
             step += 1
         torch.cuda.synchronize()
     launches = b.launches() - launches0
+    overflows = sff.lib().sffg_list_overflows() - overflows0
     split = b.tuned_split()
     step_ms = [a.elapsed_time(c) for a, c in ev]
     total_ms = sum(step_ms)
@@ -784,6 +790,8 @@ def main():
         "latency_ms": {"p50": ms_sorted[len(ms_sorted) // 2],
                        "p99": ms_sorted[min(len(ms_sorted) - 1, int(0.99 * len(ms_sorted)))]},
         "accuracy_vs_fp64": err,
+        "step_ms": [round(v, 4) for v in step_ms],
+        "list_store_overflows_in_timed_steps": int(overflows),
         "tuned_split_claim_blocks": split,
         "md_long": md_long,
         "roofline": {"bound": "fp32", "kernel": PASS_NAMES[dom], "achieved": passes[dom]["fp32_tflops"],

@@ -393,6 +393,7 @@ int Batch::upload() {
     // a tail pair has q = (rgbmax - d + s_j) / rgbmax <= 2 |s_j| / rgbmax
     const double rc = mp_.rgbmax + si.fsmax;
     sys_born[s] = make_float2(static_cast<float>(rc * rc), 2.0 * smax <= 0.3 * mp_.rgbmax * 0.999 ? 1.0f : 0.0f);
+    if (sys_born[s].y == 0.0f) tail_poly_all_ = false;
     sys_gbb2[s] = static_cast<float>(std::min(list_b_cut2(mp_, si.fsmax), 1e30));
     sys_natom[s] = n;
     sys_atom_off[s] = si.atom_off;
@@ -647,9 +648,9 @@ int Batch::upload() {
   SFFG_CK(cudaMemcpy(d.tscal.p, onesd.data(), nsys * sizeof(double), cudaMemcpyHostToDevice));
   {
     const bool neck = mp_.gb == 7 || mp_.gb == 8;
-    occ_[0] = born_blocks_per_sm(neck);
+    occ_[0] = born_blocks_per_sm(neck, tail_poly_all_);
     occ_[1] = gbpair_blocks_per_sm(mp_.kappa != 0.0);
-    occ_[2] = chain_blocks_per_sm(neck);
+    occ_[2] = chain_blocks_per_sm(neck, tail_poly_all_);
     for (int p = 0; p < 3; p++) {
       cfg_[p].claim = 4;
       cfg_[p].blocks = occ_[p] * d.nsm;
@@ -1273,10 +1274,29 @@ int Batch::settle(void *stream) {
   return settle_md(pick(*d_, stream));
 }
 
+// The pinned counter buffer, its event and the md snapshot of queued list
+// builds, made once before the first such build (a pinned allocation takes
+// milliseconds and must not fall inside a step).
+int Batch::prepare_queued_builds() {
+  DeviceState &d = *d_;
+  if (!d.list_ev) SFFG_CK(cudaEventCreateWithFlags(&d.list_ev, cudaEventDisableTiming));
+  if (!d.list_host) SFFG_CK(cudaHostAlloc(reinterpret_cast<void **>(&d.list_host), 16 * sizeof(int), cudaHostAllocDefault));
+  const size_t n3 = 3 * static_cast<size_t>(natom_total_);
+  if (d.ck_x.n < n3) {
+    SFFG_CK(d.ck_x.alloc(n3));
+    SFFG_CK(d.ck_v.alloc(n3));
+    SFFG_CK(d.ck_accel.alloc(n3));
+  }
+  if (d.ck_tscal.n < d.tscal.n) SFFG_CK(d.ck_tscal.alloc(d.tscal.n));
+  if (d.ck_ekin_last.n < d.ekin_last.n) SFFG_CK(d.ck_ekin_last.alloc(d.ekin_last.n));
+  return SFFG_OK;
+}
+
 int Batch::eval_checked(bool rebuild, void *stream) {
   int rc = settle(stream);
   if (rc) return rc;
   if (!rebuild || !sized_ || !finalized_) return eval(rebuild, stream);
+  if ((rc = prepare_queued_builds())) return rc;
   queued_builds_ = true;
   rc = eval(true, stream);
   queued_builds_ = false;
@@ -1501,7 +1521,7 @@ int Batch::run_eval_direct(bool rebuild, void *stream) {
     if (tuning_) SFFG_CK(cudaEventRecord(d.tune_ev[0][0], st));
     {
       Range range("pass 1 Born radii");
-      launch_born(neck, cfg_[0].blocks, st, t);
+      launch_born(neck, tail_poly_all_, cfg_[0].blocks, st, t);
     }
     if (tuning_) SFFG_CK(cudaEventRecord(d.tune_ev[0][1], st));
     SFFG_CK(cudaGetLastError());
@@ -1561,7 +1581,7 @@ int Batch::run_eval_direct(bool rebuild, void *stream) {
     if (tuning_) SFFG_CK(cudaEventRecord(d.tune_ev[2][0], st));
     {
       Range range("pass 3 chain rule");
-      launch_chain(neck, cfg_[2].blocks, st, t);
+      launch_chain(neck, tail_poly_all_, cfg_[2].blocks, st, t);
     }
     if (tuning_) SFFG_CK(cudaEventRecord(d.tune_ev[2][1], st));
     SFFG_CK(cudaGetLastError());
@@ -1745,6 +1765,7 @@ int Batch::md_begin(bool rebuild, NoiseFn noise, void *noise_ctx, void *stream) 
     if ((rc = upload_noise(*this, d, noise, noise_ctx, st, h))) return rc;
     a.noise = d.noise.p;
   }
+  if ((rc = prepare_queued_builds())) return rc;
   SFFG_CK(cudaMemsetAsync(d.ekin.p, 0, d.ekin.bytes(), st));
   SFFG_CK(cudaMemsetAsync(d.step.p, 0, sizeof(unsigned), st));
   const int nb = (a.n3 + 255) / 256;

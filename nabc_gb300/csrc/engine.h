@@ -252,6 +252,7 @@ class Batch {
               const std::function<int(cudaStream_t)> &body);
   int build_lists(void *stream);
   int build_lists_queued(cudaStream_t st);
+  int prepare_queued_builds();
   int resolve_list_check(bool *overflowed);
   int settle_md(cudaStream_t st);
   int md_com_remove_direct(cudaStream_t st);
@@ -272,6 +273,9 @@ class Batch {
   };
   PassCfg cfg_[3];
   int occ_[3] = {1, 1, 1};
+  // every system takes the polynomial rgbmax tail: passes 1 and 3 launch the
+  // instantiation without the logarithmic form
+  bool tail_poly_all_ = true;
   bool tuned_ = false, tuning_ = false;
   // conjgrad driver state (host copies of the device state machines)
   std::vector<CgState> cg_host_;

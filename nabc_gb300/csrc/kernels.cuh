@@ -293,7 +293,10 @@ __device__ __forceinline__ float far_deriv2(float d2i, float s, float s2) {
 // tail and neck term of it is an exact zero.
 constexpr float kOffList = 1.0e30f;
 
-template <bool NECK>
+// POLY: every system of the batch takes the polynomial rgbmax tail
+// (2 max|s| <= 0.3 rgbmax); the logarithmic form is then left out of the
+// code, which keeps it out of the hot loop's registers.
+template <bool NECK, bool POLY>
 __global__ void __launch_bounds__(256, 3) k_born(const DevTables t) {
   // far-field chunks (list B): per warp the entries twice, (x, y, z
   // relative to the i-tile's reference point, s) and (s correction, s^2,
@@ -381,7 +384,7 @@ __global__ void __launch_bounds__(256, 3) k_born(const DevTables t) {
           // evaluated throughout
           const bool qi_ = dij > rgbmax - a.w, qj_ = dij > rgbmax - si;
           float vi, vj;
-          if (tpoly) {
+          if (POLY || tpoly) {
             upk(tail_x2<false>(t.born, dij, d1, S), vi, vj);
           } else {
             vi = tail_closed<false>(t.born, dij, d1, a.w);
@@ -402,8 +405,10 @@ __global__ void __launch_bounds__(256, 3) k_born(const DevTables t) {
             const int ij = SFFG_IDX(nki * 21 + nkj, 441, kCheckNeck), ji = SFFG_IDX(nkj * 21 + nki, 441, kCheckNeck);
             const float na = neck_term(dij, s_npos[ij], s_nval[ij], t.neck_scale);
             const float nb = neck_term(dij, s_npos[ji], s_nval[ji], t.neck_scale);
-            ti += nk ? na : 0.0f;
-            tj += nk ? nb : 0.0f;
+            // the reference adds the neck term only to pairs it has not
+            // skipped as beyond rgbmax + s (eff.c:1663-1664, 1699-1707)
+            ti += nk && dij <= rgbmax + a.w ? na : 0.0f;
+            tj += nk && dij <= rgbmax + si ? nb : 0.0f;
           }
         }
         acc_i += ti;
@@ -437,14 +442,16 @@ __global__ void __launch_bounds__(256, 3) k_born(const DevTables t) {
         if (r2 <= cut2) {
           const float d1 = rsqrt_nr(r2);
           const float dij = r2 * d1;
-          ti = descreen(t.born, dij, r2, d1, gi.x, gp.y);
-          tj = descreen(t.born, dij, r2, d1, gp.x, gi.y);
+          ti = descreen<!POLY>(t.born, dij, r2, d1, gi.x, gp.y);
+          tj = descreen<!POLY>(t.born, dij, r2, d1, gp.x, gi.y);
           ti = fmaf(ti, gp.w, ti);
           tj = fmaf(tj, gi.w, tj);
           if (NECK && dij < gi.z + gp.z + 6.8f) {
             const int nkp = (si_par[w][il] >> 16) & 0xff, nkj = (sm_par[w][jl] >> 16) & 0xff;
-            ti += neck_term(dij, s_npos[SFFG_IDX(nkp * 21 + nkj, 441, kCheckNeck)], s_nval[SFFG_IDX(nkp * 21 + nkj, 441, kCheckNeck)], t.neck_scale);
-            tj += neck_term(dij, s_npos[SFFG_IDX(nkj * 21 + nkp, 441, kCheckNeck)], s_nval[SFFG_IDX(nkj * 21 + nkp, 441, kCheckNeck)], t.neck_scale);
+            if (dij <= t.born.rgbmax + gp.y)
+              ti += neck_term(dij, s_npos[SFFG_IDX(nkp * 21 + nkj, 441, kCheckNeck)], s_nval[SFFG_IDX(nkp * 21 + nkj, 441, kCheckNeck)], t.neck_scale);
+            if (dij <= t.born.rgbmax + gi.y)
+              tj += neck_term(dij, s_npos[SFFG_IDX(nkj * 21 + nkp, 441, kCheckNeck)], s_nval[SFFG_IDX(nkj * 21 + nkp, 441, kCheckNeck)], t.neck_scale);
           }
         }
       }
@@ -784,7 +791,7 @@ __global__ void __launch_bounds__(256, 3) k_gbpair(const DevTables t) {
 // Chain rule through the Born radii (src/sff/eff.c:2241-2395) over lists
 // B and C: for each pair within rgbmax + Fsmax, g = sumda_i d_ij +
 // sumda_j d_ji, f_i -= g r_ij, f_j += g r_ij.
-template <bool NECK>
+template <bool NECK, bool POLY>
 __global__ void __launch_bounds__(256, 3) k_chain(const DevTables t) {
   // far-field chunks (list B): per warp the entries twice, (x, y, z
   // relative to the i-tile's reference point, s) and (s correction, s^2,
@@ -884,7 +891,7 @@ __global__ void __launch_bounds__(256, 3) k_chain(const DevTables t) {
         {
           const bool qi_ = dij > rgbmax - a.w, qj_ = dij > rgbmax - si;
           float vi, vj;
-          if (tpoly) {
+          if (POLY || tpoly) {
             upk(tail_x2<true>(t.born, dij, d1, S), vi, vj);
           } else {
             vi = tail_closed<true>(t.born, dij, d1, a.w);
@@ -904,8 +911,9 @@ __global__ void __launch_bounds__(256, 3) k_chain(const DevTables t) {
             const int ij = SFFG_IDX(nki * 21 + nkj, 441, kCheckNeck), ji = SFFG_IDX(nkj * 21 + nki, 441, kCheckNeck);
             const float na = neck_deriv(dij, s_npos[ij], s_nval[ij], t.neck_scale);
             const float nb = neck_deriv(dij, s_npos[ji], s_nval[ji], t.neck_scale);
-            di += nk ? na : 0.0f;
-            dj += nk ? nb : 0.0f;
+            // only for pairs within rgbmax + s (eff.c:2288-2289, 2330-2345)
+            di += nk && dij <= rgbmax + a.w ? na : 0.0f;
+            dj += nk && dij <= rgbmax + si ? nb : 0.0f;
           }
         }
         const float gg = fmaf(sdai, di, b.z * dj);
@@ -945,14 +953,16 @@ __global__ void __launch_bounds__(256, 3) k_chain(const DevTables t) {
         if (r2 <= cut2) {
           const float d1 = rsqrt_nr(r2);
           const float dij = r2 * d1;
-          float di = descreen_deriv(t.born, dij, r2, d1, gi.x, gp.y);
-          float dj = descreen_deriv(t.born, dij, r2, d1, gp.x, gi.y);
+          float di = descreen_deriv<!POLY>(t.born, dij, r2, d1, gi.x, gp.y);
+          float dj = descreen_deriv<!POLY>(t.born, dij, r2, d1, gp.x, gi.y);
           di = fmaf(di, gp.w, di);
           dj = fmaf(dj, gi.w, dj);
           if (NECK && dij < gi.z + gp.z + 6.8f) {
             const int nkp = (si_par[w][il] >> 16) & 0xff, nkj = (sm_par[w][jl] >> 16) & 0xff;
-            di += neck_deriv(dij, s_npos[SFFG_IDX(nkp * 21 + nkj, 441, kCheckNeck)], s_nval[SFFG_IDX(nkp * 21 + nkj, 441, kCheckNeck)], t.neck_scale);
-            dj += neck_deriv(dij, s_npos[SFFG_IDX(nkj * 21 + nkp, 441, kCheckNeck)], s_nval[SFFG_IDX(nkj * 21 + nkp, 441, kCheckNeck)], t.neck_scale);
+            if (dij <= t.born.rgbmax + gp.y)
+              di += neck_deriv(dij, s_npos[SFFG_IDX(nkp * 21 + nkj, 441, kCheckNeck)], s_nval[SFFG_IDX(nkp * 21 + nkj, 441, kCheckNeck)], t.neck_scale);
+            if (dij <= t.born.rgbmax + gi.y)
+              dj += neck_deriv(dij, s_npos[SFFG_IDX(nkj * 21 + nkp, 441, kCheckNeck)], s_nval[SFFG_IDX(nkj * 21 + nkp, 441, kCheckNeck)], t.neck_scale);
           }
           const float gg = fmaf(li.w, di, l.w * dj);
           gx = gg * dx;

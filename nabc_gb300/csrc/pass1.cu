@@ -3,15 +3,25 @@
 
 namespace sffg {
 
-void launch_born(bool neck, int grid, cudaStream_t st, const DevTables &t) {
-  if (neck) launch_pdl(k_born<true>, grid, 256, st, t);
-  else launch_pdl(k_born<false>, grid, 256, st, t);
+void launch_born(bool neck, bool poly, int grid, cudaStream_t st, const DevTables &t) {
+  if (neck) {
+    if (poly) launch_pdl(k_born<true, true>, grid, 256, st, t);
+    else launch_pdl(k_born<true, false>, grid, 256, st, t);
+  } else {
+    if (poly) launch_pdl(k_born<false, true>, grid, 256, st, t);
+    else launch_pdl(k_born<false, false>, grid, 256, st, t);
+  }
 }
 
-int born_blocks_per_sm(bool neck) {
+int born_blocks_per_sm(bool neck, bool poly) {
   int occ = 0;
-  if (neck) cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, k_born<true>, 256, 0);
-  else cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, k_born<false>, 256, 0);
+  if (neck) {
+    if (poly) cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, k_born<true, true>, 256, 0);
+    else cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, k_born<true, false>, 256, 0);
+  } else {
+    if (poly) cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, k_born<false, true>, 256, 0);
+    else cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, k_born<false, false>, 256, 0);
+  }
   return occ > 0 ? occ : 1;
 }
 

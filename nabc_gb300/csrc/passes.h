@@ -29,13 +29,13 @@ cudaError_t launch_pdl(void (*k)(P...), dim3 grid, dim3 block, cudaStream_t st, 
 }
 
 // grid: 256-thread blocks of the persistent kernel.
-void launch_born(bool neck, int grid, cudaStream_t st, const DevTables &t);
+void launch_born(bool neck, bool poly, int grid, cudaStream_t st, const DevTables &t);
 void launch_gbpair(bool kappa, int grid, cudaStream_t st, const DevTables &t);
-void launch_chain(bool neck, int grid, cudaStream_t st, const DevTables &t);
+void launch_chain(bool neck, bool poly, int grid, cudaStream_t st, const DevTables &t);
 // Resident 256-thread blocks per SM of each pair kernel.
-int born_blocks_per_sm(bool neck);
+int born_blocks_per_sm(bool neck, bool poly);
 int gbpair_blocks_per_sm(bool kappa);
-int chain_blocks_per_sm(bool neck);
+int chain_blocks_per_sm(bool neck, bool poly);
 // The checked build's error word of each pass's translation unit (0 when
 // no check failed, and always 0 in the normal build).
 int pass1_check_code();

@@ -269,7 +269,13 @@ class Server {
     Group &g = *gp;
     g.kind = kind;
     g.cls = cls;
-    if (cudaStreamCreateWithFlags(&g.stream, cudaStreamNonBlocking) != cudaSuccess ||
+    // with size classes, smaller classes get higher stream priority: where a
+    // larger group's kernel ends, the device starts their waiting kernels first
+    int least = 0, greatest = 0;
+    if (cudaDeviceGetStreamPriorityRange(&least, &greatest) != cudaSuccess) least = greatest = 0;
+    const int prio = kind == SFFG_REQ_MINIMIZE && opts_.sffg_serve_classes ? std::max(greatest, least - (6 - std::min(cls, 6)))
+                                                                          : least;
+    if (cudaStreamCreateWithPriority(&g.stream, cudaStreamNonBlocking, prio) != cudaSuccess ||
         cudaEventCreateWithFlags(&g.ev, cudaEventDisableTiming) != cudaSuccess) {
       release(g);
       err = "stream creation failed";
