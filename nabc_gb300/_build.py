@@ -69,15 +69,20 @@ def _compile(src, obj, force):
     return r.stderr
 
 
-def build(force=False, verbose=False):
-    """Compile every translation unit and link libsffg.so; returns its path."""
+def build(force=False, verbose=False, report=False):
+    """Compile every translation unit and link libsffg.so; returns its path.
+    report: print which translation units were compiled (the others were up
+    to date), for which architecture, and where the library is."""
     os.makedirs(OUT, exist_ok=True)
     srcs = sorted(glob.glob(os.path.join(CSRC, "*.cu")) + glob.glob(os.path.join(CSRC, "*.cpp")))
     objs = [os.path.join(OUT, os.path.basename(s) + ".o") for s in srcs]
+    compiled = []
     with cf.ThreadPoolExecutor(max_workers=min(8, os.cpu_count() or 1)) as ex:
         futs = [ex.submit(_compile, s, o, force) for s, o in zip(srcs, objs)]
-        for f in futs:
+        for s, f in zip(srcs, futs):
             msg = f.result()
+            if msg is not None:
+                compiled.append(os.path.basename(s))
             if verbose and msg:
                 print(msg)
     lib = os.path.join(OUT, "libsffg.so")
@@ -86,6 +91,11 @@ def build(force=False, verbose=False):
         r = subprocess.run(cmd, capture_output=True, text=True)
         if r.returncode != 0:
             raise RuntimeError(f"link failed: {' '.join(cmd)}\n{r.stdout}\n{r.stderr}")
+        if report:
+            print(f"libsffg: linked {lib}")
+    if report:
+        print(f"libsffg: compiled {len(compiled)} of {len(srcs)} translation units for {ARCH[1]}"
+              f"{': ' + ', '.join(compiled) if compiled else ' (all up to date)'}")
     return lib
 
 
