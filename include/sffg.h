@@ -246,9 +246,11 @@ int sffg_server_submit(sffg_server *s, PARMSTRUCT_T *prm, const double *x, int k
  * and the requests waiting. */
 int sffg_server_pump(sffg_server *s, int turns, int *nrunning, int *npending);
 /* The result of a finished request: the driver's return code (conjgrad's,
- * or the steps run for md), final energy, coordinates (3*Natom, may be
- * NULL) and the time from submission to the end, in ms.  SFFG_ESTATE while
- * it runs or waits. */
+ * or the steps run for md; SFFG_ENONFINITE when its coordinates turned
+ * non-finite; another negative SFFG status, with a NaN energy, when the
+ * batch it was to run in could not be formed), final energy, coordinates
+ * (3*Natom, may be NULL) and the time from submission to the end, in ms.
+ * SFFG_ESTATE while it runs or waits. */
 int sffg_server_result(sffg_server *s, long long id, int *status, double *energy, double *x, double *latency_ms);
 /* Device memory the running groups hold (bytes). */
 size_t sffg_server_device_bytes(const sffg_server *s);

@@ -285,6 +285,8 @@ class Server {
     for (long long id : take) est += reqs_[id]->bytes;
     const int rc = form(g, {}, take, est, err);
     if (rc) {
+      for (long long id : take) fail_request(id, rc);
+      in_use_ -= std::min(in_use_, est);
       release(g);
       return rc;
     }
@@ -404,11 +406,33 @@ class Server {
     joined += static_cast<long long>(take.size());
     const size_t est = g.joiner_bytes;
     g.joiner_bytes = 0;
-    return form(g, carried, take, est, err);
+    const int rc = form(g, carried, take, est, err);
+    if (rc) {
+      // the group's old batch is gone: its running requests and the
+      // joiners end with the failure's status, and collect() drops it
+      for (auto &c : carried) fail_request(c.first, rc);
+      for (long long id : take) fail_request(id, rc);
+      g.batch.reset();
+      g.ids.clear();
+      g.finished.clear();
+      in_use_ -= std::min(in_use_, g.bytes + est);
+      g.bytes = 0;
+    }
+    return rc;
+  }
+
+  void fail_request(long long id, int status) {
+    Request &r = *reqs_[id];
+    if (r.done) return;
+    r.status = status;
+    r.energy = std::nan("");
+    r.t_done = now_ms();
+    r.done = true;
   }
 
   int launch(Group &g, int turns, std::string &err) {
     int rc = SFFG_OK;
+    if (!g.batch) return SFFG_OK;
     if (g.kind == SFFG_REQ_MINIMIZE) {
       const int nsnb = std::max(1, opts_.nsnb);
       if (!g.joiners.empty()) {
@@ -453,6 +477,11 @@ class Server {
       Group &g = *groups_[gi];
       if (g.in_flight) {
         gi++;
+        continue;
+      }
+      if (!g.batch) {  // a join that failed
+        release(g);
+        groups_.erase(groups_.begin() + gi);
         continue;
       }
       const int nsys = static_cast<int>(g.ids.size());
