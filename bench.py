@@ -24,6 +24,19 @@ evaluation plus the integrator update, device-resident.
 Both arms print the same "config": the workload, its options, the
 generator's realised radius and density and the pair counts.
 
+Further keys of the same line (--no-batched skips the batched and serving
+sections; --only serving|batched|uneven runs one section alone):
+  md_long   --md-long steps (10,000) of the workload back to back: ns/day
+  small_md  the 2,000-atom all-pairs case (gb=1, cut 999, 1,000 Langevin
+            steps at dt 1 fs) on the GPU and through the CPU restatement
+  batched   the uneven-size batch (2,048 molecules of 200-20,000 atoms,
+            gb=8), 512 conformers of a 3,000-atom molecule (evaluations,
+            conjgrad, XMIN L-BFGS) and batched LMOD searches, each against
+            the same systems one at a time
+  serving   a Poisson stream of minimisation requests (500-50,000 atoms,
+            conjgrad to RMS 0.01 or 2,000 evaluations) at 10, 100, 1,000 and
+            2,000 requests/s through the server, against one at a time
+
 Multi-GPU (--gpus N under torchrun): independent replicas (the path has
 no data exchange between systems), value = total evaluations/s; scaling
 weak.

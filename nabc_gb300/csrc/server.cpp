@@ -251,24 +251,30 @@ class Server {
       in_use_ += r.bytes;
     }
     pending_.swap(keep);
+    // every new group is started even if one fails (its requests then end
+    // with the failure's status); the first failure is reported
+    int first_rc = SFFG_OK;
     for (auto &kv : fresh_min) {
-      int rc = start_group(SFFG_REQ_MINIMIZE, kv.first, kv.second, err);
-      if (rc) return rc;
+      const int rc = start_group(SFFG_REQ_MINIMIZE, kv.first, kv.second, err);
+      if (rc && first_rc == SFFG_OK) first_rc = rc;
     }
     if (!fresh_md.empty()) {
-      int rc = start_group(SFFG_REQ_MD, 0, fresh_md, err);
-      if (rc) return rc;
+      const int rc = start_group(SFFG_REQ_MD, 0, fresh_md, err);
+      if (rc && first_rc == SFFG_OK) first_rc = rc;
     }
-    return SFFG_OK;
+    return first_rc;
   }
 
   // A new group of the given requests (their estimated bytes already in
-  // in_use_).
+  // in_use_).  On a failure the requests end with its status and their
+  // bytes return to the budget.
   int start_group(int kind, int cls, const std::vector<long long> &take, std::string &err) {
     auto gp = std::make_unique<Group>();
     Group &g = *gp;
     g.kind = kind;
     g.cls = cls;
+    size_t est = 0;
+    for (long long id : take) est += reqs_[id]->bytes;
     // with size classes, smaller classes get higher stream priority: where a
     // larger group's kernel ends, the device starts their waiting kernels first
     int least = 0, greatest = 0;
@@ -277,12 +283,12 @@ class Server {
                                                                           : least;
     if (cudaStreamCreateWithPriority(&g.stream, cudaStreamNonBlocking, prio) != cudaSuccess ||
         cudaEventCreateWithFlags(&g.ev, cudaEventDisableTiming) != cudaSuccess) {
+      for (long long id : take) fail_request(id, SFFG_ECUDA);
+      in_use_ -= std::min(in_use_, est);
       release(g);
       err = "stream creation failed";
       return SFFG_ECUDA;
     }
-    size_t est = 0;
-    for (long long id : take) est += reqs_[id]->bytes;
     const int rc = form(g, {}, take, est, err);
     if (rc) {
       for (long long id : take) fail_request(id, rc);
