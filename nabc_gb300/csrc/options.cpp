@@ -185,7 +185,6 @@ const std::vector<Key> &keys() {
       {"sffg_graph", choice(&Options::sffg_graph, {0, 1})},
       {"sffg_tune", choice(&Options::sffg_tune, {0, 1})},
       {"sffg_lj_shared", choice(&Options::sffg_lj_shared, {0, 1})},
-      {"sffg_warps", choice(&Options::sffg_warps, {0, 4, 8, 16})},
       {"sffg_serve_classes", choice(&Options::sffg_serve_classes, {0, 1})},
       {"sffg_verbose", choice(&Options::sffg_verbose, {0, 1})},
   };

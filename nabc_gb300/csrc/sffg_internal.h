@@ -40,7 +40,6 @@ struct Options {
   int sffg_graph = 1;           // capture the md/cg step in a CUDA graph
   int sffg_tune = 1;            // autotune the pair passes' work split
   int sffg_lj_shared = 1;       // pass 2 reads small Lennard-Jones tables from shared memory
-  int sffg_warps = 8;           // warps per CTA for the pair kernels (0 = tuned)
   int sffg_serve_classes = 0;   // serving: one minimisation group per size class (1) or one for all (0)
   int sffg_verbose = 0;
 };
