@@ -406,7 +406,8 @@ def main():
                           "niter": 3, "nmod": 5, "kmod": 3, "mc_option": 2, "nof_lmod_steps": 5, "seed": 99,
                           "grms_tol": 1e-4, "maxiter": 2000, "glob_min": float(m.group(1)),
                           "error_flag": int(m.group(2)), "nconf": int(m.group(3)), "iteration_energies": iters,
-                          "log": out.split("lmod returns")[0]}
+                          # the log names the topology file: kept relative to the repository
+                          "log": out.split("lmod returns")[0].replace(os.path.dirname(ROOT) + os.sep, "")}
     shutil.rmtree(work)
     os.remove(tmp)
     with open(os.path.join(HERE, "checks.json"), "w") as f:

@@ -1,7 +1,7 @@
 """GPU parity: the sm_103a kernels against the FP64 oracle on the
 reference's own test systems and on synthetic molecules.
 
-Tolerances (the spec bar): total energy within 1e-6 relative, every
+Tolerances (the accuracy bar of this path): total energy within 1e-6 relative, every
 component within 1e-6 of the total energy's magnitude (Coulomb and
 Lennard-Jones totals are small differences of large terms, so their FP32
 error scales with the system, not with the component), RMS gradient
